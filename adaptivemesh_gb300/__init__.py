@@ -1,0 +1,154 @@
+"""adaptivemesh_gb300 -- GB300 (sm_103a) implementation of AdaptiveMesh's per-timestep hot path.
+
+The compute path is the C-ABI library libamr_gb300.so (include/amr_gb300.h): hand-written CUDA
+kernels plus the C++ host octree and the reference's two plugins.  This module loads it with
+ctypes and mirrors the reference's interfaces for Python callers (tests, benchmarks):
+
+  Octree  -- AMR<T>'s host octree (AdaptiveMesh/AMR.h:118-294)
+  Sim     -- a plugin (BSSN_AMR_data, BSSN.h:104-171, or wave_AMR_data, SimpleWave.h:191-279)
+             with its timestep loop (AMR.h:324-333)
+  ops     -- one function per reference operator (AMR.h:880-1310, BSSN.h:24-102,
+             SimpleWave.h:48-150) on caller-owned device buffers
+
+There is no CPU fallback: if the library is missing or fails to load, import-time use raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+OK = 0
+ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_DEVICE, ERR_CAPACITY = 1, 2, 3, 4, 5
+SIM_BSSN, SIM_WAVE = 1, 2
+MODE_PLAIN, MODE_BATCHED, MODE_GRAPH = 0, 1, 2
+CHRISTOFFEL_REFERENCE, CHRISTOFFEL_RAISED = 0, 1
+
+VP = ctypes.c_void_p
+U32, I32, U64 = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64
+
+
+class Config(ctypes.Structure):
+    """amr_config: the reference's domain constants (AMR.h:9-20) as run-time values."""
+    _fields_ = [("size_domain", U32), ("padding_domain", U32), ("outer_size", ctypes.c_float)]
+
+    def __init__(self, size_domain: int = 28, padding_domain: int = 2, outer_size: float = 100.0):
+        super().__init__(size_domain, padding_domain, outer_size)
+
+    @property
+    def total(self) -> int:
+        return self.size_domain + 2 * self.padding_domain
+
+    @property
+    def padded_cells(self) -> int:
+        return self.total ** 3
+
+    @property
+    def inner_cells(self) -> int:
+        return self.size_domain ** 3
+
+
+CP = ctypes.POINTER(Config)
+
+EXPORTS = {
+    "amr_version": (ctypes.c_char_p, []),
+    "amr_config_supported": (ctypes.c_int, [CP]),
+    "amr_last_cuda_error": (ctypes.c_int, []),
+    "amr_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "amr_cf3_encode": (ctypes.c_int, [VP, VP, U64, VP, VP]),
+    "amr_cf3_decode": (ctypes.c_int, [VP, U64, VP, VP]),
+    "amr_differentiate": (ctypes.c_int, [CP, VP, VP, VP, VP, U32, U32, U32, I32, VP]),
+    "amr_mixed_partials": (ctypes.c_int, [CP, VP, VP, VP, U32, U32, U32, I32, VP]),
+    "amr_deriv_trace": (ctypes.c_int, [CP, VP, VP, VP, VP, VP, U32, U32, U32, VP]),
+    "amr_christoffel": (ctypes.c_int, [CP, VP, VP, I32, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
+    "amr_copy_boundaries": (ctypes.c_int, [CP, VP, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
+    "amr_copy_new_to_old": (ctypes.c_int, [CP, VP, VP, VP, VP, U32, U32, U32, VP]),
+    "amr_copy_to_child": (ctypes.c_int, [CP, VP, U32, I32, I32, VP]),
+    "amr_wave_predictor": (ctypes.c_int, [CP, VP, VP, VP, VP, VP, U32, U32, U32, VP]),
+    "amr_wave_corrector": (ctypes.c_int, [CP, VP, VP, VP, VP, VP, U32, U32, U32, VP]),
+    "amr_criterion": (ctypes.c_int, [CP, VP, VP, VP, VP, U32, U32, U32, VP]),
+    "amr_octree_create": (ctypes.c_int, [U32, ctypes.POINTER(VP)]),
+    "amr_octree_destroy": (ctypes.c_int, [VP]),
+    "amr_octree_add_node": (ctypes.c_int, [VP, I32, I32]),
+    "amr_octree_remove_node": (ctypes.c_int, [VP, I32]),
+    "amr_octree_increment_timer": (ctypes.c_int, [VP]),
+    "amr_octree_find_node_idx": (U32, [VP, U32, U32]),
+    "amr_octree_state": (ctypes.c_int, [VP, VP, VP, VP, VP, VP, VP]),
+    "amr_sim_create": (ctypes.c_int, [CP, ctypes.c_int, U32, ctypes.c_int, ctypes.POINTER(VP)]),
+    "amr_sim_destroy": (ctypes.c_int, [VP]),
+    "amr_sim_set_mode": (ctypes.c_int, [VP, ctypes.c_int]),
+    "amr_sim_add_node": (ctypes.c_int, [VP, I32, I32]),
+    "amr_sim_remove_node": (ctypes.c_int, [VP, I32]),
+    "amr_sim_octree_state": (ctypes.c_int, [VP, VP, VP, VP, VP, VP, VP]),
+    "amr_sim_buffer": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(VP), ctypes.POINTER(U64)]),
+    "amr_sim_timestep": (ctypes.c_int, [VP]),
+    "amr_sim_copy_bounds": (ctypes.c_int, [VP]),
+    "amr_sim_rng": (ctypes.c_int, [VP, ctypes.POINTER(I32)]),
+    "amr_sim_set_rng": (ctypes.c_int, [VP, I32]),
+    "amr_sim_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
+    "amr_sim_synchronize": (ctypes.c_int, [VP]),
+    "amr_sim_kernel_launches": (U64, [VP]),
+    "amr_sim_enable_kernel_timing": (ctypes.c_int, [VP, ctypes.c_int]),
+    "amr_sim_kernel_timing": (ctypes.c_int, [VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(U64)]),
+}
+
+_LIB = None
+
+
+class AmrError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        lib = _LIB
+        msg = lib.amr_status_string(status).decode() if lib else str(status)
+        cuda = lib.amr_last_cuda_error() if lib else 0
+        super().__init__(f"{what}: {msg} (status {status}, last CUDA error {cuda})")
+        self.status = status
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libamr_gb300.so (compiling it first if it is absent and nvcc is available)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH) and build_if_missing:
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run adaptivemesh_gb300.build.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != OK:
+        raise AmrError(status, what)
+
+
+def _p(t) -> int:
+    """Address of a torch tensor / numpy array / int / None."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def _ptr_array(ts) -> ctypes.Array:
+    arr = (VP * len(ts))()
+    for i, t in enumerate(ts):
+        arr[i] = _p(t)
+    return arr
+
+
+from . import ops  # noqa: E402
+from .octree import Octree, Sim  # noqa: E402
+
+__all__ = ["Config", "Octree", "Sim", "ops", "load", "check", "AmrError", "LIB_PATH", "EXPORTS"]

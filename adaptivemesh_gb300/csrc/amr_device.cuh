@@ -1,0 +1,206 @@
+// amr_device.cuh -- device building blocks shared by the GB300 kernels.
+//
+// Compiled with -fmad=false -ftz=true: every fused multiply-add below is written out
+// (__fmaf_rn) and every other product/sum is rounded on its own, so the arithmetic is the
+// operation sequence the reference's fast-math device build performs (pinned against that
+// build's outputs by the tests), and subnormals flush to zero as they do there.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "amr_types.h"
+
+namespace amr {
+
+// ------------------------------------------------------------------ fast_prng (tensors.h:276-304)
+__device__ __forceinline__ int32_t prng_next(int32_t& s) {
+    uint32_t v = (uint32_t)s + 1124781675u;
+    v ^= (uint32_t)((int32_t)v >> 7);
+    v *= 1246477263u;
+    s = (int32_t)v;
+    return s;
+}
+__device__ __forceinline__ float prng_float(int32_t& s) {
+    return __fmul_rn(__int2float_rn(prng_next(s)), 2.3283064E-10f);
+}
+// Per-cell generator of the stencil kernels, keyed by (launch seed, x, y, slot*N + z)
+// (AMR.h:1160-1162, BSSN.h:64-66).
+__device__ __forceinline__ int32_t cell_rng(int32_t seed, uint32_t x, uint32_t y, uint32_t zg) {
+    int32_t s = (int32_t)((uint32_t)seed + x * 2178614u);
+    int32_t g = prng_next(s);
+    s = (int32_t)((uint32_t)s ^ ((uint32_t)g * y));
+    g = prng_next(s);
+    s = (int32_t)((uint32_t)s ^ ((uint32_t)g * zg));
+    return s;
+}
+
+// ------------------------------------------------------------------ compressed_float3 (tensors.h:305-394)
+// word = E<<27 | s3<<26 | m3<<18 | s2<<17 | m2<<9 | s1<<8 | m1 ;  value_i = (1 - 2 s_i) m_i 2^(E-22)
+__device__ __forceinline__ uint32_t cf3_quantise_one(float v, uint32_t mpos, uint32_t spos) {
+    const float c = fmaxf(-255.f, fminf(v, 255.f));
+    return (__float2uint_rz(__fadd_rn(fabsf(c), .5f)) << mpos) | ((uint32_t)(c < 0.f) << spos);
+}
+template <bool STOCHASTIC>
+__device__ __forceinline__ uint32_t cf3_encode_impl(float x, float y, float z, int32_t& rng) {
+    const uint32_t ex = (__float_as_uint(x) >> 23) & 255u;
+    const uint32_t ey = (__float_as_uint(y) >> 23) & 255u;
+    const uint32_t ez = (__float_as_uint(z) >> 23) & 255u;
+    const uint32_t E = min(max(max(ex, max(ey, ez)), 112u) - 112u, 31u);
+    const float scale = __uint_as_float((149u - E) << 23);          // 2^(22-E), exact
+    x = __fmul_rn(x, scale);
+    y = __fmul_rn(y, scale);
+    z = __fmul_rn(z, scale);
+    if (STOCHASTIC) {
+        x = __fmaf_rn(prng_float(rng), .95f, x);
+        y = __fmaf_rn(prng_float(rng), .95f, y);
+        z = __fmaf_rn(prng_float(rng), .95f, z);
+    }
+    return (E << 27) | cf3_quantise_one(x, 0u, 8u) | cf3_quantise_one(y, 9u, 17u) | cf3_quantise_one(z, 18u, 26u);
+}
+__device__ __forceinline__ uint32_t cf3_encode(float x, float y, float z, int32_t& rng) {
+    return cf3_encode_impl<true>(x, y, z, rng);
+}
+__device__ __forceinline__ uint32_t cf3_encode_det(float x, float y, float z) {
+    int32_t unused = 0;
+    return cf3_encode_impl<false>(x, y, z, unused);
+}
+// Exact: m * 2^(E-22) is representable, the sign bit is applied last (so m = 0 keeps its sign).
+__device__ __forceinline__ float cf3_component(uint32_t w, uint32_t mpos, uint32_t spos) {
+    const float scale = __uint_as_float((105u + (w >> 27)) << 23);  // 2^(E-22)
+    const float m = __uint2float_rn((w >> mpos) & 255u);
+    return __uint_as_float(__float_as_uint(__fmul_rn(m, scale)) | (((w >> spos) & 1u) << 31));
+}
+__device__ __forceinline__ float3 cf3_decode(uint32_t w) {
+    return make_float3(cf3_component(w, 0u, 8u), cf3_component(w, 9u, 17u), cf3_component(w, 18u, 26u));
+}
+
+// ------------------------------------------------------------------ fast-math primitives
+// The reference is built with --use_fast_math; its divisions and square roots are the
+// hardware approximations, which these wrappers issue directly.
+__device__ __forceinline__ float rcp_approx(float a) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx(float a) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+
+// ------------------------------------------------------------------ symmetric 3x3 algebra (tensors.h:133-244)
+// Stored as s[0..5] = xx, xy, xz, yy, yz, zz.
+struct Sym { float xx, xy, xz, yy, yz, zz; };
+
+__device__ __forceinline__ float sym_determinant(const Sym& m) {          // tensors.h:208-210
+    float d = __fmul_rn(__fmul_rn(-m.xz, m.yy), m.xz);
+    d = __fmaf_rn(__fmul_rn(m.xy, m.yz), m.xz, d);
+    d = __fmaf_rn(__fmul_rn(m.xz, m.xy), m.yz, d);
+    d = __fmaf_rn(-__fmul_rn(m.xx, m.yz), m.yz, d);
+    d = __fmaf_rn(-__fmul_rn(m.xy, m.xy), m.zz, d);
+    d = __fmaf_rn(__fmul_rn(m.xx, m.yy), m.zz, d);
+    return d;
+}
+// Cofactor inverse (tensors.h:211-225).  The products shared with the determinant stay rounded.
+__device__ __forceinline__ Sym sym_inverse(const Sym& m) {
+    Sym r;
+    r.xx = __fmaf_rn(m.yy, m.zz, -__fmul_rn(m.yz, m.yz));
+    r.xy = __fmaf_rn(m.yz, m.xz, -__fmul_rn(m.xy, m.zz));
+    r.xz = __fsub_rn(__fmul_rn(m.xy, m.yz), __fmul_rn(m.yy, m.xz));
+    r.yy = __fmaf_rn(m.xx, m.zz, -__fmul_rn(m.xz, m.xz));
+    r.yz = __fsub_rn(__fmul_rn(m.xy, m.xz), __fmul_rn(m.xx, m.yz));
+    r.zz = __fsub_rn(__fmul_rn(m.xx, m.yy), __fmul_rn(m.xy, m.xy));
+    const float inv_det = rcp_approx(sym_determinant(m));
+    r.xx = __fmul_rn(r.xx, inv_det); r.xy = __fmul_rn(r.xy, inv_det); r.xz = __fmul_rn(r.xz, inv_det);
+    r.yy = __fmul_rn(r.yy, inv_det); r.yz = __fmul_rn(r.yz, inv_det); r.zz = __fmul_rn(r.zz, inv_det);
+    return r;
+}
+// c^ij m_ij for symmetric c, m (tensors.h:241-244)
+__device__ __forceinline__ float trace_contra(const Sym& c, const Sym& m) {
+    float a = __fmaf_rn(c.xx, m.xx, __fmul_rn(c.yy, m.yy));
+    a = __fmaf_rn(c.zz, m.zz, a);
+    float b = __fmaf_rn(c.xy, m.xy, __fmul_rn(c.xz, m.xz));
+    b = __fmaf_rn(c.yz, m.yz, b);
+    return __fmaf_rn(b, 2.f, a);
+}
+// m * v (tensors.h:201-206)
+__device__ __forceinline__ float3 sym_times(const Sym& m, float3 a) {
+    return make_float3(__fmaf_rn(a.z, m.xz, __fmaf_rn(a.x, m.xx, __fmul_rn(a.y, m.xy))),
+                       __fmaf_rn(a.z, m.yz, __fmaf_rn(a.x, m.xy, __fmul_rn(a.y, m.yy))),
+                       __fmaf_rn(a.z, m.zz, __fmaf_rn(a.x, m.xz, __fmul_rn(a.y, m.yz))));
+}
+__device__ __forceinline__ Sym sym_from_cf3(uint32_t diag, uint32_t off) {   // tensors.h:430-435
+    const float3 d = cf3_decode(diag), o = cf3_decode(off);
+    return Sym{d.x, o.x, o.y, d.y, o.z, d.z};
+}
+
+// ------------------------------------------------------------------ octree words (AMR.h:22-100)
+__device__ __forceinline__ int pos_depth(uint32_t pos) { return (~pos) ? (int)(pos >> 27) : -1; }
+__device__ __forceinline__ bool active_depth(uint32_t substep, uint32_t depth, uint32_t max_depth) {
+    return (substep & ((1u << (max_depth - depth)) - 1u)) == 0u;
+}
+__device__ __forceinline__ int32_t bd_target(uint64_t b) {
+    const uint32_t nd = (uint32_t)b;
+    return (int32_t)((nd & 16777215u) | ((nd & (1u << 23)) ? 4278190080u : 0u));
+}
+__device__ __forceinline__ uint32_t bd_depth_diff(uint64_t b) { return ((uint32_t)b >> 24) & 15u; }
+__device__ __forceinline__ int bd_curr_depth(uint64_t b) {
+    const uint32_t nd = (uint32_t)b;
+    return ((nd >> 28) == 15u) ? -1 : (int)(nd >> 28);
+}
+
+// ------------------------------------------------------------------ finite-difference weights (AMR.h:1144-1150)
+// Centred (2p+1)-point weights of the first and second derivative, index i = -p..p.
+template <int P> struct FD;
+template <> struct FD<1> {
+    static __device__ __forceinline__ float d1(int i) { return i == -1 ? -.5f : i == 1 ? .5f : 0.f; }
+    static __device__ __forceinline__ float d2(int i) { return i == 0 ? -2.f : 1.f; }
+};
+template <> struct FD<2> {
+    static __device__ __forceinline__ float d1(int i) {
+        return i == -2 ? 1.f / 12 : i == -1 ? -2.f / 3 : i == 0 ? 0.f : i == 1 ? 2.f / 3 : -1.f / 12;
+    }
+    static __device__ __forceinline__ float d2(int i) {
+        return i == -2 ? -1.f / 12 : i == -1 ? 4.f / 3 : i == 0 ? -5.f / 2 : i == 1 ? 4.f / 3 : -1.f / 12;
+    }
+};
+template <> struct FD<3> {
+    static __device__ __forceinline__ float d1(int i) {
+        return i == -3 ? -1.f / 60 : i == -2 ? 3.f / 20 : i == -1 ? -3.f / 4 : i == 0 ? 0.f
+             : i == 1 ? 3.f / 4 : i == 2 ? -3.f / 20 : 1.f / 60;
+    }
+    static __device__ __forceinline__ float d2(int i) {
+        return i == -3 ? 1.f / 90 : i == -2 ? -3.f / 20 : i == -1 ? 3.f / 2 : i == 0 ? -49.f / 18
+             : i == 1 ? 3.f / 2 : i == 2 ? -3.f / 20 : 1.f / 90;
+    }
+};
+
+// ------------------------------------------------------------------ 10-point interpolation (AMR.h:672-699)
+// d points at the nearest source cell; strides 1, T, T^2; r = offset from it in cells.
+template <int T>
+__device__ __forceinline__ float interp10(const float* __restrict__ d, float rx, float ry, float rz) {
+    constexpr int T2 = T * T;
+    const float f = d[0];
+    float fx = d[1], fy = d[T], fz = d[T2];
+    float fxx = d[-1], fyy = d[-T], fzz = d[-T2];
+    float fxy = d[T + 1], fxz = d[T2 + 1], fyz = d[T2 + T];
+    fxy = __fadd_rn(fxy, __fsub_rn(__fsub_rn(f, fx), fy));
+    fxz = __fadd_rn(fxz, __fsub_rn(__fsub_rn(f, fx), fz));
+    fyz = __fadd_rn(fyz, __fsub_rn(__fsub_rn(f, fy), fz));
+    fx = __fmul_rn(__fsub_rn(fx, fxx), .5f);
+    fy = __fmul_rn(__fsub_rn(fy, fyy), .5f);
+    fz = __fmul_rn(__fsub_rn(fz, fzz), .5f);
+    fxx = __fsub_rn(__fadd_rn(fx, fxx), f);
+    fyy = __fsub_rn(__fadd_rn(fy, fyy), f);
+    fzz = __fsub_rn(__fadd_rn(fz, fzz), f);
+    float acc = __fmaf_rn(__fadd_rn(fx, __fmul_rn(fxx, rx)), rx, f);
+    acc = __fmaf_rn(__fadd_rn(fy, __fmul_rn(fyy, ry)), ry, acc);
+    acc = __fmaf_rn(__fadd_rn(fz, __fmul_rn(fzz, rz)), rz, acc);
+    acc = __fmaf_rn(__fmul_rn(fxy, rx), ry, acc);
+    acc = __fmaf_rn(__fmul_rn(fxz, rx), rz, acc);
+    acc = __fmaf_rn(__fmul_rn(fyz, ry), rz, acc);
+    return acc;
+}
+
+}  // namespace amr

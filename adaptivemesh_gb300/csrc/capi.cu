@@ -1,0 +1,313 @@
+// capi.cu -- extern "C" operator entry points and octree bindings (include/amr_gb300.h).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "amr_gb300.h"
+#include "capi_internal.h"
+#include "kernels.h"
+#include "octree.h"
+
+namespace amr {
+
+thread_local int g_last_cuda_error = 0;
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return AMR_OK;
+    g_last_cuda_error = (int)e;
+    return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? AMR_ERR_NO_DEVICE : AMR_ERR_CUDA;
+}
+
+bool config_supported(const amr_config* c) {
+    if (!c || !(c->outer_size > 0.f)) return false;
+#define AMR_CHECK_CFG(N, P) if (c->size_domain == N && c->padding_domain == P) return true;
+    AMR_FOR_EACH_CONFIG(AMR_CHECK_CFG)
+#undef AMR_CHECK_CFG
+    return false;
+}
+bool bssn_fused_supported(const amr_config* c) {
+#define AMR_CHECK_CFG(N, P) if (c->size_domain == N && c->padding_domain == P) return true;
+    AMR_FOR_EACH_BSSN_CONFIG(AMR_CHECK_CFG)
+#undef AMR_CHECK_CFG
+    return false;
+}
+
+cudaError_t launch_stencil(const amr_config& c, int kind, const StencilArgs& a, uint32_t grid, cudaStream_t st) {
+#define AMR_DISPATCH(N, P)                                                          \
+    if (c.size_domain == N && c.padding_domain == P) {                              \
+        switch (kind) {                                                             \
+            case SK_GRAD: return launch_stencil_t<N, P, SK_GRAD>(a, grid, st);      \
+            case SK_GRAD_HESS: return launch_stencil_t<N, P, SK_GRAD_HESS>(a, grid, st); \
+            case SK_MIXED: return launch_stencil_t<N, P, SK_MIXED>(a, grid, st);    \
+            default: break;                                                         \
+        }                                                                           \
+    }
+    AMR_FOR_EACH_CONFIG(AMR_DISPATCH)
+#undef AMR_DISPATCH
+#define AMR_DISPATCH_BSSN(N, P) \
+    if (c.size_domain == N && c.padding_domain == P && kind == SK_BSSN) return launch_stencil_t<N, P, SK_BSSN>(a, grid, st);
+    AMR_FOR_EACH_BSSN_CONFIG(AMR_DISPATCH_BSSN)
+#undef AMR_DISPATCH_BSSN
+    return cudaErrorInvalidValue;
+}
+
+// Persistent grid for the streaming stencil: as many CTAs as fit on the device at once, but no
+// more than there are work items.
+uint32_t stencil_grid(const amr_config& c, int kind, uint32_t n_items) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    size_t smem = 0;
+#define AMR_SMEM(N, P) \
+    if (c.size_domain == N && c.padding_domain == P) smem = kind == SK_BSSN ? stencil_smem_bytes<N, P, SK_BSSN>() : stencil_smem_bytes<N, P, SK_GRAD>();
+    AMR_FOR_EACH_CONFIG(AMR_SMEM)
+#undef AMR_SMEM
+    const uint32_t threads = c.size_domain * c.size_domain;
+    uint32_t per_sm = (uint32_t)(220u * 1024u / (smem ? smem : 1));
+    per_sm = per_sm < 2048u / threads ? per_sm : 2048u / threads;
+    if (per_sm < 1) per_sm = 1;
+    const uint32_t cap = per_sm * (uint32_t)sms;
+    return n_items < cap ? n_items : cap;
+}
+
+// Device error flag shared by the operator entry points (set by bounded waits that give up).
+int* device_error_flag() {
+    static int* flag = nullptr;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!flag) {
+        if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) { flag = nullptr; return nullptr; }
+        cudaMemset(flag, 0, sizeof(int));
+    }
+    return flag;
+}
+
+// Per-process staging buffer for amr_copy_boundaries: allocated on first use, grown on demand.
+static float* ghost_stage(size_t floats, cudaStream_t st, cudaError_t* err) {
+    static float* buf = nullptr;
+    static size_t cap = 0;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    *err = cudaSuccess;
+    if (floats <= cap) return buf;
+    if (buf) {
+        *err = cudaStreamSynchronize(st);
+        if (*err != cudaSuccess) return nullptr;
+        cudaFree(buf);
+        buf = nullptr;
+        cap = 0;
+    }
+    *err = cudaMalloc(&buf, floats * sizeof(float));
+    if (*err != cudaSuccess) { buf = nullptr; return nullptr; }
+    cap = floats;
+    return buf;
+}
+
+}  // namespace amr
+
+using namespace amr;
+
+#define AMR_API extern "C" __attribute__((visibility("default")))
+#define AMR_REQUIRE(cond) do { if (!(cond)) return AMR_ERR_INVALID; } while (0)
+#define AMR_REQUIRE_CFG(c) do { if (!(c)) return AMR_ERR_INVALID; if (!config_supported(c)) return AMR_ERR_UNSUPPORTED; } while (0)
+
+static inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
+
+AMR_API const char* amr_version(void) { return "adaptivemesh_gb300 0.1.0 (sm_103a)"; }
+AMR_API int amr_config_supported(const amr_config* cfg) { return config_supported(cfg) ? 1 : 0; }
+AMR_API int amr_last_cuda_error(void) { return g_last_cuda_error; }
+AMR_API const char* amr_status_string(int s) {
+    switch (s) {
+        case AMR_OK: return "ok";
+        case AMR_ERR_INVALID: return "invalid argument";
+        case AMR_ERR_UNSUPPORTED: return "unsupported (size_domain, padding_domain)";
+        case AMR_ERR_CUDA: return "CUDA runtime error";
+        case AMR_ERR_NO_DEVICE: return "no CUDA device";
+        case AMR_ERR_CAPACITY: return "capacity exceeded";
+        default: return "unknown status";
+    }
+}
+
+AMR_API int amr_cf3_encode(const float* xyz, const int32_t* seeds, uint64_t n, uint32_t* out, void* stream) {
+    AMR_REQUIRE(n == 0 || (xyz && out));
+    return cuda_status(launch_cf3_encode(xyz, seeds, n, out, S(stream)));
+}
+AMR_API int amr_cf3_decode(const uint32_t* words, uint64_t n, float* xyz, void* stream) {
+    AMR_REQUIRE(n == 0 || (words && xyz));
+    return cuda_status(launch_cf3_decode(words, n, xyz, S(stream)));
+}
+
+static StencilArgs base_args(const amr_config* cfg, const uint32_t* positions, uint32_t used, uint32_t substep,
+                             uint32_t max_depth) {
+    StencilArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.positions = positions;
+    a.items = nullptr;
+    a.n_items = used;
+    a.substep = substep;
+    a.max_depth = max_depth;
+    a.geo = make_geo(*cfg);
+    a.err = device_error_flag();
+    return a;
+}
+
+AMR_API int amr_differentiate(const amr_config* cfg, const float* field, uint32_t* dif, uint32_t* d2if,
+                              const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
+                              int32_t seed, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(field && dif && positions && max_depth <= kDepthLimit);
+    StencilArgs a = base_args(cfg, positions, used, substep, max_depth);
+    if (!a.err) return AMR_ERR_CUDA;
+    a.field[0] = field;
+    a.grad[0] = dif;
+    a.hdiag = d2if;
+    a.seed_d[0] = seed;
+    const int kind = d2if ? SK_GRAD_HESS : SK_GRAD;
+    return cuda_status(launch_stencil(*cfg, kind, a, stencil_grid(*cfg, kind, used), S(stream)));
+}
+AMR_API int amr_mixed_partials(const amr_config* cfg, const float* field, uint32_t* off, const uint32_t* positions,
+                               uint32_t used, uint32_t substep, uint32_t max_depth, int32_t seed, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(field && off && positions && max_depth <= kDepthLimit);
+    StencilArgs a = base_args(cfg, positions, used, substep, max_depth);
+    if (!a.err) return AMR_ERR_CUDA;
+    a.field[0] = field;
+    a.hoff = off;
+    a.seed_m[0] = seed;
+    return cuda_status(launch_stencil(*cfg, SK_MIXED, a, stencil_grid(*cfg, SK_MIXED, used), S(stream)));
+}
+AMR_API int amr_deriv_trace(const amr_config* cfg, const uint32_t* hd, const uint32_t* ho, float* const* metric6,
+                            float* out, const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
+                            void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(hd && ho && metric6 && out && positions && max_depth <= kDepthLimit);
+    for (int k = 0; k < 6; k++) AMR_REQUIRE(metric6[k]);
+    return cuda_status(launch_deriv_trace(make_dims(*cfg), hd, ho, metric6, out, positions, used, substep, max_depth, S(stream)));
+}
+AMR_API int amr_christoffel(const amr_config* cfg, float* const* metric6, uint32_t* const* derivs6, int32_t seed,
+                            uint32_t* const* out6, const uint32_t* positions, uint32_t used, uint32_t substep,
+                            uint32_t max_depth, int mode, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(metric6 && derivs6 && out6 && positions && max_depth <= kDepthLimit);
+    AMR_REQUIRE(mode == AMR_CHRISTOFFEL_REFERENCE || mode == AMR_CHRISTOFFEL_RAISED);
+    for (int k = 0; k < 6; k++) AMR_REQUIRE(metric6[k] && derivs6[k] && out6[k]);
+    return cuda_status(launch_christoffel(make_dims(*cfg), metric6, derivs6, seed, out6, positions, used, substep,
+                                          max_depth, mode, S(stream)));
+}
+AMR_API int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,
+                                uint32_t used, uint32_t substep, uint32_t max_depth, int copy_only_new, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(old_f && new_f && boundaries && max_depth <= kDepthLimit);
+    const Dims d = make_dims(*cfg);
+    FieldSet f;
+    std::memset(&f, 0, sizeof(f));
+    f.old_f[0] = old_f;
+    f.new_f[0] = new_f;
+    f.ncomp = 1;
+    cudaError_t e;
+    float* stage = ghost_stage(ghost_scratch_floats(d, used, 1), S(stream), &e);
+    if (!stage && used) return cuda_status(e);
+    return cuda_status(launch_copy_boundaries(d, f, boundaries, used, substep, max_depth, copy_only_new, stage, S(stream)));
+}
+AMR_API int amr_copy_new_to_old(const amr_config* cfg, float* old_f, const float* new_f, const uint32_t* positions,
+                                const int32_t* children, uint32_t used, uint32_t substep, uint32_t max_depth,
+                                void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(old_f && new_f && positions && children && max_depth <= kDepthLimit);
+    AMR_REQUIRE(cfg->size_domain % 2u == 0u);
+    FieldSet f;
+    std::memset(&f, 0, sizeof(f));
+    f.old_f[0] = old_f;
+    f.new_f[0] = const_cast<float*>(new_f);
+    f.ncomp = 1;
+    return cuda_status(launch_copy_new_to_old(make_dims(*cfg), f, positions, children, nullptr, used, substep, max_depth,
+                                              S(stream)));
+}
+AMR_API int amr_copy_to_child(const amr_config* cfg, float* field, uint32_t offset, int32_t child, int32_t parent,
+                              void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(field && offset < 8u && child >= 0 && parent >= 0);
+    return cuda_status(launch_copy_to_child(make_dims(*cfg), field, offset, child, parent, S(stream)));
+}
+AMR_API int amr_wave_predictor(const amr_config* cfg, const float* old_f, const uint32_t* derivs, const uint32_t* hess,
+                               float* new_f, const uint32_t* positions, uint32_t used, uint32_t substep,
+                               uint32_t max_depth, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(old_f && derivs && hess && new_f && positions && max_depth <= kDepthLimit);
+    return cuda_status(launch_wave_step(make_dims(*cfg), make_geo(*cfg), 0, old_f, derivs, hess, new_f, positions, used,
+                                        substep, max_depth, S(stream)));
+}
+AMR_API int amr_wave_corrector(const amr_config* cfg, const float* old_f, const uint32_t* derivs, const uint32_t* hess,
+                               float* new_f, const uint32_t* positions, uint32_t used, uint32_t substep,
+                               uint32_t max_depth, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(old_f && derivs && hess && new_f && positions && max_depth <= kDepthLimit);
+    return cuda_status(launch_wave_step(make_dims(*cfg), make_geo(*cfg), 1, old_f, derivs, hess, new_f, positions, used,
+                                        substep, max_depth, S(stream)));
+}
+AMR_API int amr_criterion(const amr_config* cfg, const uint32_t* derivs, const uint32_t* hess, float* crit,
+                          const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(derivs && hess && crit && positions && max_depth <= kDepthLimit);
+    AMR_REQUIRE(cfg->size_domain % 4u == 0u);
+    return cuda_status(launch_criterion(make_dims(*cfg), make_geo(*cfg), derivs, hess, crit, positions, used, substep,
+                                        max_depth, S(stream)));
+}
+
+// ---------------------------------------------------------------- octree
+struct amr_octree { Octree tree; explicit amr_octree(uint32_t s) : tree(s) {} };
+
+AMR_API int amr_octree_create(uint32_t node_slots, amr_octree** out) {
+    AMR_REQUIRE(out && node_slots >= 1u && node_slots <= (1u << 23));
+    *out = new (std::nothrow) amr_octree(node_slots);
+    return *out ? AMR_OK : AMR_ERR_CAPACITY;
+}
+AMR_API int amr_octree_destroy(amr_octree* o) {
+    delete o;
+    return AMR_OK;
+}
+AMR_API int amr_octree_add_node(amr_octree* o, int32_t parent, int32_t offset) {
+    AMR_REQUIRE(o && parent >= 0 && (uint32_t)parent < o->tree.max_slots() && offset >= 0 && offset < 8);
+    o->tree.add_node(parent, offset);
+    return AMR_OK;
+}
+AMR_API int amr_octree_remove_node(amr_octree* o, int32_t node) {
+    AMR_REQUIRE(o && node >= -1 && node < (int32_t)o->tree.max_slots());
+    o->tree.remove_node(node);
+    return AMR_OK;
+}
+AMR_API int amr_octree_increment_timer(amr_octree* o) {
+    AMR_REQUIRE(o);
+    o->tree.increment_timer();
+    return AMR_OK;
+}
+AMR_API uint32_t amr_octree_find_node_idx(const amr_octree* o, uint32_t packed, uint32_t max_depth) {
+    return o ? o->tree.find_node_idx(packed, max_depth) : 0u;
+}
+int amr::octree_state_impl(const Octree& t, uint32_t* positions, int32_t* parent, int32_t* children,
+                           uint64_t* boundaries, uint32_t* lifetime, uint32_t* scalars) {
+    const size_t s = t.max_slots();
+    if (positions) std::memcpy(positions, t.positions().data(), s * 4);
+    if (parent) std::memcpy(parent, t.parents().data(), s * 4);
+    if (children) std::memcpy(children, t.children().data(), s * 32);
+    if (boundaries) std::memcpy(boundaries, t.boundaries().data(), s * 48);
+    if (lifetime) std::memcpy(lifetime, t.lifetime().data(), s * 4);
+    if (scalars) {
+        scalars[0] = t.timer();
+        scalars[1] = (uint32_t)t.read_max_depth();
+        scalars[2] = t.read_first_free_slot();
+        scalars[3] = t.curr_used_slots();
+        scalars[4] = t.max_slots();
+    }
+    return AMR_OK;
+}
+AMR_API int amr_octree_state(const amr_octree* o, uint32_t* positions, int32_t* parent, int32_t* children,
+                             uint64_t* boundaries, uint32_t* lifetime, uint32_t* scalars) {
+    AMR_REQUIRE(o);
+    return octree_state_impl(o->tree, positions, parent, children, boundaries, lifetime, scalars);
+}

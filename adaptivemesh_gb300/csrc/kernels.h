@@ -1,0 +1,84 @@
+// kernels.h -- launch interfaces of the GB300 kernels (host-callable, no device code).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "amr_types.h"
+
+// Compiled (size_domain, padding_domain) pairs.  (28, 2) is the reference as shipped; (16, 3) and
+// (32, 3) are the benchmark sizes; (8, 2) keeps small test cases cheap.
+#define AMR_FOR_EACH_CONFIG(X) X(16, 3) X(28, 2) X(32, 3) X(8, 2)
+// Pairs whose six-component fused kernel fits in shared memory (6 x (2p+3) padded planes).
+#define AMR_FOR_EACH_BSSN_CONFIG(X) X(16, 3) X(28, 2) X(8, 2)
+
+namespace amr {
+
+enum StencilKind { SK_GRAD = 0, SK_GRAD_HESS = 1, SK_MIXED = 2, SK_BSSN = 3 };
+
+struct StencilArgs {
+    const float* field[6];        // padded input components
+    uint32_t* grad[6];            // compressed gradients (SK_GRAD, SK_GRAD_HESS: [0]; SK_BSSN: all six)
+    uint32_t* hdiag;              // SK_GRAD_HESS: compressed diagonal Hessian
+    uint32_t* hoff;               // SK_MIXED: compressed off-diagonal Hessian
+    float* lap[6];                // SK_BSSN: g^kl d_k d_l g_ij per component (inner layout)
+    uint32_t* chr[6];             // SK_BSSN: compressed Christoffel symbols
+    int32_t seed_d[6];            // launch seeds of the derivative launches, per component
+    int32_t seed_m[6];            // launch seeds of the mixed-partial launches, per component
+    int32_t seed_c;               // launch seed of the Christoffel launch
+    const int32_t* seed_ptr;      // if set, the seeds are read from device memory instead:
+                                  // seed_d[k] = seed_ptr[2k], seed_m[k] = seed_ptr[2k+1], seed_c = seed_ptr[12]
+    int christoffel_mode;         // AMR_CHRISTOFFEL_*
+    const uint32_t* positions;    // octree_abs_pos per slot
+    const uint32_t* items;        // domains to process (nullptr: item i is slot i)
+    uint32_t n_items;
+    uint32_t substep, max_depth;
+    Geo geo;
+    int* err;                     // set to 1 if a bounded wait gave up
+};
+
+template <int N, int P, int KIND>
+cudaError_t launch_stencil_t(const StencilArgs& a, uint32_t grid, cudaStream_t st);
+template <int N, int P, int KIND>
+size_t stencil_smem_bytes();
+
+// Pointwise kernels (kernels_point.cu).  Sizes are run-time values; nothing is templated.
+struct Dims {
+    uint32_t n, p, t;             // size_domain, padding_domain, n + 2p
+};
+inline Dims make_dims(const amr_config& c) { return Dims{c.size_domain, c.padding_domain, c.size_domain + 2 * c.padding_domain}; }
+
+cudaError_t launch_cf3_encode(const float* xyz, const int32_t* seeds, uint64_t n, uint32_t* out, cudaStream_t st);
+cudaError_t launch_cf3_decode(const uint32_t* w, uint64_t n, float* xyz, cudaStream_t st);
+cudaError_t launch_deriv_trace(Dims d, const uint32_t* hd, const uint32_t* ho, float* const* metric6, float* out,
+                               const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
+                               cudaStream_t st);
+cudaError_t launch_christoffel(Dims d, float* const* metric6, uint32_t* const* der6, int32_t seed, uint32_t* const* out6,
+                               const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth, int mode,
+                               cudaStream_t st);
+cudaError_t launch_wave_step(Dims d, const Geo& g, int corrector, const float* old_f, const uint32_t* der,
+                             const uint32_t* hess, float* new_f, const uint32_t* positions, uint32_t used,
+                             uint32_t substep, uint32_t max_depth, cudaStream_t st);
+cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const uint32_t* hess, float* crit,
+                             const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
+                             cudaStream_t st);
+
+// Restriction / prolongation / ghost fill (kernels_amr.cu).  `ncomp` components are processed in
+// one launch (component k at fields_old[k], fields_new[k]).
+struct FieldSet {
+    float* old_f[6];
+    float* new_f[6];
+    int ncomp;
+};
+cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* positions, const int32_t* children,
+                                   const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
+                                   cudaStream_t st);
+cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t child, int32_t parent, cudaStream_t st);
+// Ghost values per (slot, face, layer, v, u): 2 * ncomp * 6 * p * n^2 floats per slot.
+size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp);
+cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* boundaries, uint32_t used,
+                                   uint32_t substep, uint32_t max_depth, int copy_only_new, float* scratch,
+                                   cudaStream_t st);
+
+}  // namespace amr

@@ -1,0 +1,225 @@
+// kernels_point.cu -- cell-local kernels (one thread per interior cell or codec word).
+#include "kernels.h"
+
+#include "amr_device.cuh"
+
+namespace amr {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kBlock - 1) / kBlock); }
+
+// Decompose an inner-layout index into (slot, x, y, z) and the padded index of the same cell.
+struct InnerCell {
+    uint32_t slot, x, y, z;
+    uint64_t padded;
+};
+__device__ __forceinline__ InnerCell inner_cell(uint64_t o, const Dims& d) {
+    InnerCell c;
+    const uint64_t n3 = (uint64_t)d.n * d.n * d.n;
+    c.slot = (uint32_t)(o / n3);
+    uint32_t r = (uint32_t)(o - (uint64_t)c.slot * n3);
+    c.x = r % d.n; r /= d.n;
+    c.y = r % d.n;
+    c.z = r / d.n;
+    c.padded = (((uint64_t)c.slot * d.t + c.z + d.p) * d.t + c.y + d.p) * d.t + c.x + d.p;
+    return c;
+}
+__device__ __forceinline__ bool slot_active(const uint32_t* positions, uint32_t slot, uint32_t substep,
+                                            uint32_t max_depth, int* depth_out) {
+    const int depth = pos_depth(positions[slot]);
+    *depth_out = depth;
+    return depth != -1 && active_depth(substep, (uint32_t)depth, max_depth);
+}
+
+struct Ptr6f { float* p[6]; };
+struct Ptr6u { uint32_t* p[6]; };
+
+// ---------------------------------------------------------------- codec
+__global__ void k_cf3_encode(const float* __restrict__ xyz, const int32_t* __restrict__ seeds, uint64_t n,
+                             uint32_t* __restrict__ out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    if (seeds) {
+        int32_t s = seeds[i];
+        out[i] = cf3_encode(x, y, z, s);
+    } else {
+        out[i] = cf3_encode_det(x, y, z);
+    }
+}
+__global__ void k_cf3_decode(const uint32_t* __restrict__ w, uint64_t n, float* __restrict__ xyz) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 v = cf3_decode(w[i]);
+    xyz[3 * i] = v.x; xyz[3 * i + 1] = v.y; xyz[3 * i + 2] = v.z;
+}
+
+// ---------------------------------------------------------------- g^kl H_kl, BSSN.h:7-22
+__global__ void k_deriv_trace(Dims d, const uint32_t* __restrict__ hd, const uint32_t* __restrict__ ho, Ptr6f m,
+                              float* __restrict__ out, const uint32_t* __restrict__ positions, uint32_t used,
+                              uint32_t substep, uint32_t max_depth) {
+    const uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= (uint64_t)used * d.n * d.n * d.n) return;
+    const InnerCell c = inner_cell(o, d);
+    int depth;
+    if (!slot_active(positions, c.slot, substep, max_depth, &depth)) return;
+    const Sym g{m.p[0][c.padded], m.p[1][c.padded], m.p[2][c.padded], m.p[3][c.padded], m.p[4][c.padded], m.p[5][c.padded]};
+    out[o] = trace_contra(sym_from_cf3(hd[o], ho[o]), sym_inverse(g));
+}
+
+// ---------------------------------------------------------------- Christoffel symbols, BSSN.h:55-91
+__global__ void k_christoffel(Dims d, Ptr6f m, Ptr6u der, int32_t seed, Ptr6u outp,
+                              const uint32_t* __restrict__ positions, uint32_t used, uint32_t substep,
+                              uint32_t max_depth, int mode) {
+    const uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= (uint64_t)used * d.n * d.n * d.n) return;
+    const InnerCell c = inner_cell(o, d);
+    int depth;
+    if (!slot_active(positions, c.slot, substep, max_depth, &depth)) return;
+    int32_t rng = cell_rng(seed, c.x, c.y, c.slot * d.n + c.z);
+    uint32_t G[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) G[k] = der.p[k][o];
+    const Sym g{m.p[0][c.padded], m.p[1][c.padded], m.p[2][c.padded], m.p[3][c.padded], m.p[4][c.padded], m.p[5][c.padded]};
+    const Sym M = mode == AMR_CHRISTOFFEL_RAISED ? sym_inverse(g) : g;
+    float3 dd[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) dd[k] = cf3_decode(G[k]);
+    const Sym Sx{dd[0].x, __fmul_rn(__fadd_rn(dd[0].y, dd[1].x), .5f), __fmul_rn(__fadd_rn(dd[0].z, dd[2].x), .5f),
+                 dd[1].y, __fmul_rn(__fadd_rn(dd[2].y, dd[1].z), .5f), dd[2].z};
+    const Sym Sy{dd[1].x, __fmul_rn(__fadd_rn(dd[1].y, dd[3].x), .5f), __fmul_rn(__fadd_rn(dd[1].z, dd[4].x), .5f),
+                 dd[3].y, __fmul_rn(__fadd_rn(dd[4].y, dd[3].z), .5f), dd[4].z};
+    const Sym Sz{dd[2].x, __fmul_rn(__fadd_rn(dd[2].y, dd[4].x), .5f), __fmul_rn(__fadd_rn(dd[2].z, dd[5].x), .5f),
+                 dd[4].y, __fmul_rn(__fadd_rn(dd[5].y, dd[4].z), .5f), dd[5].z};
+    const float sx[6] = {Sx.xx, Sx.xy, Sx.xz, Sx.yy, Sx.yz, Sx.zz};
+    const float sy[6] = {Sy.xx, Sy.xy, Sy.xz, Sy.yy, Sy.yz, Sy.zz};
+    const float sz[6] = {Sz.xx, Sz.xy, Sz.xz, Sz.yy, Sz.yz, Sz.zz};
+#pragma unroll
+    for (int jk = 0; jk < 6; jk++) {
+        const float3 v = make_float3(__fmaf_rn(-dd[jk].x, .5f, sx[jk]), __fmaf_rn(-dd[jk].y, .5f, sy[jk]),
+                                     __fmaf_rn(-dd[jk].z, .5f, sz[jk]));
+        const float3 r = sym_times(M, v);
+        outp.p[jk][o] = cf3_encode(r.x, r.y, r.z, rng);
+    }
+}
+
+// ---------------------------------------------------------------- SimpleWave Heun update, SimpleWave.h:7-46
+__global__ void k_wave_step(Dims d, float outer_dt, int corrector, const float* __restrict__ old_f,
+                            const uint32_t* __restrict__ der, const uint32_t* __restrict__ hess, float* new_f,
+                            const uint32_t* __restrict__ positions, uint32_t used, uint32_t substep, uint32_t max_depth) {
+    const uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= (uint64_t)used * d.n * d.n * d.n) return;
+    const InnerCell c = inner_cell(o, d);
+    int depth;
+    if (!slot_active(positions, c.slot, substep, max_depth, &depth)) return;
+    const float visc = 0.01f;                                          // SimpleWave.h:5
+    const float gx = cf3_decode(der[o]).x;
+    const float3 h = cf3_decode(hess[o]);
+    const float lap = __fmaf_rn(h.z, visc, __fmaf_rn(h.x, visc, __fmul_rn(h.y, visc)));
+    const float v = old_f[c.padded];
+    // (lap - v*gx) * dt / 2^depth; the division by a power of two is exact
+    const float upd = __fmul_rn(__fmul_rn(__fmaf_rn(-v, gx, lap), outer_dt), __uint_as_float((127u - (uint32_t)depth) << 23));
+    if (!corrector) new_f[c.padded] = __fadd_rn(v, upd);
+    else new_f[c.padded] = __fmul_rn(__fadd_rn(new_f[c.padded], __fadd_rn(v, upd)), .5f);
+}
+
+// ---------------------------------------------------------------- refinement criterion, SimpleWave.h:91-139
+__device__ __forceinline__ float cf3_length(uint32_t w) {
+    const float3 v = cf3_decode(w);
+    return sqrt_approx(__fmaf_rn(v.z, v.z, __fmaf_rn(v.x, v.x, __fmul_rn(v.y, v.y))));
+}
+__global__ void k_criterion_columns(Dims d, float outer_dx, const uint32_t* __restrict__ der,
+                                    const uint32_t* __restrict__ hess, float* __restrict__ crit,
+                                    const uint32_t* __restrict__ positions, uint32_t used, uint32_t substep,
+                                    uint32_t max_depth) {
+    const uint32_t n = d.n, h = n >> 1, q = n >> 2;
+    const uint64_t o = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;   // x + (y + zi*h)*n
+    if (o >= (uint64_t)used * n * n) return;
+    const uint32_t x = (uint32_t)(o % n);
+    const uint32_t rest = (uint32_t)(o / n);
+    const uint32_t y = rest % h, zi = rest / h;
+    const int depth = pos_depth(positions[zi / 2]);
+    if (depth == -1 || !active_depth(substep, (uint32_t)depth, max_depth)) { crit[o] = __int_as_float(0x7fc00000); return; }   // NAN, SimpleWave.h:97
+    uint64_t ro = x + ((uint64_t)y + ((y >= q) ? q : 0u) + (uint64_t)zi * n * h) * n;
+    const float s1 = __fmul_rn(outer_dx, __uint_as_float((127u - (uint32_t)depth) << 23));
+    const float s2 = __fmul_rn(__fmul_rn(outer_dx, outer_dx), __uint_as_float((127u - 2u * (uint32_t)depth) << 23));
+    float cr = 0.f;
+    for (uint32_t i = 0; i < h; i++) {
+        cr = fmaxf(cr, __fmul_rn(cf3_length(der[ro]), s1));
+        cr = fmaxf(cr, __fmul_rn(cf3_length(hess[ro]), s2));
+        cr = fmaxf(cr, __fmul_rn(cf3_length(der[ro + (uint64_t)q * n]), s1));
+        cr = fmaxf(cr, __fmul_rn(cf3_length(hess[ro + (uint64_t)q * n]), s2));
+        ro += (uint64_t)n * n;
+    }
+    crit[o] = cr;
+}
+__global__ void k_criterion_octants(Dims d, float* __restrict__ crit, uint32_t used) {
+    const uint32_t n = d.n, h = n >> 1, q = n >> 2;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= used * 8u) return;
+    const uint32_t x = idx & 1u, y = (idx >> 1) & 1u, z = (idx >> 2) & 1u, node = idx >> 3;
+    const uint64_t base = (uint64_t)node * n * n + z * (n * n >> 1) + y * (n * n >> 2) + x * h;
+    float cr = __int_as_float(0x7fc00000);
+    for (uint32_t yy = 0; yy < q; yy++)
+        for (uint32_t xx = 0; xx < h; xx++) cr = fmaxf(cr, crit[base + xx + (uint64_t)yy * n]);
+    crit[base] = cr;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+cudaError_t launch_cf3_encode(const float* xyz, const int32_t* seeds, uint64_t n, uint32_t* out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_cf3_encode<<<blocks_for(n), kBlock, 0, st>>>(xyz, seeds, n, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_cf3_decode(const uint32_t* w, uint64_t n, float* xyz, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_cf3_decode<<<blocks_for(n), kBlock, 0, st>>>(w, n, xyz);
+    return cudaGetLastError();
+}
+cudaError_t launch_deriv_trace(Dims d, const uint32_t* hd, const uint32_t* ho, float* const* metric6, float* out,
+                               const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
+                               cudaStream_t st) {
+    const uint64_t n = (uint64_t)used * d.n * d.n * d.n;
+    if (n == 0) return cudaSuccess;
+    Ptr6f m;
+    for (int k = 0; k < 6; k++) m.p[k] = metric6[k];
+    k_deriv_trace<<<blocks_for(n), kBlock, 0, st>>>(d, hd, ho, m, out, positions, used, substep, max_depth);
+    return cudaGetLastError();
+}
+cudaError_t launch_christoffel(Dims d, float* const* metric6, uint32_t* const* der6, int32_t seed, uint32_t* const* out6,
+                               const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth, int mode,
+                               cudaStream_t st) {
+    const uint64_t n = (uint64_t)used * d.n * d.n * d.n;
+    if (n == 0) return cudaSuccess;
+    Ptr6f m; Ptr6u der, out;
+    for (int k = 0; k < 6; k++) { m.p[k] = metric6[k]; der.p[k] = der6[k]; out.p[k] = out6[k]; }
+    k_christoffel<<<blocks_for(n), kBlock, 0, st>>>(d, m, der, seed, out, positions, used, substep, max_depth, mode);
+    return cudaGetLastError();
+}
+cudaError_t launch_wave_step(Dims d, const Geo& g, int corrector, const float* old_f, const uint32_t* der,
+                             const uint32_t* hess, float* new_f, const uint32_t* positions, uint32_t used,
+                             uint32_t substep, uint32_t max_depth, cudaStream_t st) {
+    const uint64_t n = (uint64_t)used * d.n * d.n * d.n;
+    if (n == 0) return cudaSuccess;
+    k_wave_step<<<blocks_for(n), kBlock, 0, st>>>(d, g.outer_dt, corrector, old_f, der, hess, new_f, positions, used,
+                                                  substep, max_depth);
+    return cudaGetLastError();
+}
+cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const uint32_t* hess, float* crit,
+                             const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
+                             cudaStream_t st) {
+    const uint64_t n = (uint64_t)used * d.n * d.n;
+    if (n == 0) return cudaSuccess;
+    k_criterion_columns<<<blocks_for(n), kBlock, 0, st>>>(d, g.outer_dx, der, hess, crit, positions, used, substep, max_depth);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_criterion_octants<<<blocks_for((uint64_t)used * 8u), kBlock, 0, st>>>(d, crit, used);
+    return cudaGetLastError();
+}
+
+}  // namespace amr

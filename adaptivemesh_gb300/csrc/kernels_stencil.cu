@@ -1,0 +1,286 @@
+// kernels_stencil.cu -- finite-difference stencils on padded domains (sm_103a).
+//
+// One CTA processes one domain at a time (a persistent loop over a work list).  The domain's
+// padded z-planes are streamed through a shared-memory ring with 1-D TMA bulk copies
+// (cp.async.bulk, one copy per plane and component, completion on an mbarrier per ring slot);
+// thread (x, y) computes the interior cell (x, y, z) of every plane, so each plane is read from
+// HBM exactly once and every stencil tap comes from shared memory.
+//
+// Kinds:
+//   SK_GRAD       gradient                                   __differentiate  (AMR.h:1152-1179)
+//   SK_GRAD_HESS  gradient + diagonal Hessian                __differentiate  (AMR.h:1181-1219)
+//   SK_MIXED      off-diagonal Hessian, edge rule            __mixed_partials (AMR.h:1221-1266)
+//   SK_BSSN       all six metric components in one pass: gradients (written), diagonal and
+//                 off-diagonal Hessians quantised through compressed_float3 in registers exactly
+//                 as the reference round-trips them through memory, g^kl d_k d_l g_ij (written),
+//                 then the Christoffel symbols (written).  Replaces, per predictor/corrector,
+//                 the 18 launches of metric_derivatives_noncovariant (BSSN.h:38-53) and the
+//                 Christoffel launch (BSSN.h:93-102).
+#include "kernels.h"
+
+#include "amr_device.cuh"
+#include "tma.cuh"
+
+namespace amr {
+
+template <int N, int P, int KIND>
+struct StencilShape {
+    static constexpr int T = N + 2 * P;
+    static constexpr int NC = KIND == SK_BSSN ? 6 : 1;
+    static constexpr int R = 2 * P + 3;                          // ring slots: 2P+1 in use, 2 in flight
+    static constexpr uint32_t PLANE = (uint32_t)(T * T);         // floats per plane
+    static constexpr uint32_t PLANE_BYTES = PLANE * 4u;
+    static constexpr size_t RING_BYTES = (size_t)NC * R * PLANE_BYTES;
+    static constexpr size_t SMEM = RING_BYTES + (size_t)R * 8u;
+    static_assert(PLANE_BYTES % 16u == 0u, "bulk copies move whole planes of 16-byte multiples");
+};
+
+template <int N, int P, int KIND>
+size_t stencil_smem_bytes() { return StencilShape<N, P, KIND>::SMEM; }
+
+// ---------------------------------------------------------------- per-cell pieces
+
+// Gradient and diagonal second derivative along the three axes.  `pl(j)` is the plane at
+// padded z offset j - P from the cell's plane; c0 is the cell's offset inside a plane.
+template <int P, int T, class PL>
+__device__ __forceinline__ void fd_axes(const PL& pl, int c0, float& gx, float& gy, float& gz,
+                                        float& hx, float& hy, float& hz) {
+    gx = gy = gz = hx = hy = hz = 0.f;
+    const float* m = pl(P);
+#pragma unroll
+    for (int i = -P; i <= P; i++) {
+        const float c1 = FD<P>::d1(i), c2 = FD<P>::d2(i);
+        float a = m[c0 + i];
+        gx = __fmaf_rn(a, c1, gx); hx = __fmaf_rn(a, c2, hx);
+        a = m[c0 + i * T];
+        gy = __fmaf_rn(a, c1, gy); hy = __fmaf_rn(a, c2, hy);
+        a = pl(P + i)[c0];
+        gz = __fmaf_rn(a, c1, gz); hz = __fmaf_rn(a, c2, hz);
+    }
+}
+
+// Mixed-partial helpers (AMR.h:1221-1230).  Offsets are given as (plane, in-plane offset).
+__device__ __forceinline__ float mixed_centre(float a, float b, float c, float d) {
+    return __fmul_rn(.25f, __fsub_rn(__fsub_rn(__fadd_rn(a, b), c), d));
+}
+__device__ __forceinline__ float mixed_edge(float f, float a, float b, float c, float d, float e, float g) {
+    float s = __fadd_rn(a, b);
+    s = __fsub_rn(s, c); s = __fsub_rn(s, d); s = __fsub_rn(s, e); s = __fsub_rn(s, g);
+    return __fmaf_rn(.5f, s, f);
+}
+
+// Off-diagonal Hessian (xy, xz, yz) before scaling, with the reference's edge fallback.
+template <int N, int P, int T, class PL>
+__device__ __forceinline__ float3 mixed_partials(const PL& pl, int c0, uint32_t x, uint32_t y, uint32_t z) {
+    const float* zm = pl(P - 1);
+    const float* z0 = pl(P);
+    const float* zp = pl(P + 1);
+    const int ex = (int)x - (int)min(max(x, 1u), (uint32_t)N - 2u);
+    const int ey = (int)y - (int)min(max(y, 1u), (uint32_t)N - 2u);
+    const int ez = (int)z - (int)min(max(z, 1u), (uint32_t)N - 2u);
+    const int cxy = ex * ey, cxz = ex * ez, cyz = ey * ez;
+    float vxy, vxz, vyz;
+    if (cxy == 0) {
+        vxy = mixed_centre(z0[c0 + 1 + T], z0[c0 - 1 - T], z0[c0 + 1 - T], z0[c0 - 1 + T]);
+    } else {
+        const int dx = -cxy;
+        vxy = __fmul_rn((float)(-cxy), mixed_edge(z0[c0], z0[c0 + dx + T], z0[c0 - dx - T], z0[c0 - dx], z0[c0 + dx],
+                                                  z0[c0 - T], z0[c0 + T]));
+    }
+    if (cxz == 0) {
+        vxz = mixed_centre(zp[c0 + 1], zm[c0 - 1], zm[c0 + 1], zp[c0 - 1]);
+    } else {
+        const int dx = -cxz;
+        vxz = __fmul_rn((float)(-cxz), mixed_edge(z0[c0], zp[c0 + dx], zm[c0 - dx], z0[c0 - dx], z0[c0 + dx],
+                                                  zm[c0], zp[c0]));
+    }
+    if (cyz == 0) {
+        vyz = mixed_centre(zp[c0 + T], zm[c0 - T], zm[c0 + T], zp[c0 - T]);
+    } else {
+        const int dx = -cyz * T;
+        vyz = __fmul_rn((float)(-cyz), mixed_edge(z0[c0], zp[c0 + dx], zm[c0 - dx], z0[c0 - dx], z0[c0 + dx],
+                                                  zm[c0], zp[c0]));
+    }
+    return make_float3(vxy, vxz, vyz);
+}
+
+// Christoffel symbols of one cell from the six compressed metric gradients (BSSN.h:72-90).
+// `M` multiplies the lowered symbols: the metric itself (reference) or its inverse.
+__device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M, int32_t& rng, uint32_t* out) {
+    float3 d[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) d[k] = cf3_decode(G[k]);
+    // rows of float3x3_sym(float3, float3, float3), tensors.h:138: S_l(j,k) = (d_j g_lk + d_k g_lj)/2
+    const Sym Sx{d[0].x, __fmul_rn(__fadd_rn(d[0].y, d[1].x), .5f), __fmul_rn(__fadd_rn(d[0].z, d[2].x), .5f),
+                 d[1].y, __fmul_rn(__fadd_rn(d[2].y, d[1].z), .5f), d[2].z};
+    const Sym Sy{d[1].x, __fmul_rn(__fadd_rn(d[1].y, d[3].x), .5f), __fmul_rn(__fadd_rn(d[1].z, d[4].x), .5f),
+                 d[3].y, __fmul_rn(__fadd_rn(d[4].y, d[3].z), .5f), d[4].z};
+    const Sym Sz{d[2].x, __fmul_rn(__fadd_rn(d[2].y, d[4].x), .5f), __fmul_rn(__fadd_rn(d[2].z, d[5].x), .5f),
+                 d[4].y, __fmul_rn(__fadd_rn(d[5].y, d[4].z), .5f), d[5].z};
+    const float sx[6] = {Sx.xx, Sx.xy, Sx.xz, Sx.yy, Sx.yz, Sx.zz};
+    const float sy[6] = {Sy.xx, Sy.xy, Sy.xz, Sy.yy, Sy.yz, Sy.zz};
+    const float sz[6] = {Sz.xx, Sz.xy, Sz.xz, Sz.yy, Sz.yz, Sz.zz};
+#pragma unroll
+    for (int jk = 0; jk < 6; jk++) {
+        const float3 v = make_float3(__fmaf_rn(-d[jk].x, .5f, sx[jk]), __fmaf_rn(-d[jk].y, .5f, sy[jk]),
+                                     __fmaf_rn(-d[jk].z, .5f, sz[jk]));
+        const float3 r = sym_times(M, v);
+        out[jk] = cf3_encode(r.x, r.y, r.z, rng);
+    }
+}
+
+// ---------------------------------------------------------------- the streaming kernel
+template <int N, int P, int KIND>
+__global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
+    using S = StencilShape<N, P, KIND>;
+    constexpr int T = S::T, NC = S::NC, R = S::R;
+    constexpr uint32_t PLANE = S::PLANE;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* ring = reinterpret_cast<float*>(smem_raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S::RING_BYTES);
+    __shared__ int s_abort;
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t x = tid % N, y = tid / N;
+    const int c0 = (int)((y + P) * T + (x + P));
+
+    if (tid == 0) {
+        for (int r = 0; r < R; r++) mbar_init(&bars[r], 1);
+        mbar_fence_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+
+    int32_t seed_d[NC], seed_m[NC], seed_c = a.seed_c;
+#pragma unroll
+    for (int k = 0; k < NC; k++) { seed_d[k] = a.seed_d[k]; seed_m[k] = a.seed_m[k]; }
+    if (a.seed_ptr) {
+#pragma unroll
+        for (int k = 0; k < NC; k++) { seed_d[k] = a.seed_ptr[2 * k]; seed_m[k] = a.seed_ptr[2 * k + 1]; }
+        seed_c = a.seed_ptr[12];
+    }
+
+    uint32_t seq0 = 0;   // sequence number of plane 0 of the current domain (ring slot = seq % R)
+    for (uint32_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+        const uint32_t node = a.items ? a.items[item] : item;
+        const int depth = pos_depth(a.positions[node]);
+        if (depth == -1 || !active_depth(a.substep, (uint32_t)depth, a.max_depth)) continue;   // uniform in the CTA
+
+        if (tid == 0) {
+#pragma unroll 1
+            for (int q = 0; q < R && q < T; q++) {
+                const uint32_t s = (seq0 + q) % R;
+                mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
+#pragma unroll
+                for (int k = 0; k < NC; k++)
+                    bulk_g2s(ring + ((size_t)k * R + s) * PLANE, a.field[k] + ((size_t)node * T + q) * PLANE,
+                             S::PLANE_BYTES, &bars[s]);
+            }
+        }
+        const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
+
+#pragma unroll 1
+        for (uint32_t z = 0; z < (uint32_t)N; z++) {
+            // planes z .. z+2P of the padded domain must have landed
+            bool ok = true;
+            const int j_first = z == 0 ? 0 : 2 * P;
+            for (int j = j_first; j <= 2 * P; j++) {
+                const uint32_t sq = seq0 + z + j;
+                ok &= mbar_wait(&bars[sq % R], (sq / R) & 1u);
+            }
+            if (!ok) s_abort = 1;
+            if (ok) {
+                uint32_t slot[2 * P + 1];
+#pragma unroll
+                for (int j = 0; j <= 2 * P; j++) slot[j] = (seq0 + z + j) % R;
+                const uint32_t zg = node * N + z;
+                const size_t o = ((size_t)zg * N + y) * N + x;   // inner-layout index
+
+                if (KIND == SK_GRAD || KIND == SK_GRAD_HESS) {
+                    auto pl = [&](int j) { return (const float*)(ring + (size_t)slot[j] * PLANE); };
+                    float gx, gy, gz, hx, hy, hz;
+                    fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
+                    int32_t rng = cell_rng(seed_d[0], x, y, zg);
+                    if (KIND == SK_GRAD_HESS)
+                        a.hdiag[o] = cf3_encode(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rng);
+                    a.grad[0][o] = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rng);
+                } else if (KIND == SK_MIXED) {
+                    auto pl = [&](int j) { return (const float*)(ring + (size_t)slot[j] * PLANE); };
+                    const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
+                    int32_t rng = cell_rng(seed_m[0], x, y, zg);
+                    a.hoff[o] = cf3_encode(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rng);
+                } else {   // SK_BSSN
+                    const size_t cz = (size_t)slot[P] * PLANE + c0;
+                    const Sym g{ring[0 * R * PLANE + cz], ring[1 * (size_t)R * PLANE + cz], ring[2 * (size_t)R * PLANE + cz],
+                                ring[3 * (size_t)R * PLANE + cz], ring[4 * (size_t)R * PLANE + cz], ring[5 * (size_t)R * PLANE + cz]};
+                    const Sym ginv = sym_inverse(g);
+                    uint32_t G[6];
+#pragma unroll
+                    for (int k = 0; k < 6; k++) {
+                        const float* base = ring + (size_t)k * R * PLANE;
+                        auto pl = [&](int j) { return base + (size_t)slot[j] * PLANE; };
+                        float gx, gy, gz, hx, hy, hz;
+                        fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
+                        int32_t rd = cell_rng(seed_d[k], x, y, zg);
+                        const uint32_t wh = cf3_encode(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
+                        G[k] = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
+                        a.grad[k][o] = G[k];
+                        const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
+                        int32_t rm = cell_rng(seed_m[k], x, y, zg);
+                        const uint32_t wo = cf3_encode(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
+                        a.lap[k][o] = trace_contra(sym_from_cf3(wh, wo), ginv);
+                    }
+                    int32_t rc = cell_rng(seed_c, x, y, zg);
+                    uint32_t out[6];
+                    christoffel_cell(G, a.christoffel_mode == AMR_CHRISTOFFEL_RAISED ? ginv : g, rc, out);
+#pragma unroll
+                    for (int k = 0; k < 6; k++) a.chr[k][o] = out[k];
+                }
+            }
+            __syncthreads();   // every thread is done with plane z: its slot may be refilled
+            if (s_abort) break;
+            if (tid == 0 && z + R < (uint32_t)T) {
+                const uint32_t q = z + R, sq = seq0 + q, s = sq % R;
+                mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
+#pragma unroll
+                for (int k = 0; k < NC; k++)
+                    bulk_g2s(ring + ((size_t)k * R + s) * PLANE, a.field[k] + ((size_t)node * T + q) * PLANE,
+                             S::PLANE_BYTES, &bars[s]);
+            }
+        }
+        if (s_abort) {
+            if (tid == 0) atomicExch(a.err, 1);
+            return;
+        }
+        seq0 += T;
+    }
+}
+
+// ---------------------------------------------------------------- launch
+template <int N, int P, int KIND>
+cudaError_t launch_stencil_t(const StencilArgs& a, uint32_t grid, cudaStream_t st) {
+    using S = StencilShape<N, P, KIND>;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_stencil<N, P, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    if (grid == 0) return cudaSuccess;
+    k_stencil<N, P, KIND><<<grid, N * N, S::SMEM, st>>>(a);
+    return cudaGetLastError();
+}
+
+#define AMR_STENCIL_INSTANCES(N, P)                                                                      \
+    template cudaError_t launch_stencil_t<N, P, SK_GRAD>(const StencilArgs&, uint32_t, cudaStream_t);      \
+    template cudaError_t launch_stencil_t<N, P, SK_GRAD_HESS>(const StencilArgs&, uint32_t, cudaStream_t); \
+    template cudaError_t launch_stencil_t<N, P, SK_MIXED>(const StencilArgs&, uint32_t, cudaStream_t);     \
+    template size_t stencil_smem_bytes<N, P, SK_GRAD>();                                                   \
+    template size_t stencil_smem_bytes<N, P, SK_BSSN>();
+AMR_FOR_EACH_CONFIG(AMR_STENCIL_INSTANCES)
+
+#define AMR_STENCIL_BSSN_INSTANCES(N, P) \
+    template cudaError_t launch_stencil_t<N, P, SK_BSSN>(const StencilArgs&, uint32_t, cudaStream_t);
+AMR_FOR_EACH_BSSN_CONFIG(AMR_STENCIL_BSSN_INSTANCES)
+
+}  // namespace amr

@@ -1,0 +1,170 @@
+// octree.cpp -- host octree (see octree.h).  Compiled with -ffp-contract=off so the few float
+// operations (boundary offsets) round identically on x86-64 and aarch64.
+#include "octree.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "amr_types.h"
+
+namespace amr {
+
+uint32_t reverse_bits32(uint32_t a) {
+    a = (a >> 16) | (a << 16);
+    a = ((a & 0xFF00FF00u) >> 8) | ((a & 0x00FF00FFu) << 8);
+    a = ((a & 0xF0F0F0F0u) >> 4) | ((a & 0x0F0F0F0Fu) << 4);
+    a = ((a & 0xCCCCCCCCu) >> 2) | ((a & 0x33333333u) << 2);
+    return ((a & 0xAAAAAAAAu) >> 1) | ((a & 0x55555555u) << 1);
+}
+
+// Each axis occupies every third bit of the 27-bit path.  Filling the other axes' bits with ones
+// lets a carry ripple to the next bit of the same axis; a carry or borrow out of bit 24+axis lands
+// in bit 27+axis and means the neighbour lies outside the root.
+namespace {
+constexpr uint32_t kLane = 0x1249249u;       // bits 0, 3, ..., 24
+constexpr uint32_t kLaneOut = 0x9249249u;    // the same plus bit 27
+}
+uint32_t morton_sum(uint32_t a, uint32_t b, bool overflow) {
+    uint32_t r = 0;
+    for (uint32_t axis = 0; axis < 3; axis++) {
+        const uint32_t gaps = (kPathMask & ~kLane) << axis;
+        r |= ((a | gaps) + (b & (kLane << axis))) & (kLaneOut << axis);
+    }
+    return ((r & (7u << 27)) && overflow) ? ~0u : (r & kPathMask);
+}
+uint32_t morton_diff(uint32_t a, uint32_t b, bool overflow) {
+    uint32_t r = 0;
+    for (uint32_t axis = 0; axis < 3; axis++) {
+        const uint32_t lane = kLane << axis;
+        r |= ((a & lane) - (b & lane)) & (kLaneOut << axis);
+    }
+    return ((r & (7u << 27)) && overflow) ? ~0u : (r & kPathMask);
+}
+
+static inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+
+uint32_t cf3_encode_host(float x, float y, float z) {
+    const float v[3] = {x, y, z};
+    uint32_t e = 0;
+    for (int i = 0; i < 3; i++) e = std::max(e, (fbits(v[i]) >> 23) & 255u);
+    const uint32_t E = std::min(std::max(e, 112u) - 112u, 31u);
+    const float scale = 4194304.f / (float)(1u << E);      // 2^(22-E), exact
+    uint32_t w = E << 27;
+    const uint32_t mpos[3] = {0, 9, 18}, spos[3] = {8, 17, 26};
+    for (int i = 0; i < 3; i++) {
+        float s = v[i] * scale;
+        s = fmaxf(-255.f, fminf(s, 255.f));
+        w |= ((uint32_t)(fabsf(s) + .5f) << mpos[i]) | ((uint32_t)(s < 0.f) << spos[i]);
+    }
+    return w;
+}
+
+uint64_t make_boundary(uint32_t this_pos, uint32_t other_pos, int32_t other_idx) {
+    const int td = pos_depth_host(this_pos), od = pos_depth_host(other_pos);
+    const uint32_t node_data = ((uint32_t)other_idx & 16777215u) | (((uint32_t)(td - od) & 15u) << 24) |
+                               (((uint32_t)td & 15u) << 28);
+    // offset of this domain's centre from the other's, in units of the other's half-edge
+    float r[3] = {0.f, 0.f, 0.f};
+    const float mult = .25f * (float)(1u << od);
+    uint32_t s = this_pos & kPathMask;
+    for (int i = 0; i < td; i++, s >>= 3)
+        for (int a = 0; a < 3; a++) r[a] += ((s & (1u << a)) ? mult : -mult) / (float)(1 << i);
+    s = other_pos & kPathMask;
+    for (int i = 0; i < od; i++, s >>= 3)
+        for (int a = 0; a < 3; a++) r[a] -= ((s & (1u << a)) ? mult : -mult) / (float)(1 << i);
+    return (uint64_t)node_data | ((uint64_t)cf3_encode_host(r[0], r[1], r[2]) << 32);
+}
+
+Octree::Octree(uint32_t node_slots, NodeHooks* hooks)
+    : hooks_(hooks), max_slots_(node_slots), positions_(node_slots, ~0u), parent_(node_slots, -1),
+      children_((size_t)node_slots * 8u, -1), boundaries_((size_t)node_slots * 6u, kNoBoundary),
+      lifetime_(node_slots, 0) {
+    positions_[0] = 0u;   // the root
+}
+
+void Octree::increment_timer() {
+    for (uint32_t i = 0; i <= final_used_slot_; i++) {
+        const int depth = pos_depth_host(positions_[i]);
+        if (depth == -1) continue;
+        lifetime_[i] += ((timer_ & ((1u << (uint32_t)(max_depth_ - depth)) - 1u)) == 0u);
+    }
+    timer_ = (timer_ + 1u) & ((1u << (uint32_t)max_depth_) - 1u);
+}
+
+void Octree::add_node(int32_t parent, int32_t offset) {
+    if (first_free_slot_ >= max_slots_ || children_[(size_t)parent * 8u + offset] != -1) return;
+    if (pos_depth_host(positions_[parent]) >= (int)kDepthLimit) return;
+    const uint32_t slot = first_free_slot_;
+    lifetime_[slot] = 0u;
+    parent_[slot] = parent;
+    children_[(size_t)parent * 8u + offset] = (int32_t)slot;
+    positions_[slot] = pos_child(positions_[parent], (uint32_t)offset);
+    const int new_depth = pos_depth_host(positions_[slot]);
+    const int change = std::max(max_depth_, new_depth) - max_depth_;
+    timer_ <<= change;
+    max_depth_ += change;
+    if (hooks_) hooks_->node_ctor((int32_t)slot);
+    final_used_slot_ = std::max(final_used_slot_, slot);
+    while (first_free_slot_ < max_slots_ && pos_depth_host(positions_[first_free_slot_]) != -1) first_free_slot_++;
+    refresh_boundaries(new_depth);
+    dirty_ = true;
+}
+
+void Octree::remove_node_recursive(int32_t node) {
+    if (node == -1 || pos_depth_host(positions_[node]) == -1) return;
+    if (hooks_) hooks_->node_dtor(node);
+    for (uint32_t i = 0; i < 8u; i++) remove_node_recursive(children_[(size_t)node * 8u + i]);
+    children_[(size_t)parent_[node] * 8u + pos_final_offset(positions_[node])] = -1;
+    parent_[node] = -1;
+    positions_[node] = ~0u;
+    first_free_slot_ = std::min(first_free_slot_, (uint32_t)node);
+}
+
+void Octree::remove_node(int32_t node) {
+    if (node == -1) return;
+    const int curr_depth = pos_depth_host(positions_[node]);
+    if (curr_depth == -1) return;
+    remove_node_recursive(node);
+    const int old_max = max_depth_;
+    max_depth_ = 0;
+    for (uint32_t i = 0; i < max_slots_; i++)
+        if (i != (uint32_t)node) max_depth_ = std::max(max_depth_, pos_depth_host(positions_[i]));
+    timer_ >>= (old_max - max_depth_);
+    while (pos_depth_host(positions_[final_used_slot_]) == -1 && final_used_slot_ > 0u) final_used_slot_--;
+    refresh_boundaries(curr_depth);
+    dirty_ = true;
+}
+
+void Octree::refresh_boundaries(int from_depth) {
+    for (uint32_t i = 0; i <= final_used_slot_; i++)
+        if (pos_depth_host(positions_[i]) >= from_depth)
+            for (uint32_t f = 0; f < 6; f++) boundaries_[(size_t)i * 6u + f] = yield_boundary((int32_t)i, f);
+}
+
+uint32_t Octree::find_node_idx(uint32_t packed, uint32_t max_depth) const {
+    uint32_t curr = 0, depth = 0;
+    while (true) {
+        const int32_t c = children_[(size_t)curr * 8u + (packed & 7u)];
+        if (c == -1 || depth >= max_depth) return curr;
+        packed >>= 3u;
+        curr = (uint32_t)c;
+        depth++;
+    }
+}
+
+uint64_t Octree::yield_boundary(int32_t node, uint32_t face) const {
+    static const uint32_t kDirections[3] = {4u, 2u, 1u};   // x, y, z within a reversed level triple
+    const int depth = pos_depth_host(positions_[node]);
+    if (depth <= 0) return kNoBoundary;
+    // Reverse the word so levels are most-significant-first (x in the high bit of each triple),
+    // step one domain along the face normal at this depth, and reverse back.
+    uint32_t p = reverse_bits32(positions_[node]) >> 5u;
+    const uint32_t step = (kDirections[face % 3u] << ((9u - (uint32_t)depth) * 3u)) & kPathMask;
+    p = face < 3 ? morton_sum(p, step, true) : morton_diff(p, step, true);
+    uint32_t neighbour = find_node_idx(reverse_bits32(p) >> 5u, (uint32_t)depth);
+    if (p == ~0u) neighbour = 0;   // outside the root: the root's ghost layer is the source
+    return make_boundary(positions_[node], positions_[neighbour], (int32_t)neighbour);
+}
+
+}  // namespace amr

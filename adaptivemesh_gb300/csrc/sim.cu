@@ -1,0 +1,688 @@
+// sim.cu -- the reference's plugins (AMR_data, AMR.h:296-334) on the GB300 kernels.
+//
+//   BssnSim  ~ BSSN_AMR_data  (BSSN.h:104-171)
+//   WaveSim  ~ wave_AMR_data  (SimpleWave.h:191-279)
+//
+// Both own an Octree (AMR<T>) whose node_ctor hook prolongates new domains, a device mirror of
+// the octree arrays uploaded when the octree changed (AMR<T>::copy_to_gpu, AMR.h:268-275), and a
+// host fast_prng that hands every kernel launch its global seed in the reference's order.
+//
+// Modes: PLAIN issues the reference's launch sequence (one launch per operator and component);
+// BATCHED issues one launch per phase for all components over the list of domains active at the
+// substep; GRAPH replays a captured CUDA graph of one whole BSSN timestep (all substeps).
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "capi_internal.h"
+
+namespace amr {
+
+namespace {
+
+int32_t host_prng_next(int32_t& s) {                       // fast_prng::generate_int, tensors.h:281-285
+    uint32_t v = (uint32_t)s + 1124781675u;
+    v ^= (uint32_t)((int32_t)v >> 7);
+    v *= 1246477263u;
+    s = (int32_t)v;
+    return s;
+}
+
+template <class T>
+cudaError_t dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) { *p = nullptr; return e; }
+    return cudaMemset(*p, 0, count * sizeof(T));
+}
+
+}  // namespace
+
+class SimBase : public NodeHooks {
+public:
+    SimBase(const amr_config& c, uint32_t slots, int mode)
+        : cfg(c), dims(make_dims(c)), geo(make_geo(c)), mode(mode), tree(slots, this) {}
+    virtual ~SimBase() {
+        if (stream) cudaStreamSynchronize(stream);
+        cudaFree(d_positions); cudaFree(d_children); cudaFree(d_boundaries); cudaFree(d_items);
+        cudaFree(ghost_stage);
+        for (auto& ev : events) cudaEventDestroy(ev);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    virtual int init() {
+        const uint32_t s = tree.max_slots();
+        cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = dev_alloc(&d_positions, s);
+        if (e == cudaSuccess) e = dev_alloc(&d_children, (size_t)s * 8u);
+        if (e == cudaSuccess) e = dev_alloc(&d_boundaries, (size_t)s * 6u);
+        if (e == cudaSuccess) e = dev_alloc(&d_items, (size_t)s << kDepthLimit);
+        if (e == cudaSuccess) { err_flag = device_error_flag(); if (!err_flag) e = cudaErrorMemoryAllocation; }
+        if (e == cudaSuccess) {
+            // set the kernels' shared-memory limits now, outside any later stream capture
+            StencilArgs none;
+            std::memset(&none, 0, sizeof(none));
+            for (int kind : {SK_GRAD, SK_GRAD_HESS, SK_MIXED, SK_BSSN}) {
+                if (kind == SK_BSSN && !bssn_fused_supported(&cfg)) continue;
+                e = launch_stencil(cfg, kind, none, 0, stream);
+                if (e != cudaSuccess) break;
+            }
+        }
+        return cuda_status(e);
+    }
+
+    // The plugin interface of the reference (AMR.h:296-334).
+    virtual int copy_back() = 0;
+    virtual int modify_nodes() = 0;
+    virtual int predictor() = 0;
+    virtual int copy_bounds() = 0;
+    virtual int corrector() = 0;
+    virtual int timestep() {
+        do {
+            int st;
+            if ((st = copy_back())) return st;
+            if ((st = modify_nodes())) return st;
+            if ((st = predictor())) return st;
+            if ((st = copy_bounds())) return st;
+            if ((st = corrector())) return st;
+            tree.increment_timer();
+        } while (tree.timer() != 0u);
+        return AMR_OK;
+    }
+    virtual int buffer(int which, int comp, void** ptr, uint64_t* count) = 0;
+
+    void node_dtor(int32_t) override {}
+
+    // AMR<T>::copy_to_gpu (AMR.h:268-275): upload the octree arrays if they changed.
+    int sync_octree() {
+        if (!tree.dirty()) return AMR_OK;
+        const uint32_t s = tree.max_slots();
+        cudaError_t e = cudaMemcpyAsync(d_positions, tree.positions().data(), s * 4u, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_children, tree.children().data(), (size_t)s * 32u, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_boundaries, tree.boundaries().data(), (size_t)s * 48u, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);   // host vectors are pageable
+        if (e != cudaSuccess) return cuda_status(e);
+        tree.mark_clean();
+        items_valid = false;
+        graph_valid = false;
+        return AMR_OK;
+    }
+
+    // Lists of the domains active at each substep of a timestep (batched launches use these).
+    int build_items() {
+        if (items_valid) return AMR_OK;
+        const uint32_t md = (uint32_t)tree.read_max_depth(), used = tree.curr_used_slots();
+        const uint32_t nsub = 1u << md;
+        std::vector<uint32_t> all;
+        item_offset.assign(nsub, 0);
+        item_count.assign(nsub, 0);
+        for (uint32_t s = 0; s < nsub; s++) {
+            item_offset[s] = (uint32_t)all.size();
+            for (uint32_t i = 0; i < used; i++) {
+                const int d = pos_depth_host(tree.positions()[i]);
+                if (d != -1 && (s & ((1u << (md - (uint32_t)d)) - 1u)) == 0u) all.push_back(i);
+            }
+            item_count[s] = (uint32_t)all.size() - item_offset[s];
+        }
+        cudaError_t e = cudaMemcpyAsync(d_items, all.data(), all.size() * 4u, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        items_valid = true;
+        return AMR_OK;
+    }
+
+    int ensure_ghost_stage(int ncomp) {
+        const size_t need = ghost_scratch_floats(dims, tree.max_slots(), ncomp);
+        if (need <= ghost_stage_floats) return AMR_OK;
+        cudaStreamSynchronize(stream);
+        cudaFree(ghost_stage);
+        ghost_stage_floats = 0;
+        cudaError_t e = dev_alloc(&ghost_stage, need);
+        if (e != cudaSuccess) return cuda_status(e);
+        ghost_stage_floats = need;
+        return AMR_OK;
+    }
+
+    int32_t next_seed() { return host_prng_next(rng); }
+    int check(cudaError_t e) {
+        if (e != cudaSuccess) return cuda_status(e);
+        launches++;
+        return AMR_OK;
+    }
+    // Optional CUDA-event timing of the dominant kernel.
+    void time_begin() {
+        if (!timing || capturing) return;
+        if (ev_used + 2 > events.size()) {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a); cudaEventCreate(&b);
+            events.push_back(a); events.push_back(b);
+        }
+        cudaEventRecord(events[ev_used], stream);
+    }
+    void time_end() {
+        if (!timing || capturing) return;
+        cudaEventRecord(events[ev_used + 1], stream);
+        ev_used += 2;
+    }
+    int harvest_timing(double* ms, uint64_t* n) {
+        cudaError_t e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        for (size_t i = 0; i + 1 < ev_used; i += 2) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, events[i], events[i + 1]);
+            timed_ms += t;
+            timed_launches++;
+        }
+        ev_used = 0;
+        *ms = timed_ms;
+        *n = timed_launches;
+        timed_ms = 0.0;
+        timed_launches = 0;
+        return AMR_OK;
+    }
+
+    amr_config cfg;
+    Dims dims;
+    Geo geo;
+    int mode;
+    Octree tree;
+    cudaStream_t stream = nullptr;
+    uint32_t* d_positions = nullptr;
+    int32_t* d_children = nullptr;
+    uint64_t* d_boundaries = nullptr;
+    uint32_t* d_items = nullptr;
+    std::vector<uint32_t> item_offset, item_count;
+    bool items_valid = false;
+    bool graph_valid = false;
+    bool capturing = false;
+    int* err_flag = nullptr;
+    float* ghost_stage = nullptr;
+    size_t ghost_stage_floats = 0;
+    int32_t rng = 12894712;      // fast_prng default seed, tensors.h:280
+    uint64_t launches = 0;
+    bool timing = false;
+    std::vector<cudaEvent_t> events;
+    size_t ev_used = 0;
+    double timed_ms = 0.0;
+    uint64_t timed_launches = 0;
+};
+
+// ============================================================================ BSSN
+class BssnSim : public SimBase {
+public:
+    using SimBase::SimBase;
+    ~BssnSim() override {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        for (int k = 0; k < 6; k++) {
+            cudaFree(old6[k]); cudaFree(new6[k]); cudaFree(ricci6[k]); cudaFree(dmet6[k]); cudaFree(chr6[k]);
+        }
+        for (int k = 0; k < 4; k++) cudaFree(hint[k]);
+        cudaFree(d_seeds);
+        for (int k = 0; k < 2; k++) { if (h_seeds[k]) cudaFreeHost(h_seeds[k]); if (seed_ev[k]) cudaEventDestroy(seed_ev[k]); }
+    }
+    int init() override {
+        int st = SimBase::init();
+        if (st) return st;
+        const size_t s = tree.max_slots();
+        const size_t padded = s * dims.t * dims.t * dims.t, inner = s * dims.n * dims.n * dims.n;
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 6 && e == cudaSuccess; k++) {
+            e = dev_alloc(&old6[k], padded);
+            if (e == cudaSuccess) e = dev_alloc(&new6[k], padded);
+            if (e == cudaSuccess) e = dev_alloc(&ricci6[k], inner);
+            if (e == cudaSuccess) e = dev_alloc(&dmet6[k], inner);
+            if (e == cudaSuccess) e = dev_alloc(&chr6[k], inner);
+        }
+        for (int k = 0; k < 4 && e == cudaSuccess; k++) e = dev_alloc(&hint[k], inner);   // didjA / didjW
+        if (e == cudaSuccess) e = dev_alloc(&d_seeds, (size_t)kSeedsPerSubstep << kDepthLimit);
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+            e = cudaMallocHost(&h_seeds[k], sizeof(int32_t) * ((size_t)kSeedsPerSubstep << kDepthLimit));
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&seed_ev[k], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) return cuda_status(e);
+        return ensure_ghost_stage(6);
+    }
+    // BSSN_AMR_data::node_ctor (BSSN.h:131-137): prolongate old and new metric into the child.
+    void node_ctor(int32_t node) override {
+        const uint32_t off = (uint32_t)pos_final_offset(tree.positions()[node]);
+        const int32_t parent = tree.parents()[node];
+        for (int k = 0; k < 6; k++) check(launch_copy_to_child(dims, old6[k], off, node, parent, stream));
+        for (int k = 0; k < 6; k++) check(launch_copy_to_child(dims, new6[k], off, node, parent, stream));
+        graph_valid = false;
+    }
+
+    // --- phases
+    int copy_back() override {                                   // BSSN.h:126-130
+        int st = sync_octree();
+        if (st) return st;
+        const uint32_t s = tree.timer(), md = (uint32_t)tree.read_max_depth(), used = tree.curr_used_slots();
+        FieldSet f;
+        std::memset(&f, 0, sizeof(f));
+        if (mode == AMR_MODE_PLAIN) {
+            f.ncomp = 1;
+            for (int k = 0; k < 6; k++) {
+                f.old_f[0] = old6[k]; f.new_f[0] = new6[k];
+                if ((st = check(launch_copy_new_to_old(dims, f, d_positions, d_children, nullptr, used, s, md, stream)))) return st;
+            }
+            return AMR_OK;
+        }
+        if ((st = build_items())) return st;
+        f.ncomp = 6;
+        for (int k = 0; k < 6; k++) { f.old_f[k] = old6[k]; f.new_f[k] = new6[k]; }
+        return check(launch_copy_new_to_old(dims, f, d_positions, d_children, d_items + item_offset[s], item_count[s], s,
+                                            md, stream));
+    }
+    int modify_nodes() override { return AMR_OK; }              // BSSN.h:139-142
+    int predictor() override { return derivatives(old6, seed_slot(0)); }
+    int corrector() override { return derivatives(new6, seed_slot(1)); }
+    int copy_bounds() override {                                 // BSSN.h:149-153
+        int st = sync_octree();
+        if (st) return st;
+        const uint32_t s = tree.timer(), md = (uint32_t)tree.read_max_depth(), used = tree.curr_used_slots();
+        FieldSet f;
+        std::memset(&f, 0, sizeof(f));
+        if (mode == AMR_MODE_PLAIN) {
+            f.ncomp = 1;
+            for (int k = 0; k < 6; k++) {
+                f.old_f[0] = old6[k]; f.new_f[0] = new6[k];
+                if ((st = check(launch_copy_boundaries(dims, f, d_boundaries, used, s, md, 1, ghost_stage, stream)))) return st;
+                launches++;   // gather + scatter
+            }
+            return AMR_OK;
+        }
+        f.ncomp = 6;
+        for (int k = 0; k < 6; k++) { f.old_f[k] = old6[k]; f.new_f[k] = new6[k]; }
+        st = check(launch_copy_boundaries(dims, f, d_boundaries, used, s, md, 1, ghost_stage, stream));
+        if (!st) launches++;
+        return st;
+    }
+
+    int timestep() override {
+        if (mode != AMR_MODE_GRAPH) {
+            seeds_from_device = false;
+            return SimBase::timestep();
+        }
+        return graph_timestep();
+    }
+
+    int buffer(int which, int comp, void** ptr, uint64_t* count) override {
+        if (comp < 0 || comp > 5) return AMR_ERR_INVALID;
+        const uint64_t s = tree.max_slots();
+        switch (which) {
+            case 0: *ptr = old6[comp]; *count = s * dims.t * dims.t * dims.t; return AMR_OK;
+            case 1: *ptr = new6[comp]; *count = s * dims.t * dims.t * dims.t; return AMR_OK;
+            case 2: *ptr = ricci6[comp]; *count = s * dims.n * dims.n * dims.n; return AMR_OK;
+            case 3: *ptr = dmet6[comp]; *count = s * dims.n * dims.n * dims.n; return AMR_OK;
+            case 4: *ptr = chr6[comp]; *count = s * dims.n * dims.n * dims.n; return AMR_OK;
+            default: return AMR_ERR_INVALID;
+        }
+    }
+
+private:
+    static constexpr int kSeedsPerSubstep = 26;   // 13 per predictor / corrector
+
+    // Where this phase's 13 seeds come from: the host generator (plain/batched) or, inside a
+    // captured graph, the device array filled before each replay.
+    const int32_t* seed_slot(int phase) const {
+        return seeds_from_device ? d_seeds + (size_t)tree.timer() * kSeedsPerSubstep + phase * 13 : nullptr;
+    }
+
+    // metric_derivatives_noncovariant + compute_raised_christoffel_symbols (BSSN.h:38-102)
+    int derivatives(float* const* g, const int32_t* dev_seeds) {
+        int st = sync_octree();
+        if (st) return st;
+        const uint32_t s = tree.timer(), md = (uint32_t)tree.read_max_depth(), used = tree.curr_used_slots();
+        StencilArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.positions = d_positions;
+        a.substep = s;
+        a.max_depth = md;
+        a.geo = geo;
+        a.err = err_flag;
+        a.christoffel_mode = AMR_CHRISTOFFEL_REFERENCE;
+        if (!dev_seeds) {
+            for (int k = 0; k < 6; k++) { a.seed_d[k] = next_seed(); a.seed_m[k] = next_seed(); }
+            a.seed_c = next_seed();
+        }
+        a.seed_ptr = dev_seeds;
+        if (mode == AMR_MODE_PLAIN || !bssn_fused_supported(&cfg)) {
+            a.items = nullptr;
+            a.n_items = used;
+            for (int k = 0; k < 6; k++) {
+                // the reference alternates two intermediate Hessians between two streams
+                uint32_t* hd = hint[(k & 1) * 2], *ho = hint[(k & 1) * 2 + 1];
+                StencilArgs b = a;
+                b.seed_ptr = nullptr;
+                b.field[0] = g[k]; b.grad[0] = dmet6[k]; b.hdiag = hd; b.seed_d[0] = a.seed_d[k];
+                time_begin();
+                if ((st = check(launch_stencil(cfg, SK_GRAD_HESS, b, stencil_grid(cfg, SK_GRAD_HESS, used), stream)))) return st;
+                time_end();
+                b.hoff = ho; b.seed_m[0] = a.seed_m[k];
+                if ((st = check(launch_stencil(cfg, SK_MIXED, b, stencil_grid(cfg, SK_MIXED, used), stream)))) return st;
+                if ((st = check(launch_deriv_trace(dims, hd, ho, g, ricci6[k], d_positions, used, s, md, stream)))) return st;
+            }
+            return check(launch_christoffel(dims, g, dmet6, a.seed_c, chr6, d_positions, used, s, md,
+                                            AMR_CHRISTOFFEL_REFERENCE, stream));
+        }
+        if ((st = build_items())) return st;
+        a.items = d_items + item_offset[s];
+        a.n_items = item_count[s];
+        for (int k = 0; k < 6; k++) { a.field[k] = g[k]; a.grad[k] = dmet6[k]; a.lap[k] = ricci6[k]; a.chr[k] = chr6[k]; }
+        time_begin();
+        st = check(launch_stencil(cfg, SK_BSSN, a, stencil_grid(cfg, SK_BSSN, a.n_items), stream));
+        time_end();
+        return st;
+    }
+
+    // One timestep from a captured graph: the host draws the seeds of every launch of the
+    // timestep in the reference's order, uploads them, and replays the graph.
+    int graph_timestep() {
+        int st = sync_octree();
+        if (st) return st;
+        if ((st = build_items())) return st;
+        if (tree.timer() != 0u) {   // a timestep always starts at counter 0 (AMR.h:324-333)
+            seeds_from_device = false;
+            return SimBase::timestep();
+        }
+        const uint32_t nsub = 1u << tree.read_max_depth();
+        if (!graph_valid) {
+            if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+            cudaGraph_t graph;
+            cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_status(e);
+            capturing = true;
+            seeds_from_device = true;
+            const uint64_t before = launches;
+            st = SimBase::timestep();        // records every launch; the counter returns to 0
+            capturing = false;
+            seeds_from_device = false;
+            e = cudaStreamEndCapture(stream, &graph);
+            if (st) { if (e == cudaSuccess) cudaGraphDestroy(graph); return st; }
+            if (e != cudaSuccess) return cuda_status(e);
+            e = cudaGraphInstantiate(&graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(e);
+            graph_launches = launches - before;
+            launches = before;
+            graph_valid = true;
+        }
+        const int b = seed_buf;
+        seed_buf ^= 1;
+        cudaError_t e = cudaEventSynchronize(seed_ev[b]);       // the buffer's previous upload has finished
+        if (e != cudaSuccess) return cuda_status(e);
+        for (uint32_t s = 0; s < nsub; s++)
+            for (int i = 0; i < kSeedsPerSubstep; i++) h_seeds[b][(size_t)s * kSeedsPerSubstep + i] = next_seed();
+        e = cudaMemcpyAsync(d_seeds, h_seeds[b], sizeof(int32_t) * nsub * kSeedsPerSubstep, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaEventRecord(seed_ev[b], stream);
+        if (e == cudaSuccess) e = cudaGraphLaunch(graph_exec, stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        launches += graph_launches;
+        return AMR_OK;
+    }
+
+    float* old6[6] = {};
+    float* new6[6] = {};
+    float* ricci6[6] = {};
+    uint32_t* dmet6[6] = {};
+    uint32_t* chr6[6] = {};
+    uint32_t* hint[4] = {};
+    int32_t* d_seeds = nullptr;
+    int32_t* h_seeds[2] = {};
+    cudaEvent_t seed_ev[2] = {};
+    int seed_buf = 0;
+    bool seeds_from_device = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_launches = 0;
+};
+
+// ============================================================================ SimpleWave
+class WaveSim : public SimBase {
+public:
+    using SimBase::SimBase;
+    ~WaveSim() override {
+        if (stream) cudaStreamSynchronize(stream);
+        cudaFree(old_f); cudaFree(new_f); cudaFree(derivs); cudaFree(hess); cudaFree(crit);
+        if (crit_host) cudaFreeHost(crit_host);
+    }
+    int init() override {
+        int st = SimBase::init();
+        if (st) return st;
+        const size_t s = tree.max_slots();
+        const size_t padded = s * dims.t * dims.t * dims.t, inner = s * dims.n * dims.n * dims.n;
+        cudaError_t e = dev_alloc(&old_f, padded);
+        if (e == cudaSuccess) e = dev_alloc(&new_f, padded);
+        if (e == cudaSuccess) e = dev_alloc(&derivs, inner);
+        if (e == cudaSuccess) e = dev_alloc(&hess, inner);
+        if (e == cudaSuccess) e = dev_alloc(&crit, s * dims.n * dims.n);
+        if (e == cudaSuccess) e = cudaMallocHost(&crit_host, sizeof(float) * s * dims.n * dims.n);
+        if (e != cudaSuccess) return cuda_status(e);
+        return ensure_ghost_stage(1);
+    }
+    void node_ctor(int32_t node) override {                     // SimpleWave.h:219-225
+        const uint32_t off = (uint32_t)pos_final_offset(tree.positions()[node]);
+        const int32_t parent = tree.parents()[node];
+        check(launch_copy_to_child(dims, old_f, off, node, parent, stream));
+        check(launch_copy_to_child(dims, new_f, off, node, parent, stream));
+    }
+    int copy_back() override {                                   // SimpleWave.h:214-218
+        int st = sync_octree();
+        if (st) return st;
+        FieldSet f;
+        std::memset(&f, 0, sizeof(f));
+        f.old_f[0] = old_f; f.new_f[0] = new_f; f.ncomp = 1;
+        return check(launch_copy_new_to_old(dims, f, d_positions, d_children, nullptr, tree.curr_used_slots(), tree.timer(),
+                                            (uint32_t)tree.read_max_depth(), stream));
+    }
+    // amr_criterion (SimpleWave.h:142-187) followed by the triage of modify_nodes (:228-248).
+    int modify_nodes() override {
+        int st = sync_octree();
+        if (st) return st;
+        const uint32_t used = tree.curr_used_slots(), n = dims.n;
+        if ((st = check(launch_criterion(dims, geo, derivs, hess, crit, d_positions, used, tree.timer(),
+                                         (uint32_t)tree.read_max_depth(), stream)))) return st;
+        launches++;
+        cudaError_t e = cudaMemcpyAsync(crit_host, crit, sizeof(float) * used * n * n, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        float* c = crit_host;
+        float avg1 = 0.f, avg2 = 0.f;
+        uint32_t active = 0;
+        const uint32_t nn = n * n;
+        for (uint32_t i = 0; i < used; i++) {
+            const uint32_t b = i * nn, h = n >> 1, q4 = nn >> 2, q2 = nn >> 1;
+            c[i * 8u] = c[b];
+            c[i * 8u + 1u] = c[b + h];
+            c[i * 8u + 2u] = c[b + q4];
+            c[i * 8u + 3u] = c[b + h + q4];
+            c[i * 8u + 4u] = c[b + q2];
+            c[i * 8u + 5u] = c[b + h + q2];
+            c[i * 8u + 6u] = c[b + q4 + q2];
+            c[i * 8u + 7u] = c[b + h + q4 + q2];
+            for (int j = 0; j < 8; j++)
+                if (!std::isnan(c[i * 8u + j])) avg2 += fmaxf(0.f, fminf(c[i * 8u + j], 2.f));
+        }
+        for (uint32_t i = 0; i < used; i++) {
+            float t = c[i * 8u];
+            for (int j = 1; j < 8; j++) t = fmaxf(t, c[i * 8u + j]);
+            c[i + used * 8u] = t;
+            if (!std::isnan(t)) { avg1 += fmaxf(0.f, fminf(t, 2.f)); active++; }
+        }
+        float ax = avg1 / (float)active, ay = (avg2 * .125f) / (float)active;
+        if (used == 1u) ax = ay = .15f;
+        const float urgency = (float)(used - 1u) / (float)tree.max_slots();
+        for (uint32_t i = 1, s = used; i < s; i++) {               // root cannot be removed
+            const float ratio = (float)pos_depth_host(tree.positions()[i]) / (float)tree.read_max_depth();
+            if (ratio <= 0.f) continue;
+            const float life = fmaxf(0.f, fminf((float)tree.lifetime()[i] * .1f - .2f, 1.f));
+            const float weight = life * urgency * urgency * ax * std::sqrt(ratio);
+            if (c[s * 8u + i] < weight) tree.remove_node((int32_t)i);
+        }
+        for (uint32_t i = 0, s = used * 8u; i < s; i++) {
+            const float weight = ay * 3.f / (1.f - urgency);
+            if (c[i] > weight && tree.children()[i] == -1) tree.add_node((int32_t)(i >> 3u), (int32_t)(i & 7u));
+        }
+        return AMR_OK;
+    }
+    int predictor() override {                                   // SimpleWave.h:249-255
+        int st = sync_octree();
+        if (st) return st;
+        if ((st = differentiate(old_f))) return st;
+        return check(launch_wave_step(dims, geo, 0, old_f, derivs, hess, new_f, d_positions, tree.curr_used_slots(),
+                                      tree.timer(), (uint32_t)tree.read_max_depth(), stream));
+    }
+    int copy_bounds() override {                                 // SimpleWave.h:256-260
+        int st = sync_octree();
+        if (st) return st;
+        FieldSet f;
+        std::memset(&f, 0, sizeof(f));
+        f.old_f[0] = old_f; f.new_f[0] = new_f; f.ncomp = 1;
+        st = check(launch_copy_boundaries(dims, f, d_boundaries, tree.curr_used_slots(), tree.timer(),
+                                          (uint32_t)tree.read_max_depth(), 1, ghost_stage, stream));
+        if (!st) launches++;
+        return st;
+    }
+    int corrector() override {                                   // SimpleWave.h:261-267
+        int st = sync_octree();
+        if (st) return st;
+        if ((st = differentiate(new_f))) return st;
+        return check(launch_wave_step(dims, geo, 1, old_f, derivs, hess, new_f, d_positions, tree.curr_used_slots(),
+                                      tree.timer(), (uint32_t)tree.read_max_depth(), stream));
+    }
+    int buffer(int which, int comp, void** ptr, uint64_t* count) override {
+        if (comp != 0) return AMR_ERR_INVALID;
+        const uint64_t s = tree.max_slots();
+        switch (which) {
+            case 0: *ptr = old_f; *count = s * dims.t * dims.t * dims.t; return AMR_OK;
+            case 1: *ptr = new_f; *count = s * dims.t * dims.t * dims.t; return AMR_OK;
+            case 3: *ptr = derivs; *count = s * dims.n * dims.n * dims.n; return AMR_OK;
+            case 4: *ptr = hess; *count = s * dims.n * dims.n * dims.n; return AMR_OK;
+            case 5: *ptr = crit; *count = s * dims.n * dims.n; return AMR_OK;
+            default: return AMR_ERR_INVALID;
+        }
+    }
+
+private:
+    int differentiate(const float* field) {
+        StencilArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.positions = d_positions;
+        a.n_items = tree.curr_used_slots();
+        a.substep = tree.timer();
+        a.max_depth = (uint32_t)tree.read_max_depth();
+        a.geo = geo;
+        a.err = err_flag;
+        a.field[0] = field;
+        a.grad[0] = derivs;
+        a.hdiag = hess;
+        a.seed_d[0] = next_seed();
+        time_begin();
+        const int st = check(launch_stencil(cfg, SK_GRAD_HESS, a, stencil_grid(cfg, SK_GRAD_HESS, a.n_items), stream));
+        time_end();
+        return st;
+    }
+    float* old_f = nullptr;
+    float* new_f = nullptr;
+    uint32_t* derivs = nullptr;
+    uint32_t* hess = nullptr;
+    float* crit = nullptr;
+    float* crit_host = nullptr;
+};
+
+}  // namespace amr
+
+using namespace amr;
+
+#define AMR_API extern "C" __attribute__((visibility("default")))
+
+struct amr_sim {
+    SimBase* impl;
+};
+
+AMR_API int amr_sim_create(const amr_config* cfg, int kind, uint32_t node_slots, int mode, amr_sim** out) {
+    if (!cfg || !out || node_slots < 1u || node_slots > (1u << 23)) return AMR_ERR_INVALID;
+    if (!config_supported(cfg)) return AMR_ERR_UNSUPPORTED;
+    if (mode < AMR_MODE_PLAIN || mode > AMR_MODE_GRAPH) return AMR_ERR_INVALID;
+    if (kind == AMR_SIM_WAVE && cfg->size_domain % 4u != 0u) return AMR_ERR_UNSUPPORTED;
+    SimBase* s = nullptr;
+    if (kind == AMR_SIM_BSSN) s = new (std::nothrow) BssnSim(*cfg, node_slots, mode);
+    else if (kind == AMR_SIM_WAVE) s = new (std::nothrow) WaveSim(*cfg, node_slots, mode == AMR_MODE_GRAPH ? AMR_MODE_BATCHED : mode);
+    else return AMR_ERR_INVALID;
+    if (!s) return AMR_ERR_CAPACITY;
+    const int st = s->init();
+    if (st) { delete s; return st; }
+    *out = new (std::nothrow) amr_sim{s};
+    if (!*out) { delete s; return AMR_ERR_CAPACITY; }
+    return AMR_OK;
+}
+AMR_API int amr_sim_destroy(amr_sim* s) {
+    if (!s) return AMR_ERR_INVALID;
+    delete s->impl;
+    delete s;
+    return AMR_OK;
+}
+AMR_API int amr_sim_set_mode(amr_sim* s, int mode) {
+    if (!s || mode < AMR_MODE_PLAIN || mode > AMR_MODE_GRAPH) return AMR_ERR_INVALID;
+    if (dynamic_cast<WaveSim*>(s->impl) && mode == AMR_MODE_GRAPH) mode = AMR_MODE_BATCHED;
+    if (mode == AMR_MODE_GRAPH && s->impl->timing) return AMR_ERR_INVALID;
+    s->impl->mode = mode;
+    s->impl->graph_valid = false;
+    return AMR_OK;
+}
+AMR_API int amr_sim_add_node(amr_sim* s, int32_t parent, int32_t offset) {
+    if (!s || parent < 0 || (uint32_t)parent >= s->impl->tree.max_slots() || offset < 0 || offset > 7) return AMR_ERR_INVALID;
+    s->impl->tree.add_node(parent, offset);
+    return AMR_OK;
+}
+AMR_API int amr_sim_remove_node(amr_sim* s, int32_t node) {
+    if (!s || node < -1 || node >= (int32_t)s->impl->tree.max_slots()) return AMR_ERR_INVALID;
+    s->impl->tree.remove_node(node);
+    return AMR_OK;
+}
+AMR_API int amr_sim_octree_state(const amr_sim* s, uint32_t* positions, int32_t* parent, int32_t* children,
+                                 uint64_t* boundaries, uint32_t* lifetime, uint32_t* scalars) {
+    if (!s) return AMR_ERR_INVALID;
+    return octree_state_impl(s->impl->tree, positions, parent, children, boundaries, lifetime, scalars);
+}
+AMR_API int amr_sim_buffer(amr_sim* s, int which, int comp, void** ptr, uint64_t* count) {
+    if (!s || !ptr || !count) return AMR_ERR_INVALID;
+    return s->impl->buffer(which, comp, ptr, count);
+}
+AMR_API int amr_sim_timestep(amr_sim* s) { return s ? s->impl->timestep() : AMR_ERR_INVALID; }
+AMR_API int amr_sim_copy_bounds(amr_sim* s) { return s ? s->impl->copy_bounds() : AMR_ERR_INVALID; }
+AMR_API int amr_sim_rng(const amr_sim* s, int32_t* seed) {
+    if (!s || !seed) return AMR_ERR_INVALID;
+    *seed = s->impl->rng;
+    return AMR_OK;
+}
+AMR_API int amr_sim_set_rng(amr_sim* s, int32_t seed) {
+    if (!s) return AMR_ERR_INVALID;
+    s->impl->rng = seed;
+    return AMR_OK;
+}
+AMR_API int amr_sim_stream(amr_sim* s, void** stream) {
+    if (!s || !stream) return AMR_ERR_INVALID;
+    *stream = s->impl->stream;
+    return AMR_OK;
+}
+AMR_API int amr_sim_synchronize(amr_sim* s) {
+    if (!s) return AMR_ERR_INVALID;
+    int st = cuda_status(cudaStreamSynchronize(s->impl->stream));
+    if (st) return st;
+    int h = 0;
+    if (cudaMemcpy(&h, s->impl->err_flag, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return AMR_ERR_CUDA;
+    return h ? AMR_ERR_CUDA : AMR_OK;
+}
+AMR_API uint64_t amr_sim_kernel_launches(const amr_sim* s) { return s ? s->impl->launches : 0u; }
+AMR_API int amr_sim_enable_kernel_timing(amr_sim* s, int enable) {
+    if (!s) return AMR_ERR_INVALID;
+    if (enable && s->impl->mode == AMR_MODE_GRAPH) return AMR_ERR_INVALID;
+    s->impl->timing = enable != 0;
+    return AMR_OK;
+}
+AMR_API int amr_sim_kernel_timing(amr_sim* s, double* ms, uint64_t* n) {
+    if (!s || !ms || !n) return AMR_ERR_INVALID;
+    return s->impl->harvest_timing(ms, n);
+}

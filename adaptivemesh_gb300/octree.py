@@ -1,0 +1,152 @@
+"""Python handles of the C++ octree and plugin simulations (include/amr_gb300.h)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import MODE_GRAPH, SIM_BSSN, Config, VP, U64, check, load
+
+
+def _state(fn, h, slots: int) -> dict:
+    pos = np.zeros(slots, np.uint32)
+    par = np.zeros(slots, np.int32)
+    ch = np.zeros(slots * 8, np.int32)
+    bd = np.zeros(slots * 6, np.uint64)
+    life = np.zeros(slots, np.uint32)
+    sc = np.zeros(5, np.uint32)
+    check(fn(h, pos.ctypes.data, par.ctypes.data, ch.ctypes.data, bd.ctypes.data, life.ctypes.data, sc.ctypes.data),
+          "octree_state")
+    return {"positions": pos, "parent": par, "children": ch, "boundaries": bd, "lifetime": life,
+            "timer": int(sc[0]), "max_depth": int(sc[1]), "first_free": int(sc[2]), "used_slots": int(sc[3]),
+            "max_slots": int(sc[4])}
+
+
+class Octree:
+    """The reference's AMR<T> host octree (AdaptiveMesh/AMR.h:118-294) without device data."""
+
+    def __init__(self, slots: int):
+        self.slots = slots
+        h = VP()
+        check(load().amr_octree_create(slots, ctypes.byref(h)), "amr_octree_create")
+        self.h = h
+
+    def add_node(self, parent: int, offset: int) -> None:
+        check(load().amr_octree_add_node(self.h, parent, offset), "amr_octree_add_node")
+
+    def remove_node(self, node: int) -> None:
+        check(load().amr_octree_remove_node(self.h, node), "amr_octree_remove_node")
+
+    def increment_timer(self) -> None:
+        check(load().amr_octree_increment_timer(self.h), "amr_octree_increment_timer")
+
+    def find_node_idx(self, packed: int, max_depth: int = 0xFFFFFFFF) -> int:
+        return int(load().amr_octree_find_node_idx(self.h, packed, max_depth))
+
+    def state(self) -> dict:
+        return _state(load().amr_octree_state, self.h, self.slots)
+
+    def close(self) -> None:
+        if self.h:
+            load().amr_octree_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Sim:
+    """A reference plugin (BSSN_AMR_data or wave_AMR_data) driven through the C ABI."""
+
+    # buffer ids of amr_sim_buffer
+    OLD, NEW, RICCI, DMET, CHR = 0, 1, 2, 3, 4
+    WAVE_DERIVS, WAVE_HESS, WAVE_CRIT = 3, 4, 5
+
+    def __init__(self, cfg: Config, kind: int = SIM_BSSN, slots: int = 128, mode: int = MODE_GRAPH):
+        self.cfg, self.kind, self.slots = cfg, kind, slots
+        h = VP()
+        check(load().amr_sim_create(ctypes.byref(cfg), kind, slots, mode, ctypes.byref(h)), "amr_sim_create")
+        self.h = h
+
+    def set_mode(self, mode: int) -> None:
+        check(load().amr_sim_set_mode(self.h, mode), "amr_sim_set_mode")
+
+    def add_node(self, parent: int, offset: int) -> None:
+        check(load().amr_sim_add_node(self.h, parent, offset), "amr_sim_add_node")
+
+    def remove_node(self, node: int) -> None:
+        check(load().amr_sim_remove_node(self.h, node), "amr_sim_remove_node")
+
+    def state(self) -> dict:
+        return _state(load().amr_sim_octree_state, self.h, self.slots)
+
+    def buffer(self, which: int, comp: int = 0) -> tuple[int, int]:
+        """(device address, element count) of a simulation buffer."""
+        p, n = VP(), U64()
+        check(load().amr_sim_buffer(self.h, which, comp, ctypes.byref(p), ctypes.byref(n)), "amr_sim_buffer")
+        return int(p.value or 0), int(n.value)
+
+    def tensor(self, which: int, comp: int = 0, dtype=None):
+        """A torch view of a simulation buffer (float32 or int32 for compressed words)."""
+        import torch
+        addr, n = self.buffer(which, comp)
+        if dtype is None:
+            floaty = which in (self.OLD, self.NEW) or (self.kind == SIM_BSSN and which == self.RICCI) or \
+                (self.kind != SIM_BSSN and which == self.WAVE_CRIT)
+            dtype = torch.float32 if floaty else torch.int32
+        typestr = {torch.float32: "<f4", torch.int32: "<i4"}[dtype]
+
+        class _Mem:
+            __cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (addr, False), "version": 3}
+        return torch.as_tensor(_Mem(), device="cuda")
+
+    def timestep(self) -> None:
+        check(load().amr_sim_timestep(self.h), "amr_sim_timestep")
+
+    def copy_bounds(self) -> None:
+        check(load().amr_sim_copy_bounds(self.h), "amr_sim_copy_bounds")
+
+    @property
+    def rng(self) -> int:
+        s = ctypes.c_int32()
+        check(load().amr_sim_rng(self.h, ctypes.byref(s)), "amr_sim_rng")
+        return int(s.value)
+
+    @rng.setter
+    def rng(self, seed: int) -> None:
+        check(load().amr_sim_set_rng(self.h, seed), "amr_sim_set_rng")
+
+    @property
+    def stream(self) -> int:
+        s = VP()
+        check(load().amr_sim_stream(self.h, ctypes.byref(s)), "amr_sim_stream")
+        return int(s.value or 0)
+
+    def synchronize(self) -> None:
+        check(load().amr_sim_synchronize(self.h), "amr_sim_synchronize")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(load().amr_sim_kernel_launches(self.h))
+
+    def enable_kernel_timing(self, enable: bool = True) -> None:
+        check(load().amr_sim_enable_kernel_timing(self.h, 1 if enable else 0), "amr_sim_enable_kernel_timing")
+
+    def kernel_timing(self) -> tuple[float, int]:
+        ms, n = ctypes.c_double(), U64()
+        check(load().amr_sim_kernel_timing(self.h, ctypes.byref(ms), ctypes.byref(n)), "amr_sim_kernel_timing")
+        return float(ms.value), int(n.value)
+
+    def close(self) -> None:
+        if self.h:
+            load().amr_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

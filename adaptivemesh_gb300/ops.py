@@ -1,0 +1,91 @@
+"""Operator-level entry points on caller-owned device buffers (torch tensors or raw addresses).
+
+Each function forwards to the C ABI entry point of the same name (include/amr_gb300.h) and
+raises AmrError on a non-zero status.  Argument order and meaning follow the reference's
+operator wrappers, cited per function.
+"""
+from __future__ import annotations
+
+import ctypes
+
+from . import Config, _p, _ptr_array, check, load
+
+
+def _s(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream   # torch.cuda.Stream
+
+
+def cf3_encode(xyz, out, seeds=None, stream=None) -> None:
+    """compressed_float3 encode of n triples (tensors.h:350-393); seeds=None: deterministic."""
+    n = out.numel()
+    check(load().amr_cf3_encode(_p(xyz), _p(seeds), n, _p(out), _s(stream)), "amr_cf3_encode")
+
+
+def cf3_decode(words, xyz, stream=None) -> None:
+    """compressed_float3 decode (tensors.h:335-348)."""
+    check(load().amr_cf3_decode(_p(words), words.numel(), _p(xyz), _s(stream)), "amr_cf3_decode")
+
+
+def differentiate(cfg: Config, field, dif, d2if, positions, used: int, substep: int, max_depth: int, seed: int,
+                  stream=None) -> None:
+    """differentiate() (AMR.h:1280-1302)."""
+    check(load().amr_differentiate(ctypes.byref(cfg), _p(field), _p(dif), _p(d2if), _p(positions), used, substep,
+                                   max_depth, seed, _s(stream)), "amr_differentiate")
+
+
+def mixed_partials(cfg: Config, field, off, positions, used: int, substep: int, max_depth: int, seed: int,
+                   stream=None) -> None:
+    """mixed_partials() (AMR.h:1268-1278)."""
+    check(load().amr_mixed_partials(ctypes.byref(cfg), _p(field), _p(off), _p(positions), used, substep, max_depth,
+                                    seed, _s(stream)), "amr_mixed_partials")
+
+
+def deriv_trace(cfg: Config, hess_diag, hess_off, metric6, out, positions, used: int, substep: int, max_depth: int,
+                stream=None) -> None:
+    """__deriv_trace launch of scalar_laplacian_noncovariant (BSSN.h:31-35)."""
+    check(load().amr_deriv_trace(ctypes.byref(cfg), _p(hess_diag), _p(hess_off), _ptr_array(metric6), _p(out),
+                                 _p(positions), used, substep, max_depth, _s(stream)), "amr_deriv_trace")
+
+
+def christoffel(cfg: Config, metric6, derivs6, seed: int, out6, positions, used: int, substep: int, max_depth: int,
+                mode: int = 0, stream=None) -> None:
+    """compute_raised_christoffel_symbols() (BSSN.h:93-102)."""
+    check(load().amr_christoffel(ctypes.byref(cfg), _ptr_array(metric6), _ptr_array(derivs6), seed, _ptr_array(out6),
+                                 _p(positions), used, substep, max_depth, mode, _s(stream)), "amr_christoffel")
+
+
+def copy_boundaries(cfg: Config, old, new, boundaries, used: int, substep: int, max_depth: int,
+                    copy_only_new: bool = True, stream=None) -> None:
+    """copy_boundaries() (AMR.h:880-900)."""
+    check(load().amr_copy_boundaries(ctypes.byref(cfg), _p(old), _p(new), _p(boundaries), used, substep, max_depth,
+                                     1 if copy_only_new else 0, _s(stream)), "amr_copy_boundaries")
+
+
+def copy_new_to_old(cfg: Config, old, new, positions, children, used: int, substep: int, max_depth: int,
+                    stream=None) -> None:
+    """copy_new_to_old() (AMR.h:998-1018)."""
+    check(load().amr_copy_new_to_old(ctypes.byref(cfg), _p(old), _p(new), _p(positions), _p(children), used, substep,
+                                     max_depth, _s(stream)), "amr_copy_new_to_old")
+
+
+def copy_to_child(cfg: Config, field, offset: int, child: int, parent: int, stream=None) -> None:
+    """copy_to_child() (AMR.h:1075-1082)."""
+    check(load().amr_copy_to_child(ctypes.byref(cfg), _p(field), offset, child, parent, _s(stream)), "amr_copy_to_child")
+
+
+def wave_step(cfg: Config, corrector: bool, old, derivs, hess, new, positions, used: int, substep: int,
+              max_depth: int, stream=None) -> None:
+    """wave_equation_predictor() / wave_equation_corrector() (SimpleWave.h:48-72)."""
+    fn = load().amr_wave_corrector if corrector else load().amr_wave_predictor
+    check(fn(ctypes.byref(cfg), _p(old), _p(derivs), _p(hess), _p(new), _p(positions), used, substep, max_depth,
+             _s(stream)), "amr_wave_step")
+
+
+def criterion(cfg: Config, derivs, hess, crit, positions, used: int, substep: int, max_depth: int, stream=None) -> None:
+    """The device half of amr_criterion() (SimpleWave.h:142-150)."""
+    check(load().amr_criterion(ctypes.byref(cfg), _p(derivs), _p(hess), _p(crit), _p(positions), used, substep,
+                               max_depth, _s(stream)), "amr_criterion")

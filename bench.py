@@ -1,0 +1,326 @@
+"""Benchmark: BSSN timesteps (reference semantics) on the uniform depth-3 octree, 16^3 domains.
+
+Workload (the BSSN linear-gauge-wave configuration's octree): uniform refinement to depth 3
+= 512 leaf domains + 73 covered parents = 585 slots, size_domain 16, padding 3 (6th-order FD,
+as the reference couples FD order to the padding), root edge 100.  One step = one
+BSSN_AMR_data::timestep(): 8 substeps of copy_back (restriction), predictor (metric gradients,
+Hessians, g^kl d_k d_l g_ij, Christoffel symbols), copy_bounds (ghost fill), corrector.
+Metric: zone-cycles/s = 512 * 16^3 leaf zones x steps / seconds (covered parents are overhead).
+
+  value  device-resident state, graph replay of each timestep (inputs larger than L2: the
+         state is 299 MB, so no L2 flush is needed between steps)
+  e2e    the same metric through the C ABI with host buffers: every step uploads the state
+         (old + new metric) from pinned host memory and downloads new metric, gradients,
+         Christoffel symbols and traces to pinned host memory, inside the timed region
+
+`--impl reference` times the reference path on the CPU: the reference has no CPU solver, so
+this is the oracle's restatement of BSSN_AMR_data::timestep (OpenMP over domains), on a bounded
+sample of the same workload each step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+
+N, P, OUTER, DEPTH = 16, 3, 100.0, 3
+METRIC = "BSSN zone-cycles/s"
+UNIT = "zone-cycles/s"
+WORKLOAD = "BSSN fragment timestep (reference semantics), uniform depth-3 octree: 512 leaf + 73 parent domains of 16^3, padding 3"
+
+
+def build_tree(o):
+    import cases
+    cases.tree_uniform(o, DEPTH)
+
+
+def leaf_zones(st) -> int:
+    used = st["used_slots"]
+    ch = st["children"][: used * 8].reshape(used, 8)
+    leaves = sum(1 for i in range(used) if st["positions"][i] != 0xFFFFFFFF and (ch[i] == -1).all())
+    return leaves * N ** 3
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.samples, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def fused_kernel_bytes_per_domain() -> int:
+    """Algorithmic HBM bytes of the fused BSSN stencil per domain: the six metric components'
+    interior plus face ghosts read once (g = (N^3 + 6 p N^2) / N^3), and 18 inner-layout outputs
+    written (6 compressed gradients, 6 traces, 6 compressed Christoffel symbols)."""
+    return 6 * 4 * (N ** 3 + 6 * P * N ** 2) + 18 * 4 * N ** 3
+
+
+def cpu_sample(seconds_target: float, threads: int | None = None) -> dict:
+    """Time the oracle's BSSN timestep on a bounded sample of the workload's domains."""
+    import numpy as np
+    import adaptivemesh_gb300 as am
+    from oracle import oracle as orc
+    import cases
+
+    o = am.Octree(600)
+    build_tree(o)
+    st = o.state()
+    used = st["used_slots"]
+    xyz = cases.cell_coordinates(st["positions"], used, N, P, OUTER)
+    metric = cases.metric_fields(xyz, OUTER, 500)
+    c = orc.cfg(N, P, OUTER)
+    L = orc.lib()
+    if threads:
+        L.orc_set_num_threads(threads)
+    cores = int(L.orc_num_threads())
+    inner = used * N ** 3
+    old6 = [m.copy() for m in metric]
+    new6 = [m.copy() for m in metric]
+    dm = [np.zeros(inner, np.uint32) for _ in range(6)]
+    ch = [np.zeros(inner, np.uint32) for _ in range(6)]
+    ri = [np.zeros(inner, np.float32) for _ in range(6)]
+    pp = [orc.ptrs(x) for x in (old6, new6, dm, ch, ri)]
+    # leaves are the last 512 slots of the breadth-first tree
+    first_leaf = used - 512
+
+    def run(n_leaf: int) -> float:
+        timer, rng = ctypes.c_uint32(0), ctypes.c_int32(12894712)
+        t0 = time.perf_counter()
+        L.orc_bssn_timestep(ctypes.byref(c), orc.P(pp[0]), orc.P(pp[1]), orc.P(pp[2]), orc.P(pp[3]), orc.P(pp[4]),
+                            orc.P(st["positions"]), orc.P(st["children"]), orc.P(st["boundaries"]), used,
+                            st["max_depth"], ctypes.byref(timer), ctypes.byref(rng), first_leaf, first_leaf + n_leaf)
+        return time.perf_counter() - t0
+
+    t = run(8)
+    n_leaf = int(max(8, min(512, 8 * seconds_target / max(t, 1e-3))))
+    t = run(n_leaf)
+    return {"value": n_leaf * N ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n_leaf} of 512 leaf domains, one full timestep (8 substeps), {t:.2f} s"}
+
+
+def reference_arm(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_sample(0.5)
+    vals = [cpu_sample(args.cpu_seconds) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 512 * N ** 3 / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "global_batch": 512, "seq_len": N ** 3, "parallelism": "replicas"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="graph", choices=["plain", "batched", "graph"])
+    ap.add_argument("--cpu-seconds", type=float, default=4.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import numpy as np
+    import torch
+    import adaptivemesh_gb300 as am
+    import cases
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    mode = {"plain": am.MODE_PLAIN, "batched": am.MODE_BATCHED, "graph": am.MODE_GRAPH}[args.mode]
+    cfg = am.Config(N, P, OUTER)
+    sim = am.Sim(cfg, am.SIM_BSSN, slots=600, mode=mode)
+    build_tree(sim)
+    sim.synchronize()
+    st = sim.state()
+    used, md = st["used_slots"], st["max_depth"]
+    zones = leaf_zones(st)
+    xyz = cases.cell_coordinates(st["positions"], used, N, P, OUTER)
+    metric = cases.metric_fields(xyz, OUTER, 500)
+    T3 = cfg.total ** 3
+    padded, inner = used * T3, used * N ** 3
+    state = [sim.tensor(w, k)[:padded] for w in (am.Sim.OLD, am.Sim.NEW) for k in range(6)]
+    outs = [sim.tensor(am.Sim.NEW, k)[:padded] for k in range(6)] + \
+           [sim.tensor(w, k)[:inner] for w in (am.Sim.DMET, am.Sim.CHR, am.Sim.RICCI) for k in range(6)]
+    for i, t in enumerate(state):
+        t.copy_(torch.from_numpy(metric[i % 6]).cuda())
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(sim.stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        sim.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident timesteps (value)
+    for _ in range(args.warmup):
+        sim.timestep()
+    barrier()
+    launches0 = sim.kernel_launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.timestep()
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    gpu_launches = sim.kernel_launches - launches0
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = zones * args.steps * world / (ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers (e2e)
+    h_in = [torch.empty(padded, dtype=torch.float32, pin_memory=True) for _ in range(12)]
+    for i, t in enumerate(h_in):
+        t.copy_(torch.from_numpy(metric[i % 6]))
+    h_out = [torch.empty(x.numel(), dtype=x.dtype, pin_memory=True) for x in outs]
+    h2d = sum(t.numel() * 4 for t in h_in)
+    d2h = sum(t.numel() * 4 for t in h_out)
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for d, h in zip(state, h_in):
+                d.copy_(h, non_blocking=True)
+        sim.timestep()
+        with torch.cuda.stream(stream):
+            for h, d in zip(h_out, outs):
+                h.copy_(d, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    ms_e2e = e0.elapsed_time(e1)
+    e2e_value = zones * args.steps * world / (ms_e2e / 1e3)
+
+    # ---- dominant kernel (fused BSSN stencil) timed with CUDA events around each launch
+    sim.set_mode(am.MODE_BATCHED)
+    sim.enable_kernel_timing(True)
+    for _ in range(args.warmup):
+        sim.timestep()
+    sim.kernel_timing()   # discard warm-up
+    for _ in range(args.steps):
+        sim.timestep()
+    k_ms, k_n = sim.kernel_timing()
+    sim.enable_kernel_timing(False)
+    # domains processed per timestep by the fused kernel: active domains of each substep, twice
+    depths = [int(p) >> 27 for p in st["positions"][:used]]
+    per_step = sum(2 * sum(1 for d in depths if (s & ((1 << (md - d)) - 1)) == 0) for s in range(1 << md))
+    bytes_per_launch = fused_kernel_bytes_per_domain() * per_step / (2 << md)
+    achieved = bytes_per_launch / (k_ms / k_n / 1e3) / 1e9 if k_n else None
+    pk = peaks()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"] if achieved else None, "traffic": None,
+                "kernel": "k_stencil<16,3,SK_BSSN> (fused BSSN derivatives)", "peak_source": pk["source"],
+                "avg_launch_ms": k_ms / k_n if k_n else None, "launches_timed": k_n}
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            roofline["traffic"] = json.load(f).get("bssn_fused_bytes_per_launch")
+    except Exception:
+        pass
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "global_batch": 512 * world, "seq_len": N ** 3,
+                       "parallelism": "replicas" if world > 1 else "single", "mode": args.mode,
+                       "l2": "state 299 MB > L2 129 MB, no flush"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": ms_e2e / args.steps},
+            "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clocks.summary()}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line))
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

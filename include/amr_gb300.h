@@ -1,0 +1,181 @@
+/* amr_gb300.h -- C ABI of the GB300 (sm_103a) implementation of AdaptiveMesh's per-timestep
+ * hot path.
+ *
+ * Data layout (identical to the reference so its host octree can hand buffers over as is):
+ *   padded field   float    slot * T^3 + (z*T + y)*T + x,  T = size_domain + 2*padding_domain
+ *                           (AdaptiveMesh/AMR.h:1165-1166); one buffer per tensor component.
+ *   inner field    float or compressed_float3 words (uint32)
+ *                           slot * N^3 + (z*N + y)*N + x,  N = size_domain (AMR.h:1177-1178).
+ *   positions      uint32 octree_abs_pos words, one per slot (AMR.h:22-55).
+ *   children       int32, 8 per slot, -1 = none (AMR.h:123).
+ *   boundaries     uint64 domain_boundary words, 6 per slot in face order +x,+y,+z,-x,-y,-z
+ *                           (AMR.h:56-100, AMR.h:276-290).
+ *
+ * Conventions: every entry point returns AMR_OK (0) or an error code; device work is enqueued
+ * on the caller's stream (a cudaStream_t passed as void*, NULL = legacy default stream) with no
+ * implicit device synchronisation.  `used_slots` is the octree's curr_used_slots() (AMR.h:205).
+ * Slots with octree_abs_pos == 0xFFFFFFFF, and slots whose depth is not active at `substep`
+ * (AMR.h:640-644), are skipped, as in the reference.  Not thread-safe per simulation object.
+ */
+#ifndef AMR_GB300_H
+#define AMR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMR_OK 0
+#define AMR_ERR_INVALID 1           /* bad argument (null pointer, size out of range) */
+#define AMR_ERR_UNSUPPORTED 2       /* (size_domain, padding_domain) not compiled in */
+#define AMR_ERR_CUDA 3              /* a CUDA runtime call failed; see amr_last_cuda_error() */
+#define AMR_ERR_NO_DEVICE 4         /* no CUDA device is visible */
+#define AMR_ERR_CAPACITY 5          /* node slots exhausted or a fixed-size buffer is too small */
+
+/* Domain configuration: the reference's compile-time constants (AMR.h:9-20) as run-time values. */
+typedef struct amr_config {
+    uint32_t size_domain;       /* interior cells per edge, N   (AMR.h:11) */
+    uint32_t padding_domain;    /* ghost cells per side, p      (AMR.h:12); FD order = 2p (AMR.h:1171) */
+    float outer_size;           /* edge length of the root      (AMR.h:10) */
+} amr_config;
+
+/* Christoffel modes for amr_christoffel: AMR_CHRISTOFFEL_REFERENCE multiplies the lowered
+ * symbols by the metric as BSSN.h:82 does; AMR_CHRISTOFFEL_RAISED multiplies by its inverse. */
+#define AMR_CHRISTOFFEL_REFERENCE 0
+#define AMR_CHRISTOFFEL_RAISED 1
+
+/* ---------------------------------------------------------------- library */
+const char* amr_version(void);
+/* 1 if (size_domain, padding_domain) has compiled kernels. */
+int amr_config_supported(const amr_config* cfg);
+/* The last CUDA error code seen by this thread (0 if none). */
+int amr_last_cuda_error(void);
+/* Human-readable text for a status code. */
+const char* amr_status_string(int status);
+
+/* ---------------------------------------------------------------- compressed_float3 codec
+ * 3 x (sign + 8-bit mantissa) with a 5-bit shared exponent, bit-exact with the reference's
+ * device build (tensors.h:305-394).  seeds == NULL selects the deterministic encoder
+ * (tensors.h:374-393); otherwise element i uses a fresh fast_prng(seeds[i]) (tensors.h:276-304). */
+int amr_cf3_encode(const float* xyz, const int32_t* seeds, uint64_t n, uint32_t* out, void* stream);
+int amr_cf3_decode(const uint32_t* words, uint64_t n, float* xyz, void* stream);
+
+/* ---------------------------------------------------------------- operator kernels
+ * One entry point per reference operator; the global seed is the value the reference draws
+ * from its host fast_prng for that launch (rng.generate_int(), AMR.h:1277, 1289, 1301). */
+
+/* Gradient (and, if d2if != NULL, the diagonal of the Hessian) by (2p+1)-point centred
+ * differences, scaled by 2^depth / outer_dx.  Replaces differentiate(), AMR.h:1280-1302. */
+int amr_differentiate(const amr_config* cfg, const float* field, uint32_t* dif, uint32_t* d2if,
+                      const uint32_t* positions, uint32_t used_slots, uint32_t substep, uint32_t max_depth,
+                      int32_t seed, void* stream);
+/* Off-diagonal Hessian (xy, xz, yz) with the reference's edge rule.  Replaces mixed_partials(),
+ * AMR.h:1268-1278. */
+int amr_mixed_partials(const amr_config* cfg, const float* field, uint32_t* off_diag,
+                       const uint32_t* positions, uint32_t used_slots, uint32_t substep, uint32_t max_depth,
+                       int32_t seed, void* stream);
+/* g^kl H_kl from a compressed Hessian (diag, off-diag) and the six padded metric components
+ * (xx, xy, xz, yy, yz, zz; a host array of device pointers).  Replaces the third launch of
+ * scalar_laplacian_noncovariant(), BSSN.h:24-36. */
+int amr_deriv_trace(const amr_config* cfg, const uint32_t* hess_diag, const uint32_t* hess_off,
+                    float* const* metric6, float* out, const uint32_t* positions, uint32_t used_slots,
+                    uint32_t substep, uint32_t max_depth, void* stream);
+/* Christoffel symbols from the six compressed metric gradients.  Replaces
+ * compute_raised_christoffel_symbols(), BSSN.h:93-102.  mode: AMR_CHRISTOFFEL_*. */
+int amr_christoffel(const amr_config* cfg, float* const* metric6, uint32_t* const* derivs6, int32_t seed,
+                    uint32_t* const* out6, const uint32_t* positions, uint32_t used_slots, uint32_t substep,
+                    uint32_t max_depth, int mode, void* stream);
+/* Face ghost fill with space (10-point) and time interpolation from the coarser-or-equal
+ * neighbour.  Replaces copy_boundaries(), AMR.h:880-900.  All reads see the fields as they
+ * were before the call (the reference's single launch races where a domain reads a coarser
+ * neighbour's innermost ghost layer); the values are staged in a per-device scratch buffer that
+ * the library allocates on first use and grows when needed. */
+int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,
+                        uint32_t used_slots, uint32_t substep, uint32_t max_depth, int copy_only_new,
+                        void* stream);
+/* old <- new for active domains; cells covered by a child <- mean of the child's 2x2x2 cells.
+ * Replaces copy_new_to_old(), AMR.h:998-1018. */
+int amr_copy_new_to_old(const amr_config* cfg, float* old_f, const float* new_f, const uint32_t* positions,
+                        const int32_t* children, uint32_t used_slots, uint32_t substep, uint32_t max_depth,
+                        void* stream);
+/* Prolongation of a parent's padded domain into a new child (all cells, ghosts included).
+ * Replaces copy_to_child(), AMR.h:1075-1082. */
+int amr_copy_to_child(const amr_config* cfg, float* field, uint32_t offset, int32_t child, int32_t parent,
+                      void* stream);
+/* SimpleWave Heun predictor / corrector.  Replace wave_equation_predictor() and
+ * wave_equation_corrector(), SimpleWave.h:48-72. */
+int amr_wave_predictor(const amr_config* cfg, const float* old_f, const uint32_t* derivs, const uint32_t* hess_diag,
+                       float* new_f, const uint32_t* positions, uint32_t used_slots, uint32_t substep,
+                       uint32_t max_depth, void* stream);
+int amr_wave_corrector(const amr_config* cfg, const float* old_f, const uint32_t* derivs, const uint32_t* hess_diag,
+                       float* new_f, const uint32_t* positions, uint32_t used_slots, uint32_t substep,
+                       uint32_t max_depth, void* stream);
+/* Device half of amr_criterion(): per-octant maxima of |grad u| dx and |diag H| dx^2, written
+ * at the strided positions __amr_criterion_2 leaves them (SimpleWave.h:91-150).  crit holds
+ * used_slots * N * N floats. */
+int amr_criterion(const amr_config* cfg, const uint32_t* derivs, const uint32_t* hess_diag, float* crit,
+                  const uint32_t* positions, uint32_t used_slots, uint32_t substep, uint32_t max_depth,
+                  void* stream);
+
+/* ---------------------------------------------------------------- host octree
+ * The reference's AMR<T> (AMR.h:118-294) without device data: same slot allocation, Morton
+ * positions, boundary descriptors and subcycling counter, bit for bit. */
+typedef struct amr_octree amr_octree;
+int amr_octree_create(uint32_t node_slots, amr_octree** out);
+int amr_octree_destroy(amr_octree* o);
+int amr_octree_add_node(amr_octree* o, int32_t parent, int32_t offset);        /* AMR.h:208-232 */
+int amr_octree_remove_node(amr_octree* o, int32_t node);                       /* AMR.h:233-254 */
+int amr_octree_increment_timer(amr_octree* o);                                 /* AMR.h:180-188 */
+uint32_t amr_octree_find_node_idx(const amr_octree* o, uint32_t packed_pos, uint32_t max_depth); /* AMR.h:255-263 */
+/* scalars: timer_helper, max_depth, first_free_slot, curr_used_slots, max_slots.  Any output
+ * pointer may be NULL; arrays hold node_slots (x8 children, x6 boundaries) entries. */
+int amr_octree_state(const amr_octree* o, uint32_t* positions, int32_t* parent, int32_t* children,
+                     uint64_t* boundaries, uint32_t* lifetime, uint32_t* scalars5);
+
+/* ---------------------------------------------------------------- simulations (plugins)
+ * A simulation owns an octree, the device fields of one reference plugin and its host
+ * fast_prng (default seed 12894712, tensors.h:280), and runs the plugin's timestep loop
+ * (AMR.h:324-333): copy_back, modify_nodes, predictor, copy_bounds, corrector, increment_timer,
+ * until the counter wraps.  Kinds: */
+#define AMR_SIM_BSSN 1      /* BSSN_AMR_data, BSSN.h:104-171 */
+#define AMR_SIM_WAVE 2      /* wave_AMR_data, SimpleWave.h:191-279 */
+/* Execution modes: */
+#define AMR_MODE_PLAIN 0    /* one launch per operator and component, in the reference's order */
+#define AMR_MODE_BATCHED 1  /* fused multi-component kernels over the active-domain list */
+#define AMR_MODE_GRAPH 2    /* AMR_MODE_BATCHED, each timestep replayed from a captured CUDA graph */
+
+typedef struct amr_sim amr_sim;
+int amr_sim_create(const amr_config* cfg, int kind, uint32_t node_slots, int mode, amr_sim** out);
+int amr_sim_destroy(amr_sim* s);
+int amr_sim_set_mode(amr_sim* s, int mode);
+int amr_sim_add_node(amr_sim* s, int32_t parent, int32_t offset);     /* runs node_ctor (prolongation) */
+int amr_sim_remove_node(amr_sim* s, int32_t node);
+int amr_sim_octree_state(const amr_sim* s, uint32_t* positions, int32_t* parent, int32_t* children,
+                         uint64_t* boundaries, uint32_t* lifetime, uint32_t* scalars5);
+/* Device address and element count of a simulation buffer.
+ *   BSSN: which 0 cyij_old, 1 cyij_new (padded float), 2 cRij (inner float),
+ *         3 cyij_k, 4 cGijk (inner compressed_float3); comp 0..5 = xx, xy, xz, yy, yz, zz.
+ *   WAVE: which 0 old_field, 1 new_field (padded float), 3 first_derivs, 4 hessian_diag
+ *         (inner compressed_float3), 5 criterion (used_slots * N * N float); comp 0. */
+int amr_sim_buffer(amr_sim* s, int which, int comp, void** dev_ptr, uint64_t* count);
+int amr_sim_timestep(amr_sim* s);                                      /* the plugin's timestep() */
+int amr_sim_copy_bounds(amr_sim* s);                                   /* the plugin's copy_bounds() */
+int amr_sim_rng(const amr_sim* s, int32_t* seed);
+int amr_sim_set_rng(amr_sim* s, int32_t seed);
+int amr_sim_stream(amr_sim* s, void** stream);
+int amr_sim_synchronize(amr_sim* s);
+/* Kernel launches the library issued for this simulation since creation (graph replays count
+ * the kernels in the graph). */
+uint64_t amr_sim_kernel_launches(const amr_sim* s);
+/* Optional timing of the dominant kernel (the derivative stencil) with CUDA events on the
+ * simulation's stream.  amr_sim_kernel_timing returns the summed milliseconds and launch count
+ * since the last reset. */
+int amr_sim_enable_kernel_timing(amr_sim* s, int enable);
+int amr_sim_kernel_timing(amr_sim* s, double* ms, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AMR_GB300_H */
