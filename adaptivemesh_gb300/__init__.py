@@ -84,6 +84,10 @@ EXPORTS = {
     "amr_sim_remove_node": (ctypes.c_int, [VP, I32]),
     "amr_sim_octree_state": (ctypes.c_int, [VP, VP, VP, VP, VP, VP, VP]),
     "amr_sim_buffer": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(VP), ctypes.POINTER(U64)]),
+    "amr_sim_copy_to_device": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, VP, U64]),
+    "amr_sim_copy_to_host": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, VP, U64]),
+    "amr_sim_event_record": (ctypes.c_int, [VP, ctypes.c_int]),
+    "amr_sim_event_elapsed": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "amr_sim_timestep": (ctypes.c_int, [VP]),
     "amr_sim_copy_bounds": (ctypes.c_int, [VP]),
     "amr_sim_rng": (ctypes.c_int, [VP, ctypes.POINTER(I32)]),

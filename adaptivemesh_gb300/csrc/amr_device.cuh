@@ -51,10 +51,10 @@ __device__ __forceinline__ uint32_t cf3_encode_impl(float x, float y, float z, i
     x = __fmul_rn(x, scale);
     y = __fmul_rn(y, scale);
     z = __fmul_rn(z, scale);
-    if (STOCHASTIC) {
-        x = __fmaf_rn(prng_float(rng), .95f, x);
-        y = __fmaf_rn(prng_float(rng), .95f, y);
-        z = __fmaf_rn(prng_float(rng), .95f, z);
+    if (STOCHASTIC) {   // the noise product is rounded before it is added (not fused)
+        x = __fadd_rn(x, __fmul_rn(prng_float(rng), .95f));
+        y = __fadd_rn(y, __fmul_rn(prng_float(rng), .95f));
+        z = __fadd_rn(z, __fmul_rn(prng_float(rng), .95f));
     }
     return (E << 27) | cf3_quantise_one(x, 0u, 8u) | cf3_quantise_one(y, 9u, 17u) | cf3_quantise_one(z, 18u, 26u);
 }

@@ -144,14 +144,15 @@ __global__ void k_criterion_columns(Dims d, float outer_dx, const uint32_t* __re
     const int depth = pos_depth(positions[zi / 2]);
     if (depth == -1 || !active_depth(substep, (uint32_t)depth, max_depth)) { crit[o] = __int_as_float(0x7fc00000); return; }   // NAN, SimpleWave.h:97
     uint64_t ro = x + ((uint64_t)y + ((y >= q) ? q : 0u) + (uint64_t)zi * n * h) * n;
-    const float s1 = __fmul_rn(outer_dx, __uint_as_float((127u - (uint32_t)depth) << 23));
-    const float s2 = __fmul_rn(__fmul_rn(outer_dx, outer_dx), __uint_as_float((127u - 2u * (uint32_t)depth) << 23));
+    // |g| * dx / 2^depth and |H| * dx * dx / 4^depth, left to right (the power-of-two scaling is exact)
+    const float s1 = __uint_as_float((127u - (uint32_t)depth) << 23);
+    const float s2 = __uint_as_float((127u - 2u * (uint32_t)depth) << 23);
     float cr = 0.f;
     for (uint32_t i = 0; i < h; i++) {
-        cr = fmaxf(cr, __fmul_rn(cf3_length(der[ro]), s1));
-        cr = fmaxf(cr, __fmul_rn(cf3_length(hess[ro]), s2));
-        cr = fmaxf(cr, __fmul_rn(cf3_length(der[ro + (uint64_t)q * n]), s1));
-        cr = fmaxf(cr, __fmul_rn(cf3_length(hess[ro + (uint64_t)q * n]), s2));
+        cr = fmaxf(cr, __fmul_rn(__fmul_rn(cf3_length(der[ro]), outer_dx), s1));
+        cr = fmaxf(cr, __fmul_rn(__fmul_rn(__fmul_rn(cf3_length(hess[ro]), outer_dx), outer_dx), s2));
+        cr = fmaxf(cr, __fmul_rn(__fmul_rn(cf3_length(der[ro + (uint64_t)q * n]), outer_dx), s1));
+        cr = fmaxf(cr, __fmul_rn(__fmul_rn(__fmul_rn(cf3_length(hess[ro + (uint64_t)q * n]), outer_dx), outer_dx), s2));
         ro += (uint64_t)n * n;
     }
     crit[o] = cr;

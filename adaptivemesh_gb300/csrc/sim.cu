@@ -49,6 +49,7 @@ public:
         cudaFree(d_positions); cudaFree(d_children); cudaFree(d_boundaries); cudaFree(d_items);
         cudaFree(ghost_stage);
         for (auto& ev : events) cudaEventDestroy(ev);
+        for (auto& ev : user_events) if (ev) cudaEventDestroy(ev);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -205,6 +206,7 @@ public:
     bool timing = false;
     std::vector<cudaEvent_t> events;
     size_t ev_used = 0;
+    cudaEvent_t user_events[16] = {};
     double timed_ms = 0.0;
     uint64_t timed_launches = 0;
 };
@@ -649,6 +651,40 @@ AMR_API int amr_sim_octree_state(const amr_sim* s, uint32_t* positions, int32_t*
 AMR_API int amr_sim_buffer(amr_sim* s, int which, int comp, void** ptr, uint64_t* count) {
     if (!s || !ptr || !count) return AMR_ERR_INVALID;
     return s->impl->buffer(which, comp, ptr, count);
+}
+static int sim_copy(amr_sim* s, int which, int comp, void* host, uint64_t count, bool to_device) {
+    if (!s || !host) return AMR_ERR_INVALID;
+    void* dev = nullptr;
+    uint64_t n = 0;
+    const int st = s->impl->buffer(which, comp, &dev, &n);
+    if (st) return st;
+    if (count > n) return AMR_ERR_INVALID;
+    if (count == 0) return AMR_OK;
+    return cuda_status(to_device ? cudaMemcpyAsync(dev, host, count * 4u, cudaMemcpyHostToDevice, s->impl->stream)
+                                 : cudaMemcpyAsync(host, dev, count * 4u, cudaMemcpyDeviceToHost, s->impl->stream));
+}
+AMR_API int amr_sim_copy_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count) {
+    return sim_copy(s, which, comp, const_cast<void*>(host), count, true);
+}
+AMR_API int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, uint64_t count) {
+    return sim_copy(s, which, comp, host, count, false);
+}
+AMR_API int amr_sim_event_record(amr_sim* s, int slot) {
+    if (!s || slot < 0 || slot >= 16) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    if (!b->user_events[slot]) {
+        const int st = cuda_status(cudaEventCreate(&b->user_events[slot]));
+        if (st) return st;
+    }
+    return cuda_status(cudaEventRecord(b->user_events[slot], b->stream));
+}
+AMR_API int amr_sim_event_elapsed(amr_sim* s, int first, int second, float* ms) {
+    if (!s || !ms || first < 0 || first >= 16 || second < 0 || second >= 16) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    if (!b->user_events[first] || !b->user_events[second]) return AMR_ERR_INVALID;
+    const int st = cuda_status(cudaEventSynchronize(b->user_events[second]));
+    if (st) return st;
+    return cuda_status(cudaEventElapsedTime(ms, b->user_events[first], b->user_events[second]));
 }
 AMR_API int amr_sim_timestep(amr_sim* s) { return s ? s->impl->timestep() : AMR_ERR_INVALID; }
 AMR_API int amr_sim_copy_bounds(amr_sim* s) { return s ? s->impl->copy_bounds() : AMR_ERR_INVALID; }

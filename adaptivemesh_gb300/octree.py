@@ -103,6 +103,26 @@ class Sim:
             __cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (addr, False), "version": 3}
         return torch.as_tensor(_Mem(), device="cuda")
 
+    def copy_to_device(self, which: int, comp: int, host, count: int | None = None) -> None:
+        """Asynchronous host -> buffer copy on the simulation's stream (host: pinned tensor/array)."""
+        n = host.numel() if count is None and hasattr(host, "numel") else (count if count is not None else host.size)
+        addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
+        check(load().amr_sim_copy_to_device(self.h, which, comp, addr, n), "amr_sim_copy_to_device")
+
+    def copy_to_host(self, which: int, comp: int, host, count: int | None = None) -> None:
+        """Asynchronous buffer -> host copy on the simulation's stream."""
+        n = host.numel() if count is None and hasattr(host, "numel") else (count if count is not None else host.size)
+        addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
+        check(load().amr_sim_copy_to_host(self.h, which, comp, addr, n), "amr_sim_copy_to_host")
+
+    def event_record(self, slot: int) -> None:
+        check(load().amr_sim_event_record(self.h, slot), "amr_sim_event_record")
+
+    def event_elapsed(self, first: int, second: int) -> float:
+        ms = ctypes.c_float()
+        check(load().amr_sim_event_elapsed(self.h, first, second, ctypes.byref(ms)), "amr_sim_event_elapsed")
+        return float(ms.value)
+
     def timestep(self) -> None:
         check(load().amr_sim_timestep(self.h), "amr_sim_timestep")
 

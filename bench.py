@@ -39,9 +39,13 @@ UNIT = "zone-cycles/s"
 WORKLOAD = "BSSN fragment timestep (reference semantics), uniform depth-3 octree: 512 leaf + 73 parent domains of 16^3, padding 3"
 
 
-def build_tree(o):
+def progress(msg: str) -> None:
+    print(f"[bench] {msg}", file=sys.stderr, flush=True)
+
+
+def build_tree(o, depth: int = DEPTH):
     import cases
-    cases.tree_uniform(o, DEPTH)
+    cases.tree_uniform(o, depth)
 
 
 def leaf_zones(st) -> int:
@@ -113,56 +117,70 @@ def fused_kernel_bytes_per_domain() -> int:
     return 6 * 4 * (N ** 3 + 6 * P * N ** 2) + 18 * 4 * N ** 3
 
 
-def cpu_sample(seconds_target: float, threads: int | None = None) -> dict:
-    """Time the oracle's BSSN timestep on a bounded sample of the workload's domains."""
-    import numpy as np
-    import adaptivemesh_gb300 as am
-    from oracle import oracle as orc
-    import cases
+class CpuPort:
+    """The oracle's restatement of BSSN_AMR_data::timestep on the host cores (OpenMP over
+    domains), run on a bounded sample of the workload's leaf domains."""
 
-    o = am.Octree(600)
-    build_tree(o)
-    st = o.state()
-    used = st["used_slots"]
-    xyz = cases.cell_coordinates(st["positions"], used, N, P, OUTER)
-    metric = cases.metric_fields(xyz, OUTER, 500)
-    c = orc.cfg(N, P, OUTER)
-    L = orc.lib()
-    if threads:
-        L.orc_set_num_threads(threads)
-    cores = int(L.orc_num_threads())
-    inner = used * N ** 3
-    old6 = [m.copy() for m in metric]
-    new6 = [m.copy() for m in metric]
-    dm = [np.zeros(inner, np.uint32) for _ in range(6)]
-    ch = [np.zeros(inner, np.uint32) for _ in range(6)]
-    ri = [np.zeros(inner, np.float32) for _ in range(6)]
-    pp = [orc.ptrs(x) for x in (old6, new6, dm, ch, ri)]
-    # leaves are the last 512 slots of the breadth-first tree
-    first_leaf = used - 512
+    def __init__(self, threads: int | None = None):
+        import numpy as np
+        import adaptivemesh_gb300 as am
+        from oracle import oracle as orc
+        import cases
 
-    def run(n_leaf: int) -> float:
+        o = am.Octree(600)
+        build_tree(o)
+        self.st = st = o.state()
+        self.used = used = st["used_slots"]
+        xyz = cases.cell_coordinates(st["positions"], used, N, P, OUTER)
+        metric = cases.metric_fields(xyz, OUTER, 500)
+        self.orc, self.c, self.L = orc, orc.cfg(N, P, OUTER), orc.lib()
+        if threads:
+            self.L.orc_set_num_threads(threads)
+        self.cores = int(self.L.orc_num_threads())
+        inner = used * N ** 3
+        self.arrays = ([m.copy() for m in metric], [m.copy() for m in metric],
+                       [np.zeros(inner, np.uint32) for _ in range(6)], [np.zeros(inner, np.uint32) for _ in range(6)],
+                       [np.zeros(inner, np.float32) for _ in range(6)])
+        self.pp = [orc.ptrs(x) for x in self.arrays]
+        self.first_leaf = used - 512          # leaves are the last 512 slots of the breadth-first tree
+        self.n_leaf = 8
+
+    def run(self, n_leaf: int) -> float:
+        st, orc, pp = self.st, self.orc, self.pp
         timer, rng = ctypes.c_uint32(0), ctypes.c_int32(12894712)
         t0 = time.perf_counter()
-        L.orc_bssn_timestep(ctypes.byref(c), orc.P(pp[0]), orc.P(pp[1]), orc.P(pp[2]), orc.P(pp[3]), orc.P(pp[4]),
-                            orc.P(st["positions"]), orc.P(st["children"]), orc.P(st["boundaries"]), used,
-                            st["max_depth"], ctypes.byref(timer), ctypes.byref(rng), first_leaf, first_leaf + n_leaf)
+        self.L.orc_bssn_timestep(ctypes.byref(self.c), pp[0], pp[1], pp[2], pp[3], pp[4],
+                                 orc.P(st["positions"]), orc.P(st["children"]), orc.P(st["boundaries"]), self.used,
+                                 st["max_depth"], ctypes.byref(timer), ctypes.byref(rng), self.first_leaf,
+                                 self.first_leaf + n_leaf)
         return time.perf_counter() - t0
 
-    t = run(8)
-    n_leaf = int(max(8, min(512, 8 * seconds_target / max(t, 1e-3))))
-    t = run(n_leaf)
-    return {"value": n_leaf * N ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n_leaf} of 512 leaf domains, one full timestep (8 substeps), {t:.2f} s"}
+    def calibrate(self, seconds: float) -> None:
+        t = self.run(8)
+        self.n_leaf = int(max(8, min(512, 8 * seconds / max(t, 1e-3))))
+
+    def sample(self) -> dict:
+        t = self.run(self.n_leaf)
+        return {"value": self.n_leaf * N ** 3 / t, "unit": UNIT, "cores": self.cores, "kind": "port",
+                "sample": f"{self.n_leaf} of 512 leaf domains, one full timestep (8 substeps), {t:.2f} s"}
+
+
+def cpu_sample(seconds_target: float, threads: int | None = None) -> dict:
+    port = CpuPort(threads)
+    port.calibrate(seconds_target)
+    return port.sample()
 
 
 def reference_arm(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    port = CpuPort()
+    # each step is a bounded sample, sized so that the whole run stays within a few minutes
+    port.calibrate(max(0.2, min(args.cpu_seconds, 150.0 / (args.steps + args.warmup))))
     for _ in range(args.warmup):
-        cpu_sample(0.5)
-    vals = [cpu_sample(args.cpu_seconds) for _ in range(args.steps)]
+        port.sample()
+    vals = [port.sample() for _ in range(args.steps)]
     v = statistics.median(x["value"] for x in vals)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 512 * N ** 3 / v * 1e3, "higher_is_better": True,
@@ -178,12 +196,13 @@ def reference_arm(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="graph", choices=["plain", "batched", "graph"])
     ap.add_argument("--cpu-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--depth", type=int, default=DEPTH, help="uniform octree depth (3 = the benchmark workload)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
@@ -205,8 +224,8 @@ def main() -> None:
 
     mode = {"plain": am.MODE_PLAIN, "batched": am.MODE_BATCHED, "graph": am.MODE_GRAPH}[args.mode]
     cfg = am.Config(N, P, OUTER)
-    sim = am.Sim(cfg, am.SIM_BSSN, slots=600, mode=mode)
-    build_tree(sim)
+    sim = am.Sim(cfg, am.SIM_BSSN, slots=sum(8 ** d for d in range(args.depth + 1)), mode=mode)
+    build_tree(sim, args.depth)
     sim.synchronize()
     st = sim.state()
     used, md = st["used_slots"], st["max_depth"]
@@ -215,33 +234,45 @@ def main() -> None:
     metric = cases.metric_fields(xyz, OUTER, 500)
     T3 = cfg.total ** 3
     padded, inner = used * T3, used * N ** 3
-    state = [sim.tensor(w, k)[:padded] for w in (am.Sim.OLD, am.Sim.NEW) for k in range(6)]
-    outs = [sim.tensor(am.Sim.NEW, k)[:padded] for k in range(6)] + \
-           [sim.tensor(w, k)[:inner] for w in (am.Sim.DMET, am.Sim.CHR, am.Sim.RICCI) for k in range(6)]
-    for i, t in enumerate(state):
-        t.copy_(torch.from_numpy(metric[i % 6]).cuda())
-    torch.cuda.synchronize()
-    stream = torch.cuda.ExternalStream(sim.stream)
+    # host buffers (page-locked) of the state and of the step's outputs; every copy goes through
+    # the C ABI on the simulation's stream
+    ins = [(w, k) for w in (am.Sim.OLD, am.Sim.NEW) for k in range(6)]
+    outs = [(am.Sim.NEW, k, padded) for k in range(6)] + \
+           [(w, k, inner) for w in (am.Sim.DMET, am.Sim.CHR, am.Sim.RICCI) for k in range(6)]
+    h_in = [torch.from_numpy(metric[k]).pin_memory() for _, k in ins]
+    h_out = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _, _, n in outs]
+    h2d = sum(t.numel() * 4 for t in h_in)
+    d2h = sum(t.numel() * 4 for t in h_out)
+
+    def upload():
+        for (w, k), h in zip(ins, h_in):
+            sim.copy_to_device(w, k, h)
+
+    def download():
+        for (w, k, n), h in zip(outs, h_out):
+            sim.copy_to_host(w, k, h)
+
+    upload()
+    sim.synchronize()
 
     def barrier():
-        torch.cuda.synchronize()
         sim.synchronize()
         if dist is not None:
             dist.barrier()
 
-    # ---- device-resident timesteps (value)
-    for _ in range(args.warmup):
-        sim.timestep()
-    barrier()
-    launches0 = sim.kernel_launches
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    progress("value: device-resident timesteps")
+    # ---- device-resident timesteps (value); clocks are sampled from the warm-up on
     with ClockSampler(local) as clocks:
-        ev0.record(stream)
+        for _ in range(args.warmup):
+            sim.timestep()
+        barrier()
+        launches0 = sim.kernel_launches
+        sim.event_record(0)
         for _ in range(args.steps):
             sim.timestep()
-        ev1.record(stream)
+        sim.event_record(1)
         barrier()
-    ms = ev0.elapsed_time(ev1)
+    ms = sim.event_elapsed(0, 1)
     gpu_launches = sim.kernel_launches - launches0
     if dist is not None:
         t = torch.tensor([ms], device="cuda")
@@ -249,35 +280,26 @@ def main() -> None:
         ms = float(t.item())
     value = zones * args.steps * world / (ms / 1e3)
 
+    progress("e2e")
     # ---- end to end through the C ABI with host buffers (e2e)
-    h_in = [torch.empty(padded, dtype=torch.float32, pin_memory=True) for _ in range(12)]
-    for i, t in enumerate(h_in):
-        t.copy_(torch.from_numpy(metric[i % 6]))
-    h_out = [torch.empty(x.numel(), dtype=x.dtype, pin_memory=True) for x in outs]
-    h2d = sum(t.numel() * 4 for t in h_in)
-    d2h = sum(t.numel() * 4 for t in h_out)
 
     def e2e_step():
-        with torch.cuda.stream(stream):
-            for d, h in zip(state, h_in):
-                d.copy_(h, non_blocking=True)
+        upload()
         sim.timestep()
-        with torch.cuda.stream(stream):
-            for h, d in zip(h_out, outs):
-                h.copy_(d, non_blocking=True)
+        download()
 
     for _ in range(args.warmup):
         e2e_step()
     barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    sim.event_record(2)
     for _ in range(args.steps):
         e2e_step()
-    e1.record(stream)
+    sim.event_record(3)
     barrier()
-    ms_e2e = e0.elapsed_time(e1)
+    ms_e2e = sim.event_elapsed(2, 3)
     e2e_value = zones * args.steps * world / (ms_e2e / 1e3)
 
+    progress("kernel timing")
     # ---- dominant kernel (fused BSSN stencil) timed with CUDA events around each launch
     sim.set_mode(am.MODE_BATCHED)
     sim.enable_kernel_timing(True)
@@ -314,9 +336,16 @@ def main() -> None:
                     "ms_per_step": ms_e2e / args.steps},
             "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clocks.summary()}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        progress("cpu baseline")
         line["cpu_baseline"] = cpu_sample(args.cpu_seconds)
     if rank == 0:
-        print(json.dumps(line))
+        print(json.dumps(line), flush=True)
+    # release every torch object that refers to the simulation's memory or stream first
+    torch.cuda.synchronize()
+    del h_in, h_out
+    import gc
+    gc.collect()
+    torch.cuda.synchronize()
     sim.close()
     if dist is not None:
         dist.destroy_process_group()

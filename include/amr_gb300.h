@@ -160,6 +160,15 @@ int amr_sim_octree_state(const amr_sim* s, uint32_t* positions, int32_t* parent,
  *   WAVE: which 0 old_field, 1 new_field (padded float), 3 first_derivs, 4 hessian_diag
  *         (inner compressed_float3), 5 criterion (used_slots * N * N float); comp 0. */
 int amr_sim_buffer(amr_sim* s, int which, int comp, void** dev_ptr, uint64_t* count);
+/* Asynchronous copies between host memory (page-locked for overlap) and a simulation buffer on
+ * the simulation's stream, the counterparts of smart_gpu_cpu_buffer::copy_to_gpu / copy_to_cpu
+ * (CUDA_memory.h:177-184).  `count` elements (4 bytes each) from the start of the buffer. */
+int amr_sim_copy_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count);
+int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, uint64_t count);
+/* Timing events on the simulation's stream: record event `slot` (0..15), and read the
+ * milliseconds between two recorded events (waits for the later one). */
+int amr_sim_event_record(amr_sim* s, int slot);
+int amr_sim_event_elapsed(amr_sim* s, int first, int second, float* ms);
 int amr_sim_timestep(amr_sim* s);                                      /* the plugin's timestep() */
 int amr_sim_copy_bounds(amr_sim* s);                                   /* the plugin's copy_bounds() */
 int amr_sim_rng(const amr_sim* s, int32_t* seed);

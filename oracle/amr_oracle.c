@@ -140,9 +140,10 @@ float orc_trace_contra_sym(const float* c, const float* m) {           /* tensor
     return fmaf(b, 2.f, a);
 }
 void orc_sym_times_vec(const float* m, const float* a, float* o) {     /* tensors.h:201-206 */
-    o[0] = fmaf(a[2], m[2], fmaf(a[1], m[1], a[0] * m[0]));
-    o[1] = fmaf(a[2], m[4], fmaf(a[1], m[3], a[0] * m[1]));
-    o[2] = fmaf(a[2], m[5], fmaf(a[1], m[4], a[0] * m[2]));
+    /* a.x*m0 + a.y*m1 fuses the left product; the third product is fused into that sum */
+    o[0] = fmaf(a[2], m[2], fmaf(a[0], m[0], a[1] * m[1]));
+    o[1] = fmaf(a[2], m[4], fmaf(a[0], m[1], a[1] * m[3]));
+    o[2] = fmaf(a[2], m[5], fmaf(a[0], m[2], a[1] * m[4]));
 }
 
 /* ------------------------------------------------------------------ octree helpers, AMR.h:22-116 */
@@ -578,16 +579,18 @@ void orc_criterion(const orc_cfg* c, const uint32_t* derivs, const uint32_t* hes
                 const uint64_t o = x + ((uint64_t)y + (uint64_t)zi * h) * n;
                 if (depth == -1 || !active_depth(substep, (uint32_t)depth, max_depth)) { crit[o] = NAN; continue; }
                 uint64_t ro = x + ((uint64_t)y + ((y >= q) ? q : 0u) + (uint64_t)zi * n * h) * n;
-                const float s1 = c->outer_dx / (float)(1u << depth);
-                const float s2 = (c->outer_dx * c->outer_dx) / (float)(1u << (depth * 2u));
                 float cr = 0.f;
                 for (uint32_t i = 0; i < h; i++) {
                     const uint32_t w[4] = {derivs[ro], hess[ro], derivs[ro + q * n], hess[ro + q * n]};
                     for (int k = 0; k < 4; k++) {
                         float v[3];
                         orc_cf3_decode(w[k], v);
+                        /* the device build takes sqrt with the hardware approximation; this one is exact */
                         const float len = sqrtf(fmaf(v[2], v[2], fmaf(v[0], v[0], v[1] * v[1])));
-                        cr = fmaxf(cr, len * ((k & 1) ? s2 : s1));
+                        /* |g| * dx / 2^depth and |H| * dx * dx / 4^depth, left to right (SimpleWave.h:108-115) */
+                        const float s = (k & 1) ? (len * c->outer_dx) * c->outer_dx / (float)(1u << (depth * 2u))
+                                                : len * c->outer_dx / (float)(1u << depth);
+                        cr = fmaxf(cr, s);
                     }
                     ro += (uint64_t)n * n;
                 }

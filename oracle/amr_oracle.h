@@ -32,8 +32,10 @@ typedef struct {
     uint32_t flags;      /* ORC_* below */
 } orc_cfg;
 
-/* ORC_FUSED_NOISE: the stochastic codec adds its noise with one fused multiply-add
- *                  (device build) instead of a rounded product then a sum (x86 host build).
+/* ORC_FUSED_NOISE: the stochastic codec adds its noise with one fused multiply-add instead of
+ *                  a rounded product then a sum.  Both builds of the reference round the
+ *                  product (pinned on the device by tests/golden/codec_fused_probe_inputs.npz);
+ *                  the flag exists to show that the distinction is observable.
  * ORC_FTZ:         flush subnormal inputs/results of the codec to zero (device build). */
 #define ORC_FUSED_NOISE 1u
 #define ORC_FTZ 2u

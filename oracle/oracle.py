@@ -17,7 +17,8 @@ SRC = [os.path.join(HERE, "amr_oracle.c"), os.path.join(HERE, "amr_oracle.h")]
 
 FUSED_NOISE = 1
 FTZ = 2
-DEVICE_FLAGS = FUSED_NOISE | FTZ   # the reference's device build (fast-math)
+DEVICE_FLAGS = FTZ                 # the reference's device build (fast-math: flush-to-zero; its
+                                   # noise product is rounded before the add, see test_codec_noise_rounding)
 HOST_FLAGS = 0                     # the reference's host build (no contraction, no flush)
 
 VP = ctypes.c_void_p
@@ -92,12 +93,18 @@ def lib():
     return _lib
 
 
-def P(a) -> int:
+def P(a):
+    """Argument for a pointer parameter: a numpy array's address (the caller keeps the array
+    alive), or a ctypes pointer table from ptrs() passed through as is."""
+    if isinstance(a, ctypes.Array):
+        return a
     return a.ctypes.data
 
 
-def ptrs(arrs) -> np.ndarray:
-    return np.array([a.ctypes.data for a in arrs], dtype=np.uint64)
+def ptrs(arrs) -> ctypes.Array:
+    """A C table of the arrays' addresses.  Pass the returned object itself to the call so it
+    stays alive until the call returns."""
+    return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
 
 
 def cfg(n: int, p: int, outer_size: float = 100.0, flags: int = DEVICE_FLAGS, inv_dx=None) -> Cfg:

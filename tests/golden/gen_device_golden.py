@@ -37,8 +37,10 @@ def host(t: torch.Tensor) -> np.ndarray:
     return t.detach().cpu().numpy()
 
 
-def ptr_array(ts) -> np.ndarray:
-    return np.array([t.data_ptr() for t in ts], dtype=np.uint64)
+def ptr_array(ts):
+    """A C table of device addresses; pass the object itself so it outlives the call."""
+    import ctypes
+    return (ctypes.c_void_p * len(ts))(*[t.data_ptr() for t in ts])
 
 
 def substeps_for(max_depth: int) -> list[int]:
@@ -132,13 +134,13 @@ def kernel_case(lib, cfgname: str, tree: str, out: dict, full: dict, keep_full: 
         mets = [dev(m) for m in metric]
         mp = ptr_array(mets)
         lap = z_in()
-        assert lib.refd_deriv_trace(d2.data_ptr(), off.data_ptr(), mp.ctypes.data, lap.data_ptr(), pos_d.data_ptr(), used, s, md) == 0
+        assert lib.refd_deriv_trace(d2.data_ptr(), off.data_ptr(), mp, lap.data_ptr(), pos_d.data_ptr(), used, s, md) == 0
         # metric derivatives + Christoffel symbols
         mder = [z_cf3() for _ in range(6)]
         for k in range(6):
             assert lib.refd_differentiate(mets[k].data_ptr(), mder[k].data_ptr(), None, pos_d.data_ptr(), used, s, md, seed + 10 + k) == 0
         chr_ = [z_cf3() for _ in range(6)]
-        assert lib.refd_christoffel(mp.ctypes.data, ptr_array(mder).ctypes.data, seed + 20, ptr_array(chr_).ctypes.data,
+        assert lib.refd_christoffel(mp, ptr_array(mder), seed + 20, ptr_array(chr_),
                                     pos_d.data_ptr(), used, s, md) == 0
         # ghost fill: both modes
         go, gn = dev(f_old), dev(f_new)
