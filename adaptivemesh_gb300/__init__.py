@@ -65,6 +65,7 @@ EXPORTS = {
     "amr_deriv_trace": (ctypes.c_int, [CP, VP, VP, VP, VP, VP, U32, U32, U32, VP]),
     "amr_christoffel": (ctypes.c_int, [CP, VP, VP, I32, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
     "amr_copy_boundaries": (ctypes.c_int, [CP, VP, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
+    "amr_copy_boundaries_noalloc": (ctypes.c_int, [CP, VP, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
     "amr_copy_new_to_old": (ctypes.c_int, [CP, VP, VP, VP, VP, U32, U32, U32, VP]),
     "amr_copy_to_child": (ctypes.c_int, [CP, VP, U32, I32, I32, VP]),
     "amr_wave_predictor": (ctypes.c_int, [CP, VP, VP, VP, VP, VP, U32, U32, U32, VP]),

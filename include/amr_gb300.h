@@ -95,6 +95,18 @@ int amr_christoffel(const amr_config* cfg, float* const* metric6, uint32_t* cons
 int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,
                         uint32_t used_slots, uint32_t substep, uint32_t max_depth, int copy_only_new,
                         void* stream);
+/* The same ghost fill as amr_copy_boundaries, for callers that cannot let the library allocate
+ * device memory (an application that owns a fixed device-memory budget, or a time-critical loop
+ * that must not block on cudaMalloc).  It has no counterpart in the reference.  Instead of an
+ * allocated staging buffer it uses a fixed 8 MiB array compiled into the library (held by every
+ * GPU that loads it, until exit), so it calls no allocator.  Limit: 2 * 6 * padding_domain *
+ * size_domain^2 floats per slot must fit in 2^21 floats (227 slots at 16/3, 111 at 28/2, 56 at
+ * 32/3); larger cases return AMR_ERR_CAPACITY.  The first call on a device looks up the array's
+ * address; make that first call before any stream capture.  All calls share the array, so calls
+ * that overlap on the GPU race and must be ordered by the caller; nothing in it needs clearing. */
+int amr_copy_boundaries_noalloc(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,
+                                uint32_t used_slots, uint32_t substep, uint32_t max_depth, int copy_only_new,
+                                void* stream);
 /* old <- new for active domains; cells covered by a child <- mean of the child's 2x2x2 cells.
  * Replaces copy_new_to_old(), AMR.h:998-1018. */
 int amr_copy_new_to_old(const amr_config* cfg, float* old_f, const float* new_f, const uint32_t* positions,
