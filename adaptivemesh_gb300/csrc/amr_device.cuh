@@ -37,12 +37,21 @@ __device__ __forceinline__ int32_t cell_rng(int32_t seed, uint32_t x, uint32_t y
 
 // ------------------------------------------------------------------ compressed_float3 (tensors.h:305-394)
 // word = E<<27 | s3<<26 | m3<<18 | s2<<17 | m2<<9 | s1<<8 | m1 ;  value_i = (1 - 2 s_i) m_i 2^(E-22)
-__device__ __forceinline__ uint32_t cf3_quantise_one(float v, uint32_t mpos, uint32_t spos) {
-    const float c = fmaxf(-255.f, fminf(v, 255.f));
-    return (__float2uint_rz(__fadd_rn(fabsf(c), .5f)) << mpos) | ((uint32_t)(c < 0.f) << spos);
+// Mantissa of one component: trunc(|clamp(v, -255, 255)| + 0.5) (tensors.h:369-372).  For every
+// value the encoder produces -- NaN and +-Inf included -- this equals min(trunc(|v| + 0.5), 255):
+// adding 2^23 with round-toward-zero leaves trunc(q) in the low mantissa bits of q + 2^23, an
+// integer min against the bits of 2^23 + 255 saturates (NaN and Inf bits compare above it), and
+// the sign is (v < 0) as for the clamped value.  Returns the raw sum bits (2^23 + m as a float).
+__device__ __forceinline__ uint32_t cf3_mantissa_bits(float v) {
+    const float q = __fadd_rn(fabsf(v), .5f);
+    return min(__float_as_uint(__fadd_rz(q, 8388608.f)), 0x4B0000FFu);
 }
-template <bool STOCHASTIC>
-__device__ __forceinline__ uint32_t cf3_encode_impl(float x, float y, float z, int32_t& rng) {
+struct Cf3Quantised {
+    uint32_t word;
+    float3 value;   // the decoded value of `word`
+};
+template <bool STOCHASTIC, bool WANT_VALUE>
+__device__ __forceinline__ Cf3Quantised cf3_encode_impl(float x, float y, float z, int32_t& rng) {
     const uint32_t ex = (__float_as_uint(x) >> 23) & 255u;
     const uint32_t ey = (__float_as_uint(y) >> 23) & 255u;
     const uint32_t ez = (__float_as_uint(z) >> 23) & 255u;
@@ -56,14 +65,28 @@ __device__ __forceinline__ uint32_t cf3_encode_impl(float x, float y, float z, i
         y = __fadd_rn(y, __fmul_rn(prng_float(rng), .95f));
         z = __fadd_rn(z, __fmul_rn(prng_float(rng), .95f));
     }
-    return (E << 27) | cf3_quantise_one(x, 0u, 8u) | cf3_quantise_one(y, 9u, 17u) | cf3_quantise_one(z, 18u, 26u);
+    const uint32_t bx = cf3_mantissa_bits(x), by = cf3_mantissa_bits(y), bz = cf3_mantissa_bits(z);
+    const uint32_t sx = x < 0.f, sy = y < 0.f, sz = z < 0.f;
+    Cf3Quantised r;
+    r.word = (E << 27) | (bx & 255u) | (sx << 8) | ((by & 255u) << 9) | (sy << 17) | ((bz & 255u) << 18) | (sz << 26);
+    if (WANT_VALUE) {   // (2^23 + m) - 2^23 = m exactly; times 2^(E-22); sign applied last
+        const float back = __uint_as_float((105u + E) << 23);
+        r.value = make_float3(__uint_as_float(__float_as_uint(__fmul_rn(__fsub_rn(__uint_as_float(bx), 8388608.f), back)) | (sx << 31)),
+                              __uint_as_float(__float_as_uint(__fmul_rn(__fsub_rn(__uint_as_float(by), 8388608.f), back)) | (sy << 31)),
+                              __uint_as_float(__float_as_uint(__fmul_rn(__fsub_rn(__uint_as_float(bz), 8388608.f), back)) | (sz << 31)));
+    }
+    return r;
 }
 __device__ __forceinline__ uint32_t cf3_encode(float x, float y, float z, int32_t& rng) {
-    return cf3_encode_impl<true>(x, y, z, rng);
+    return cf3_encode_impl<true, false>(x, y, z, rng).word;
+}
+// Encode and also return the decoded (quantised) value, as a consumer reading the word back sees it.
+__device__ __forceinline__ Cf3Quantised cf3_encode_quantised(float x, float y, float z, int32_t& rng) {
+    return cf3_encode_impl<true, true>(x, y, z, rng);
 }
 __device__ __forceinline__ uint32_t cf3_encode_det(float x, float y, float z) {
     int32_t unused = 0;
-    return cf3_encode_impl<false>(x, y, z, unused);
+    return cf3_encode_impl<false, false>(x, y, z, unused).word;
 }
 // Exact: m * 2^(E-22) is representable, the sign bit is applied last (so m = 0 keeps its sign).
 __device__ __forceinline__ float cf3_component(uint32_t w, uint32_t mpos, uint32_t spos) {

@@ -16,38 +16,49 @@ constexpr int kBlock = 256;
 inline uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------- restriction, AMR.h:961-996
-// grid: x = cells of one padded domain, y = work item (domain), z = component
-__global__ void k_copy_new_to_old(Dims d, FieldSet f, const uint32_t* __restrict__ positions,
-                                  const int32_t* __restrict__ children, const uint32_t* __restrict__ items,
-                                  uint32_t substep, uint32_t max_depth) {
-    const uint32_t cells = d.t * d.t * d.t;
-    const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= cells) return;
-    const uint32_t slot = items ? items[blockIdx.y] : blockIdx.y;
+// One CTA per (domain, component).  A domain without children is a straight copy of its padded
+// cube (contiguous, 16-byte aligned: 128-bit loads and stores); otherwise every cell covered by a
+// child becomes the mean of the child's 2x2x2 cells and the rest is copied.
+template <int N, int P>
+__global__ void __launch_bounds__(256) k_copy_new_to_old(FieldSet f, const uint32_t* __restrict__ positions,
+                                                        const int32_t* __restrict__ children,
+                                                        const uint32_t* __restrict__ items, uint32_t substep,
+                                                        uint32_t max_depth) {
+    constexpr uint32_t T = N + 2 * P, CELLS = T * T * T, H = N / 2;
+    static_assert(CELLS % 4 == 0, "padded domains are whole 16-byte vectors");
+    const uint32_t slot = items ? items[blockIdx.x] : blockIdx.x;
     const int depth = pos_depth(positions[slot]);
     if (depth == -1 || !active_depth(substep, (uint32_t)depth, max_depth)) return;
-    const uint32_t x = cell % d.t, y = (cell / d.t) % d.t, z = cell / (d.t * d.t);
-    const uint32_t h = d.n / 2u;
-    const uint32_t tx = (x - d.p) / h, ty = (y - d.p) / h, tz = (z - d.p) / h;   // ghosts wrap to >= 2
-    const int32_t child = (tx < 2u && ty < 2u && tz < 2u) ? children[tx + ty * 2u + tz * 4u + slot * 8u] : -1;
-    const uint64_t o = (uint64_t)slot * cells + cell;
-    float* __restrict__ dst = f.old_f[blockIdx.z];
-    const float* __restrict__ src = f.new_f[blockIdx.z];
-    if (child == -1) {
-        dst[o] = src[o];
+    float* __restrict__ dst = f.old_f[blockIdx.y] + (size_t)slot * CELLS;
+    const float* __restrict__ src = f.new_f[blockIdx.y];
+    const float* __restrict__ own = src + (size_t)slot * CELLS;
+    int32_t ch[8];
+    bool any_child = false;
+#pragma unroll
+    for (int i = 0; i < 8; i++) { ch[i] = children[slot * 8u + i]; any_child |= ch[i] != -1; }
+    if (!any_child) {
+        const float4* s4 = reinterpret_cast<const float4*>(own);
+        float4* d4 = reinterpret_cast<float4*>(dst);
+        for (uint32_t i = threadIdx.x; i < CELLS / 4; i += blockDim.x) d4[i] = __ldcs(s4 + i);
         return;
     }
-    const uint32_t cx = ((x - d.p) * 2u) % d.n + d.p, cy = ((y - d.p) * 2u) % d.n + d.p, cz = ((z - d.p) * 2u) % d.n + d.p;
-    const uint64_t ci = (uint64_t)child * cells + ((uint64_t)cz * d.t + cy) * d.t + cx;
-    const uint64_t t = d.t, t2 = t * t;
-    float s = __fadd_rn(src[ci], src[ci + 1]);
-    s = __fadd_rn(s, src[ci + t]);
-    s = __fadd_rn(s, src[ci + t + 1]);
-    s = __fadd_rn(s, src[ci + t2]);
-    s = __fadd_rn(s, src[ci + t2 + 1]);
-    s = __fadd_rn(s, src[ci + t2 + t]);
-    s = __fadd_rn(s, src[ci + t2 + t + 1]);
-    dst[o] = __fmul_rn(s, .125f);
+    for (uint32_t cell = threadIdx.x; cell < CELLS; cell += blockDim.x) {
+        const uint32_t x = cell % T, y = (cell / T) % T, z = cell / (T * T);
+        const uint32_t tx = (x - P) / H, ty = (y - P) / H, tz = (z - P) / H;   // ghosts wrap to >= 2
+        const int32_t child = (tx < 2u && ty < 2u && tz < 2u) ? ch[tx + ty * 2u + tz * 4u] : -1;
+        if (child == -1) { dst[cell] = own[cell]; continue; }
+        const uint32_t cx = ((x - P) * 2u) % N + P, cy = ((y - P) * 2u) % N + P, cz = ((z - P) * 2u) % N + P;
+        const float* c = src + (size_t)child * CELLS + (cz * T + cy) * T + cx;
+        constexpr uint32_t T2 = T * T;
+        float s = __fadd_rn(c[0], c[1]);
+        s = __fadd_rn(s, c[T]);
+        s = __fadd_rn(s, c[T + 1]);
+        s = __fadd_rn(s, c[T2]);
+        s = __fadd_rn(s, c[T2 + 1]);
+        s = __fadd_rn(s, c[T2 + T]);
+        s = __fadd_rn(s, c[T2 + T + 1]);
+        dst[cell] = __fmul_rn(s, .125f);
+    }
 }
 
 // ---------------------------------------------------------------- prolongation, AMR.h:1053-1073
@@ -79,21 +90,31 @@ __global__ void k_copy_to_child(Dims d, float inv_n, float* buf, uint32_t offset
 }
 
 // ---------------------------------------------------------------- ghost fill, AMR.h:634-762
-// Index of ghost cell (slot, face, layer, v, u) in the staging buffer of one field.
-__device__ __forceinline__ uint64_t ghost_index(const Dims& d, uint32_t slot, uint32_t face, uint32_t layer,
-                                                uint32_t v, uint32_t u) {
-    return ((((uint64_t)slot * 6u + face) * d.p + layer) * d.n + v) * d.n + u;
-}
-// Padded cell written by ghost (face, layer, u, v) of a domain (AMR.h:715-735).
-__device__ __forceinline__ void ghost_cell(const Dims& d, uint32_t face, uint32_t layer, uint32_t u, uint32_t v,
-                                           uint32_t* w) {
+// The ghost cells of one field are enumerated per (slot, face) in the order that is contiguous
+// in the destination domain: x-faces with the layer (x) fastest, the other faces with u (x)
+// fastest.  The staging buffer uses the same order, so both phases stream it.
+template <int N, int P>
+struct GhostShape {
+    static constexpr uint32_t T = N + 2 * P, FACE = P * N * N, SLOT = 6 * FACE, CELLS = T * T * T;
+};
+// slot, face and written padded cell (AMR.h:715-735) of ghost number gid
+template <int N, int P>
+__device__ __forceinline__ void ghost_decode(uint64_t gid, uint32_t& slot, uint32_t& face, uint32_t* w) {
+    using G = GhostShape<N, P>;
+    slot = (uint32_t)(gid / G::SLOT);
+    const uint32_t r = (uint32_t)(gid - (uint64_t)slot * G::SLOT);
+    face = r / G::FACE;
+    const uint32_t j = r - face * G::FACE;
+    uint32_t layer, u, v;
+    if (face == 0 || face == 3) { layer = j % P; u = (j / P) % N; v = j / (P * N); }
+    else { u = j % N; v = (j / N) % N; layer = j / (N * N); }
     switch (face) {
-        case 0: w[0] = layer + d.p + d.n; w[1] = u + d.p; w[2] = v + d.p; break;
-        case 1: w[0] = u + d.p; w[1] = layer + d.p + d.n; w[2] = v + d.p; break;
-        case 2: w[0] = u + d.p; w[1] = v + d.p; w[2] = layer + d.p + d.n; break;
-        case 3: w[0] = layer; w[1] = u + d.p; w[2] = v + d.p; break;
-        case 4: w[0] = u + d.p; w[1] = layer; w[2] = v + d.p; break;
-        default: w[0] = u + d.p; w[1] = v + d.p; w[2] = layer; break;
+        case 0: w[0] = layer + P + N; w[1] = u + P; w[2] = v + P; break;
+        case 1: w[0] = u + P; w[1] = layer + P + N; w[2] = v + P; break;
+        case 2: w[0] = u + P; w[1] = v + P; w[2] = layer + P + N; break;
+        case 3: w[0] = layer; w[1] = u + P; w[2] = v + P; break;
+        case 4: w[0] = u + P; w[1] = layer; w[2] = v + P; break;
+        default: w[0] = u + P; w[1] = v + P; w[2] = layer; break;
     }
 }
 struct GhostJob {
@@ -112,25 +133,22 @@ __device__ __forceinline__ GhostJob ghost_job(uint64_t bd, uint32_t substep, uin
 }
 
 // Phase 1: interpolate every ghost value of every component from the unmodified fields into
-// the staging buffer (old values first, then new, per component).
-template <int T>
-__global__ void k_ghost_gather(Dims d, float inv_n, FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
-                               uint32_t substep, uint32_t max_depth, int copy_only_new, float* __restrict__ stage) {
+// the staging buffer (per component: old values, then new values).
+template <int N, int P>
+__global__ void __launch_bounds__(256) k_ghost_gather(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
+                                                     uint32_t substep, uint32_t max_depth, int copy_only_new,
+                                                     float* __restrict__ stage) {
+    using G = GhostShape<N, P>;
+    constexpr uint32_t T = G::T;
+    constexpr float inv_n = 1.f / N;
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t per_slot = 6ull * d.p * d.n * d.n;
-    const uint64_t total = (uint64_t)used * per_slot;
+    const uint64_t total = (uint64_t)used * G::SLOT;
     if (gid >= total) return;
-    uint32_t u = (uint32_t)(gid % d.n);
-    uint64_t rest = gid / d.n;
-    const uint32_t v = (uint32_t)(rest % d.n); rest /= d.n;
-    const uint32_t layer = (uint32_t)(rest % d.p); rest /= d.p;
-    const uint32_t face = (uint32_t)(rest % 6u);
-    const uint32_t slot = (uint32_t)(rest / 6u);
+    uint32_t slot, face, w[3];
+    ghost_decode<N, P>(gid, slot, face, w);
     const uint64_t bd = bds[slot * 6u + face];
     const GhostJob j = ghost_job(bd, substep, max_depth);
     if (!j.active) return;
-    uint32_t w[3];
-    ghost_cell(d, face, layer, u, v, w);
     const float rel_scale = __uint_as_float((127u - j.dd) << 23);         // 1 / 2^depth_diff
     const float3 rel_pos = cf3_decode((uint32_t)(bd >> 32));
     const float relp[3] = {rel_pos.x, rel_pos.y, rel_pos.z};
@@ -138,49 +156,44 @@ __global__ void k_ghost_gather(Dims d, float inv_n, FieldSet f, const uint64_t* 
     float r[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {                                          // AMR.h:737-753
-        float rp = __fmaf_rn(__fadd_rn(__fsub_rn((float)w[a], (float)d.p), .5f), inv_n, -.5f);
+        float rp = __fmaf_rn(__fadd_rn(__fsub_rn((float)w[a], (float)P), .5f), inv_n, -.5f);
         rp = __fmaf_rn(rp, rel_scale, relp[a]);
-        rp = __fsub_rn(__fmaf_rn(__fadd_rn(rp, .5f), (float)d.n, (float)d.p), .5f);
-        const uint32_t idx = j.target == 0 ? min(__float2uint_rz(__fadd_rn(fmaxf(rp, 0.f), .5f)), d.t - 2u)
-                                           : min(__float2uint_rz(__fadd_rn(fmaxf(rp, (float)d.p), .5f)), d.t - d.p - 2u);
+        rp = __fsub_rn(__fmaf_rn(__fadd_rn(rp, .5f), (float)N, (float)P), .5f);
+        const uint32_t idx = j.target == 0 ? min(__float2uint_rz(__fadd_rn(fmaxf(rp, 0.f), .5f)), T - 2u)
+                                           : min(__float2uint_rz(__fadd_rn(fmaxf(rp, (float)P), .5f)), T - P - 2u);
         ri[a] = idx;
         r[a] = __fsub_rn(rp, (float)idx);
     }
-    const uint64_t cells = (uint64_t)T * T * T;
-    const uint64_t rin = (uint64_t)j.target * cells + ri[0] + ((uint64_t)ri[1] + (uint64_t)ri[2] * T) * T;
+    const uint64_t rin = (uint64_t)j.target * G::CELLS + ri[0] + (ri[1] + ri[2] * T) * T;
     const float tm = (float)((substep >> (max_depth - (uint32_t)j.cd)) & ((1u << j.dd) - 1u));   // AMR.h:634-639
     const float t0 = __fmul_rn(tm, rel_scale), t1 = __fmul_rn(__fadd_rn(tm, 1.f), rel_scale);
-    const uint64_t gi = ghost_index(d, slot, face, layer, v, u);
     for (int k = 0; k < f.ncomp; k++) {
         const float od = interp10<T>(f.old_f[k] + rin, r[0], r[1], r[2]);
         const float nw = interp10<T>(f.new_f[k] + rin, r[0], r[1], r[2]);
         float* sk = stage + (uint64_t)k * 2u * total;
-        if (!copy_only_new) sk[gi] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
-        sk[total + gi] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
+        if (!copy_only_new) sk[gid] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
+        sk[total + gid] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
     }
 }
 // Phase 2: write the staged ghost values into the fields.
-__global__ void k_ghost_scatter(Dims d, FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
-                                uint32_t substep, uint32_t max_depth, int copy_only_new, const float* __restrict__ stage) {
+template <int N, int P>
+__global__ void __launch_bounds__(256) k_ghost_scatter(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
+                                                      uint32_t substep, uint32_t max_depth, int copy_only_new,
+                                                      const float* __restrict__ stage) {
+    using G = GhostShape<N, P>;
+    constexpr uint32_t T = G::T;
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t per_slot = 6ull * d.p * d.n * d.n;
-    const uint64_t total = (uint64_t)used * per_slot;
+    const uint64_t total = (uint64_t)used * G::SLOT;
     if (gid >= total) return;
-    uint32_t u = (uint32_t)(gid % d.n);
-    uint64_t rest = gid / d.n;
-    const uint32_t v = (uint32_t)(rest % d.n); rest /= d.n;
-    const uint32_t layer = (uint32_t)(rest % d.p); rest /= d.p;
-    const uint32_t face = (uint32_t)(rest % 6u);
-    const uint32_t slot = (uint32_t)(rest / 6u);
+    uint32_t slot, face, w[3];
+    ghost_decode<N, P>(gid, slot, face, w);
     const GhostJob j = ghost_job(bds[slot * 6u + face], substep, max_depth);
     if (!j.active) return;
-    uint32_t w[3];
-    ghost_cell(d, face, layer, u, v, w);
-    const uint64_t win = (uint64_t)slot * d.t * d.t * d.t + w[0] + ((uint64_t)w[1] + (uint64_t)w[2] * d.t) * d.t;
+    const uint64_t win = (uint64_t)slot * G::CELLS + w[0] + (w[1] + w[2] * T) * T;
     for (int k = 0; k < f.ncomp; k++) {
         const float* sk = stage + (uint64_t)k * 2u * total;
-        if (!copy_only_new) f.old_f[k][win] = sk[gid];
-        f.new_f[k][win] = sk[total + gid];
+        if (!copy_only_new) f.old_f[k][win] = __ldcs(sk + gid);
+        f.new_f[k][win] = __ldcs(sk + total + gid);
     }
 }
 
@@ -191,9 +204,12 @@ cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* po
                                    const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
                                    cudaStream_t st) {
     if (n_items == 0 || f.ncomp == 0) return cudaSuccess;
-    const dim3 grid(blocks_for((uint64_t)d.t * d.t * d.t), n_items, (uint32_t)f.ncomp);
-    k_copy_new_to_old<<<grid, kBlock, 0, st>>>(d, f, positions, children, items, substep, max_depth);
-    return cudaGetLastError();
+    const dim3 grid(n_items, (uint32_t)f.ncomp);
+#define AMR_RESTRICT(N, P) \
+    if (d.n == N && d.p == P) { k_copy_new_to_old<N, P><<<grid, kBlock, 0, st>>>(f, positions, children, items, substep, max_depth); return cudaGetLastError(); }
+    AMR_FOR_EACH_CONFIG(AMR_RESTRICT)
+#undef AMR_RESTRICT
+    return cudaErrorInvalidValue;
 }
 cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t child, int32_t parent, cudaStream_t st) {
     const float inv_n = 1.f / (float)d.n;
@@ -208,18 +224,19 @@ cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* bo
                                    cudaStream_t st) {
     const uint64_t total = (uint64_t)used * 6u * d.p * d.n * d.n;
     if (total == 0 || f.ncomp == 0) return cudaSuccess;
-    const float inv_n = 1.f / (float)d.n;
-    switch (d.t) {
-        case 22: k_ghost_gather<22><<<blocks_for(total), kBlock, 0, st>>>(d, inv_n, f, boundaries, used, substep, max_depth, copy_only_new, scratch); break;
-        case 32: k_ghost_gather<32><<<blocks_for(total), kBlock, 0, st>>>(d, inv_n, f, boundaries, used, substep, max_depth, copy_only_new, scratch); break;
-        case 38: k_ghost_gather<38><<<blocks_for(total), kBlock, 0, st>>>(d, inv_n, f, boundaries, used, substep, max_depth, copy_only_new, scratch); break;
-        case 12: k_ghost_gather<12><<<blocks_for(total), kBlock, 0, st>>>(d, inv_n, f, boundaries, used, substep, max_depth, copy_only_new, scratch); break;
-        default: return cudaErrorInvalidValue;
+#define AMR_GHOST(N, P)                                                                                     \
+    if (d.n == N && d.p == P) {                                                                             \
+        k_ghost_gather<N, P><<<blocks_for(total), kBlock, 0, st>>>(f, boundaries, used, substep, max_depth,  \
+                                                                   copy_only_new, scratch);                \
+        cudaError_t e = cudaGetLastError();                                                                 \
+        if (e != cudaSuccess) return e;                                                                     \
+        k_ghost_scatter<N, P><<<blocks_for(total), kBlock, 0, st>>>(f, boundaries, used, substep, max_depth, \
+                                                                    copy_only_new, scratch);               \
+        return cudaGetLastError();                                                                          \
     }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_ghost_scatter<<<blocks_for(total), kBlock, 0, st>>>(d, f, boundaries, used, substep, max_depth, copy_only_new, scratch);
-    return cudaGetLastError();
+    AMR_FOR_EACH_CONFIG(AMR_GHOST)
+#undef AMR_GHOST
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace amr

@@ -141,7 +141,11 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
     __shared__ int s_abort;
 
     const uint32_t tid = threadIdx.x;
-    const uint32_t x = tid % N, y = tid / N;
+    // Thread -> (x, y).  At N = 16 a warp would cover rows y and y+1 of the 22-float plane rows,
+    // whose banks overlap for 6 lanes; pairing rows y and y+8 (176 floats apart = 16 banks)
+    // makes every shared-memory access of the warp conflict-free.
+    const uint32_t x = tid % N;
+    const uint32_t y = N == 16 ? ((tid / N) >> 1) | (((tid / N) & 1u) << 3) : tid / N;
     const int c0 = (int)((y + P) * T + (x + P));
 
     if (tid == 0) {
@@ -179,6 +183,7 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
         }
         const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
 
+        uint32_t base = seq0 % R;   // ring slot of plane z, advanced incrementally
 #pragma unroll 1
         for (uint32_t z = 0; z < (uint32_t)N; z++) {
             // planes z .. z+2P of the padded domain must have landed
@@ -192,7 +197,7 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
             if (ok) {
                 uint32_t slot[2 * P + 1];
 #pragma unroll
-                for (int j = 0; j <= 2 * P; j++) slot[j] = (seq0 + z + j) % R;
+                for (int j = 0; j <= 2 * P; j++) slot[j] = base + j >= (uint32_t)R ? base + j - R : base + j;
                 const uint32_t zg = node * N + z;
                 const size_t o = ((size_t)zg * N + y) * N + x;   // inner-layout index
 
@@ -222,13 +227,15 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
                         float gx, gy, gz, hx, hy, hz;
                         fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
                         int32_t rd = cell_rng(seed_d[k], x, y, zg);
-                        const uint32_t wh = cf3_encode(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
+                        // the Hessians are quantised exactly as the reference writes and re-reads them
+                        const Cf3Quantised hq = cf3_encode_quantised(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
                         G[k] = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
                         a.grad[k][o] = G[k];
                         const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
                         int32_t rm = cell_rng(seed_m[k], x, y, zg);
-                        const uint32_t wo = cf3_encode(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
-                        a.lap[k][o] = trace_contra(sym_from_cf3(wh, wo), ginv);
+                        const Cf3Quantised oq = cf3_encode_quantised(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
+                        const Sym H{hq.value.x, oq.value.x, oq.value.y, hq.value.y, oq.value.z, hq.value.z};   // tensors.h:430-435
+                        a.lap[k][o] = trace_contra(H, ginv);
                     }
                     int32_t rc = cell_rng(seed_c, x, y, zg);
                     uint32_t out[6];
@@ -239,6 +246,7 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
             }
             __syncthreads();   // every thread is done with plane z: its slot may be refilled
             if (s_abort) break;
+            base = base + 1 == (uint32_t)R ? 0u : base + 1;
             if (tid == 0 && z + R < (uint32_t)T) {
                 const uint32_t q = z + R, sq = seq0 + q, s = sq % R;
                 mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
