@@ -21,18 +21,32 @@ __device__ __forceinline__ int32_t prng_next(int32_t& s) {
     s = (int32_t)v;
     return s;
 }
-__device__ __forceinline__ float prng_float(int32_t& s) {
-    return __fmul_rn(__int2float_rn(prng_next(s)), 2.3283064E-10f);
+// generate_float() * 0.95f, the encoder's noise (tensors.h:359-361).  The float 2.3283064E-10f is
+// exactly 2^-32, so generate_float() is an exact power-of-two scaling of the converted integer
+// (nonzero results are at least 2^-32, far from the subnormal range) and the two products round
+// once: as the single product by 0.95f * 2^-32, which is exact as a float constant.
+__device__ __forceinline__ float prng_noise(int32_t& s) {
+    constexpr float kScale = 0.95f * 0x1p-32f;
+    return __fmul_rn(__int2float_rn(prng_next(s)), kScale);
 }
 // Per-cell generator of the stencil kernels, keyed by (launch seed, x, y, slot*N + z)
-// (AMR.h:1160-1162, BSSN.h:64-66).
-__device__ __forceinline__ int32_t cell_rng(int32_t seed, uint32_t x, uint32_t y, uint32_t zg) {
+// (AMR.h:1160-1162, BSSN.h:64-66):
+//   s = seed + x*2178614;  s ^= next(s) * y;  s ^= next(s) * zg
+// next() leaves its result in s, so the first three steps give s = g ^ (g*y) with g = next(seed +
+// x*2178614) and the last one s = h ^ (h*zg) with h = next(that): everything but the final
+// multiply and xor depends on (seed, x, y) only.  cell_rng_prefix computes h once per thread;
+// cell_rng_at finishes the generator for one cell.
+__device__ __forceinline__ int32_t cell_rng_prefix(int32_t seed, uint32_t x, uint32_t y) {
     int32_t s = (int32_t)((uint32_t)seed + x * 2178614u);
-    int32_t g = prng_next(s);
-    s = (int32_t)((uint32_t)s ^ ((uint32_t)g * y));
-    g = prng_next(s);
-    s = (int32_t)((uint32_t)s ^ ((uint32_t)g * zg));
-    return s;
+    const int32_t g = prng_next(s);
+    s = (int32_t)((uint32_t)g ^ ((uint32_t)g * y));
+    return prng_next(s);
+}
+__device__ __forceinline__ int32_t cell_rng_at(int32_t prefix, uint32_t zg) {
+    return (int32_t)((uint32_t)prefix ^ ((uint32_t)prefix * zg));
+}
+__device__ __forceinline__ int32_t cell_rng(int32_t seed, uint32_t x, uint32_t y, uint32_t zg) {
+    return cell_rng_at(cell_rng_prefix(seed, x, y), zg);
 }
 
 // ------------------------------------------------------------------ compressed_float3 (tensors.h:305-394)
@@ -52,18 +66,18 @@ struct Cf3Quantised {
 };
 template <bool STOCHASTIC, bool WANT_VALUE>
 __device__ __forceinline__ Cf3Quantised cf3_encode_impl(float x, float y, float z, int32_t& rng) {
-    const uint32_t ex = (__float_as_uint(x) >> 23) & 255u;
-    const uint32_t ey = (__float_as_uint(y) >> 23) & 255u;
-    const uint32_t ez = (__float_as_uint(z) >> 23) & 255u;
-    const uint32_t E = min(max(max(ex, max(ey, ez)), 112u) - 112u, 31u);
+    // largest biased exponent of the three: the exponent field of the largest magnitude's bits
+    const uint32_t amax = max(__float_as_uint(x) & 0x7FFFFFFFu, max(__float_as_uint(y) & 0x7FFFFFFFu,
+                                                                    __float_as_uint(z) & 0x7FFFFFFFu));
+    const uint32_t E = min(max(amax >> 23, 112u) - 112u, 31u);
     const float scale = __uint_as_float((149u - E) << 23);          // 2^(22-E), exact
     x = __fmul_rn(x, scale);
     y = __fmul_rn(y, scale);
     z = __fmul_rn(z, scale);
     if (STOCHASTIC) {   // the noise product is rounded before it is added (not fused)
-        x = __fadd_rn(x, __fmul_rn(prng_float(rng), .95f));
-        y = __fadd_rn(y, __fmul_rn(prng_float(rng), .95f));
-        z = __fadd_rn(z, __fmul_rn(prng_float(rng), .95f));
+        x = __fadd_rn(x, prng_noise(rng));
+        y = __fadd_rn(y, prng_noise(rng));
+        z = __fadd_rn(z, prng_noise(rng));
     }
     const uint32_t bx = cf3_mantissa_bits(x), by = cf3_mantissa_bits(y), bz = cf3_mantissa_bits(z);
     const uint32_t sx = x < 0.f, sy = y < 0.f, sz = z < 0.f;

@@ -16,11 +16,14 @@ constexpr int kBlock = 256;
 inline uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------- restriction, AMR.h:961-996
-// One CTA per (domain, component).  A domain without children is a straight copy of its padded
-// cube (contiguous, 16-byte aligned: 128-bit loads and stores); otherwise every cell covered by a
-// child becomes the mean of the child's 2x2x2 cells and the rest is copied.
+// One CTA per (domain, component, slab): the padded cube is cut into kSlabs contiguous ranges so a
+// domain with children (8 gathers per covered cell) spreads over as many CTAs as a leaf.  A domain
+// without children is a straight copy of its range (16-byte aligned: 128-bit loads and stores,
+// several in flight per thread); otherwise every cell covered by a child becomes the mean of the
+// child's 2x2x2 cells and the rest is copied.
+constexpr uint32_t kSlabs = 4;
 template <int N, int P>
-__global__ void __launch_bounds__(256) k_copy_new_to_old(FieldSet f, const uint32_t* __restrict__ positions,
+__global__ void __launch_bounds__(kBlock) k_copy_new_to_old(FieldSet f, const uint32_t* __restrict__ positions,
                                                         const int32_t* __restrict__ children,
                                                         const uint32_t* __restrict__ items, uint32_t substep,
                                                         uint32_t max_depth) {
@@ -36,13 +39,24 @@ __global__ void __launch_bounds__(256) k_copy_new_to_old(FieldSet f, const uint3
     bool any_child = false;
 #pragma unroll
     for (int i = 0; i < 8; i++) { ch[i] = children[slot * 8u + i]; any_child |= ch[i] != -1; }
-    if (!any_child) {
+    if (!any_child) {   // kU vectors per thread in flight before the first store
+        constexpr uint32_t V = CELLS / 4, kU = 8;
+        const uint32_t end = (blockIdx.z + 1u) * V / kSlabs;
         const float4* s4 = reinterpret_cast<const float4*>(own);
         float4* d4 = reinterpret_cast<float4*>(dst);
-        for (uint32_t i = threadIdx.x; i < CELLS / 4; i += blockDim.x) d4[i] = __ldcs(s4 + i);
+        for (uint32_t base = blockIdx.z * V / kSlabs + threadIdx.x; base < end; base += kU * kBlock) {
+            float4 b[kU];
+#pragma unroll
+            for (uint32_t i = 0; i < kU; i++)
+                if (base + i * kBlock < end) b[i] = __ldcs(s4 + base + i * kBlock);
+#pragma unroll
+            for (uint32_t i = 0; i < kU; i++)
+                if (base + i * kBlock < end) d4[base + i * kBlock] = b[i];
+        }
         return;
     }
-    for (uint32_t cell = threadIdx.x; cell < CELLS; cell += blockDim.x) {
+    const uint32_t end = (blockIdx.z + 1u) * CELLS / kSlabs;
+    for (uint32_t cell = blockIdx.z * CELLS / kSlabs + threadIdx.x; cell < end; cell += kBlock) {
         const uint32_t x = cell % T, y = (cell / T) % T, z = cell / (T * T);
         const uint32_t tx = (x - P) / H, ty = (y - P) / H, tz = (z - P) / H;   // ghosts wrap to >= 2
         const int32_t child = (tx < 2u && ty < 2u && tz < 2u) ? ch[tx + ty * 2u + tz * 4u] : -1;
@@ -90,24 +104,27 @@ __global__ void k_copy_to_child(Dims d, float inv_n, float* buf, uint32_t offset
 }
 
 // ---------------------------------------------------------------- ghost fill, AMR.h:634-762
-// The ghost cells of one field are enumerated per (slot, face) in the order that is contiguous
-// in the destination domain: x-faces with the layer (x) fastest, the other faces with u (x)
-// fastest.  The staging buffer uses the same order, so both phases stream it.
+// The fill's result is defined as the interpolation of the fields as they were before the fill
+// (the reference's own launch reads cells that it may be writing at the same time).  Which cells
+// can a fill read?  For a non-root source the nearest index is clamped to [P, T-P-2]
+// (AMR.h:743-750) and the 10-point stencil reaches one cell back (d[-1], d[-T], d[-T^2]) and one
+// forward (d[+1], ...), so its reads stay in [P-1, T-P-1] along each axis, with at most one axis
+// at P-1: the interior and the innermost layer (P-1) of the -x, -y and -z ghost faces.  The root
+// source (target 0) may be read anywhere, but the root is never filled (its depth is 0).  So the
+// only ghost cells that a fill both reads and writes are those innermost lower layers.  Phase 1
+// writes every other ghost cell directly and stages the innermost lower layers; phase 2 copies the
+// staged values into place.  Every cell ends with the value computed from the pre-fill state.
+//
+// Ghost cells of one field are enumerated per (slot, face) in the order that is contiguous in the
+// destination domain: x-faces with the layer (x) fastest, the other faces with u (x) fastest.
 template <int N, int P>
 struct GhostShape {
     static constexpr uint32_t T = N + 2 * P, FACE = P * N * N, SLOT = 6 * FACE, CELLS = T * T * T;
+    static constexpr uint32_t STAGED = 3 * N * N;   // staged cells per slot: one layer of each lower face
 };
-// slot, face and written padded cell (AMR.h:715-735) of ghost number gid
+// padded cell written for layer `layer` and face coordinates (u, v) of a face (AMR.h:715-735)
 template <int N, int P>
-__device__ __forceinline__ void ghost_decode(uint64_t gid, uint32_t& slot, uint32_t& face, uint32_t* w) {
-    using G = GhostShape<N, P>;
-    slot = (uint32_t)(gid / G::SLOT);
-    const uint32_t r = (uint32_t)(gid - (uint64_t)slot * G::SLOT);
-    face = r / G::FACE;
-    const uint32_t j = r - face * G::FACE;
-    uint32_t layer, u, v;
-    if (face == 0 || face == 3) { layer = j % P; u = (j / P) % N; v = j / (P * N); }
-    else { u = j % N; v = (j / N) % N; layer = j / (N * N); }
+__device__ __forceinline__ void ghost_cell(uint32_t face, uint32_t layer, uint32_t u, uint32_t v, uint32_t* w) {
     switch (face) {
         case 0: w[0] = layer + P + N; w[1] = u + P; w[2] = v + P; break;
         case 1: w[0] = u + P; w[1] = layer + P + N; w[2] = v + P; break;
@@ -116,6 +133,20 @@ __device__ __forceinline__ void ghost_decode(uint64_t gid, uint32_t& slot, uint3
         case 4: w[0] = u + P; w[1] = layer; w[2] = v + P; break;
         default: w[0] = u + P; w[1] = v + P; w[2] = layer; break;
     }
+}
+// slot, face, face coordinates (u, v) and written padded cell of ghost number gid
+template <int N, int P>
+__device__ __forceinline__ void ghost_decode(uint64_t gid, uint32_t& slot, uint32_t& face, uint32_t& u, uint32_t& v,
+                                             uint32_t* w) {
+    using G = GhostShape<N, P>;
+    slot = (uint32_t)(gid / G::SLOT);
+    const uint32_t r = (uint32_t)(gid - (uint64_t)slot * G::SLOT);
+    face = r / G::FACE;
+    const uint32_t j = r - face * G::FACE;
+    uint32_t layer;
+    if (face == 0 || face == 3) { layer = j % P; u = (j / P) % N; v = j / (P * N); }
+    else { u = j % N; v = (j / N) % N; layer = j / (N * N); }
+    ghost_cell<N, P>(face, layer, u, v, w);
 }
 struct GhostJob {
     bool active;
@@ -132,20 +163,19 @@ __device__ __forceinline__ GhostJob ghost_job(uint64_t bd, uint32_t substep, uin
     return j;
 }
 
-// Phase 1: interpolate every ghost value of every component from the unmodified fields into
-// the staging buffer (per component: old values, then new values).
+// Phase 1: interpolate every ghost value of every component from the fields; write it, or stage
+// it if it lies in an innermost lower layer (per component: old values, then new values).
 template <int N, int P>
-__global__ void __launch_bounds__(256) k_ghost_gather(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
-                                                     uint32_t substep, uint32_t max_depth, int copy_only_new,
-                                                     float* __restrict__ stage) {
+__global__ void __launch_bounds__(256) k_ghost_fill(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
+                                                   uint32_t substep, uint32_t max_depth, int copy_only_new,
+                                                   float* __restrict__ stage) {
     using G = GhostShape<N, P>;
     constexpr uint32_t T = G::T;
     constexpr float inv_n = 1.f / N;
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t total = (uint64_t)used * G::SLOT;
-    if (gid >= total) return;
-    uint32_t slot, face, w[3];
-    ghost_decode<N, P>(gid, slot, face, w);
+    if (gid >= (uint64_t)used * G::SLOT) return;
+    uint32_t slot, face, u, v, w[3];
+    ghost_decode<N, P>(gid, slot, face, u, v, w);
     const uint64_t bd = bds[slot * 6u + face];
     const GhostJob j = ghost_job(bd, substep, max_depth);
     if (!j.active) return;
@@ -167,33 +197,39 @@ __global__ void __launch_bounds__(256) k_ghost_gather(FieldSet f, const uint64_t
     const uint64_t rin = (uint64_t)j.target * G::CELLS + ri[0] + (ri[1] + ri[2] * T) * T;
     const float tm = (float)((substep >> (max_depth - (uint32_t)j.cd)) & ((1u << j.dd) - 1u));   // AMR.h:634-639
     const float t0 = __fmul_rn(tm, rel_scale), t1 = __fmul_rn(__fadd_rn(tm, 1.f), rel_scale);
+    const bool staged = face >= 3u && w[face - 3u] == P - 1u;
+    const uint64_t n_staged = (uint64_t)used * G::STAGED;
+    const uint64_t out = staged ? ((uint64_t)slot * 3u + (face - 3u)) * (N * N) + u + v * N
+                                : (uint64_t)slot * G::CELLS + w[0] + (w[1] + w[2] * T) * T;
     for (int k = 0; k < f.ncomp; k++) {
         const float od = interp10<T>(f.old_f[k] + rin, r[0], r[1], r[2]);
         const float nw = interp10<T>(f.new_f[k] + rin, r[0], r[1], r[2]);
-        float* sk = stage + (uint64_t)k * 2u * total;
-        if (!copy_only_new) sk[gid] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
-        sk[total + gid] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
+        float* dst_old = staged ? stage + (uint64_t)k * 2u * n_staged : f.old_f[k];
+        float* dst_new = staged ? stage + ((uint64_t)k * 2u + 1u) * n_staged : f.new_f[k];
+        if (!copy_only_new) dst_old[out] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
+        dst_new[out] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
     }
 }
-// Phase 2: write the staged ghost values into the fields.
+// Phase 2: write the staged innermost lower layers into the fields.
 template <int N, int P>
-__global__ void __launch_bounds__(256) k_ghost_scatter(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
-                                                      uint32_t substep, uint32_t max_depth, int copy_only_new,
-                                                      const float* __restrict__ stage) {
+__global__ void __launch_bounds__(256) k_ghost_commit(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
+                                                     uint32_t substep, uint32_t max_depth, int copy_only_new,
+                                                     const float* __restrict__ stage) {
     using G = GhostShape<N, P>;
     constexpr uint32_t T = G::T;
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t total = (uint64_t)used * G::SLOT;
-    if (gid >= total) return;
-    uint32_t slot, face, w[3];
-    ghost_decode<N, P>(gid, slot, face, w);
-    const GhostJob j = ghost_job(bds[slot * 6u + face], substep, max_depth);
-    if (!j.active) return;
+    const uint64_t n_staged = (uint64_t)used * G::STAGED;
+    if (gid >= n_staged) return;
+    const uint32_t slot = (uint32_t)(gid / G::STAGED);
+    const uint32_t r = (uint32_t)(gid - (uint64_t)slot * G::STAGED);
+    const uint32_t face = 3u + r / (N * N), u = r % N, v = (r / N) % N;
+    if (!ghost_job(bds[slot * 6u + face], substep, max_depth).active) return;
+    uint32_t w[3];
+    ghost_cell<N, P>(face, P - 1u, u, v, w);
     const uint64_t win = (uint64_t)slot * G::CELLS + w[0] + (w[1] + w[2] * T) * T;
     for (int k = 0; k < f.ncomp; k++) {
-        const float* sk = stage + (uint64_t)k * 2u * total;
-        if (!copy_only_new) f.old_f[k][win] = __ldcs(sk + gid);
-        f.new_f[k][win] = __ldcs(sk + total + gid);
+        if (!copy_only_new) f.old_f[k][win] = __ldcs(stage + (uint64_t)k * 2u * n_staged + gid);
+        f.new_f[k][win] = __ldcs(stage + ((uint64_t)k * 2u + 1u) * n_staged + gid);
     }
 }
 
@@ -204,7 +240,7 @@ cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* po
                                    const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
                                    cudaStream_t st) {
     if (n_items == 0 || f.ncomp == 0) return cudaSuccess;
-    const dim3 grid(n_items, (uint32_t)f.ncomp);
+    const dim3 grid(n_items, (uint32_t)f.ncomp, kSlabs);
 #define AMR_RESTRICT(N, P) \
     if (d.n == N && d.p == P) { k_copy_new_to_old<N, P><<<grid, kBlock, 0, st>>>(f, positions, children, items, substep, max_depth); return cudaGetLastError(); }
     AMR_FOR_EACH_CONFIG(AMR_RESTRICT)
@@ -217,7 +253,7 @@ cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t ch
     return cudaGetLastError();
 }
 size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp) {
-    return (size_t)ncomp * 2u * used * 6u * d.p * d.n * d.n;
+    return (size_t)ncomp * 2u * used * 3u * d.n * d.n;
 }
 cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* boundaries, uint32_t used,
                                    uint32_t substep, uint32_t max_depth, int copy_only_new, float* scratch,
@@ -226,12 +262,12 @@ cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* bo
     if (total == 0 || f.ncomp == 0) return cudaSuccess;
 #define AMR_GHOST(N, P)                                                                                     \
     if (d.n == N && d.p == P) {                                                                             \
-        k_ghost_gather<N, P><<<blocks_for(total), kBlock, 0, st>>>(f, boundaries, used, substep, max_depth,  \
-                                                                   copy_only_new, scratch);                \
+        k_ghost_fill<N, P><<<blocks_for(total), kBlock, 0, st>>>(f, boundaries, used, substep, max_depth,    \
+                                                                 copy_only_new, scratch);                  \
         cudaError_t e = cudaGetLastError();                                                                 \
         if (e != cudaSuccess) return e;                                                                     \
-        k_ghost_scatter<N, P><<<blocks_for(total), kBlock, 0, st>>>(f, boundaries, used, substep, max_depth, \
-                                                                    copy_only_new, scratch);               \
+        k_ghost_commit<N, P><<<blocks_for((uint64_t)used * 3u * N * N), kBlock, 0, st>>>(                   \
+            f, boundaries, used, substep, max_depth, copy_only_new, scratch);                               \
         return cudaGetLastError();                                                                          \
     }
     AMR_FOR_EACH_CONFIG(AMR_GHOST)

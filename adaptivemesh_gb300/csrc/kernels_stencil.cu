@@ -155,13 +155,20 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
     }
     __syncthreads();
 
-    int32_t seed_d[NC], seed_m[NC], seed_c = a.seed_c;
+    // per-cell generators: the part that depends on (seed, x, y) only, once per thread
+    int32_t pre_d[NC], pre_m[NC], pre_c;
+    {
+        int32_t seed_d[NC], seed_m[NC], seed_c = a.seed_c;
 #pragma unroll
-    for (int k = 0; k < NC; k++) { seed_d[k] = a.seed_d[k]; seed_m[k] = a.seed_m[k]; }
-    if (a.seed_ptr) {
+        for (int k = 0; k < NC; k++) { seed_d[k] = a.seed_d[k]; seed_m[k] = a.seed_m[k]; }
+        if (a.seed_ptr) {
 #pragma unroll
-        for (int k = 0; k < NC; k++) { seed_d[k] = a.seed_ptr[2 * k]; seed_m[k] = a.seed_ptr[2 * k + 1]; }
-        seed_c = a.seed_ptr[12];
+            for (int k = 0; k < NC; k++) { seed_d[k] = a.seed_ptr[2 * k]; seed_m[k] = a.seed_ptr[2 * k + 1]; }
+            seed_c = a.seed_ptr[12];
+        }
+#pragma unroll
+        for (int k = 0; k < NC; k++) { pre_d[k] = cell_rng_prefix(seed_d[k], x, y); pre_m[k] = cell_rng_prefix(seed_m[k], x, y); }
+        pre_c = cell_rng_prefix(seed_c, x, y);
     }
 
     uint32_t seq0 = 0;   // sequence number of plane 0 of the current domain (ring slot = seq % R)
@@ -205,14 +212,14 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
                     auto pl = [&](int j) { return (const float*)(ring + (size_t)slot[j] * PLANE); };
                     float gx, gy, gz, hx, hy, hz;
                     fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
-                    int32_t rng = cell_rng(seed_d[0], x, y, zg);
+                    int32_t rng = cell_rng_at(pre_d[0], zg);
                     if (KIND == SK_GRAD_HESS)
                         a.hdiag[o] = cf3_encode(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rng);
                     a.grad[0][o] = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rng);
                 } else if (KIND == SK_MIXED) {
                     auto pl = [&](int j) { return (const float*)(ring + (size_t)slot[j] * PLANE); };
                     const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
-                    int32_t rng = cell_rng(seed_m[0], x, y, zg);
+                    int32_t rng = cell_rng_at(pre_m[0], zg);
                     a.hoff[o] = cf3_encode(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rng);
                 } else {   // SK_BSSN
                     const size_t cz = (size_t)slot[P] * PLANE + c0;
@@ -226,18 +233,18 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
                         auto pl = [&](int j) { return base + (size_t)slot[j] * PLANE; };
                         float gx, gy, gz, hx, hy, hz;
                         fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
-                        int32_t rd = cell_rng(seed_d[k], x, y, zg);
+                        int32_t rd = cell_rng_at(pre_d[k], zg);
                         // the Hessians are quantised exactly as the reference writes and re-reads them
                         const Cf3Quantised hq = cf3_encode_quantised(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
                         G[k] = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
                         a.grad[k][o] = G[k];
                         const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
-                        int32_t rm = cell_rng(seed_m[k], x, y, zg);
+                        int32_t rm = cell_rng_at(pre_m[k], zg);
                         const Cf3Quantised oq = cf3_encode_quantised(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
                         const Sym H{hq.value.x, oq.value.x, oq.value.y, hq.value.y, oq.value.z, hq.value.z};   // tensors.h:430-435
                         a.lap[k][o] = trace_contra(H, ginv);
                     }
-                    int32_t rc = cell_rng(seed_c, x, y, zg);
+                    int32_t rc = cell_rng_at(pre_c, zg);
                     uint32_t out[6];
                     christoffel_cell(G, a.christoffel_mode == AMR_CHRISTOFFEL_RAISED ? ginv : g, rc, out);
 #pragma unroll

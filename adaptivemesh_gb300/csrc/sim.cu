@@ -291,7 +291,7 @@ public:
             for (int k = 0; k < 6; k++) {
                 f.old_f[0] = old6[k]; f.new_f[0] = new6[k];
                 if ((st = check(launch_copy_boundaries(dims, f, d_boundaries, used, s, md, 1, ghost_stage, stream)))) return st;
-                launches++;   // gather + scatter
+                launches++;   // fill + commit
             }
             return AMR_OK;
         }

@@ -99,9 +99,9 @@ int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_f, const
  * device memory (an application that owns a fixed device-memory budget, or a time-critical loop
  * that must not block on cudaMalloc).  It has no counterpart in the reference.  Instead of an
  * allocated staging buffer it uses a fixed 8 MiB array compiled into the library (held by every
- * GPU that loads it, until exit), so it calls no allocator.  Limit: 2 * 6 * padding_domain *
- * size_domain^2 floats per slot must fit in 2^21 floats (227 slots at 16/3, 111 at 28/2, 56 at
- * 32/3); larger cases return AMR_ERR_CAPACITY.  The first call on a device looks up the array's
+ * GPU that loads it, until exit), so it calls no allocator.  Limit: 2 * 3 * size_domain^2 floats
+ * per slot must fit in 2^21 floats (1365 slots at 16/3, 445 at 28/2, 341 at 32/3); larger cases
+ * return AMR_ERR_CAPACITY.  The first call on a device looks up the array's
  * address; make that first call before any stream capture.  All calls share the array, so calls
  * that overlap on the GPU race and must be ordered by the caller; nothing in it needs clearing. */
 int amr_copy_boundaries_noalloc(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,

@@ -152,3 +152,37 @@ def digest(a) -> str:
     if not isinstance(a, np.ndarray):
         a = a.detach().cpu().numpy()
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def codec_words(n: int, seed: int) -> np.ndarray:
+    """Random compressed_float3 words (every bit pattern is a valid word)."""
+    return np.random.default_rng(seed).integers(0, 2 ** 32, n, dtype=np.uint64).astype(np.uint32)
+
+
+def substeps_for(md: int) -> list[int]:
+    """Substeps exercised per tree: the first two, the middle-plus-one and the last of a timestep
+    (timer_helper values, AMR.h:178), so every depth is active in at least one of them."""
+    s = {0, 1, (1 << md) - 1}
+    if md >= 2:
+        s.add((1 << (md - 1)) + 1)
+    return sorted(x for x in s if x < (1 << md))
+
+
+def ghost_write_mask(boundaries: np.ndarray, used: int, n: int, p: int, md: int, s: int) -> np.ndarray:
+    """Cells the ghost fill writes at substep s: the face ghost layers of every face with a
+    neighbour whose depth is active (AMR.h:710-735), as a flat mask over the padded fields."""
+    t = n + 2 * p
+    m = np.zeros((used, t, t, t), bool)          # [slot, z, y, x]
+    lo, hi, inn = slice(0, p), slice(p + n, t), slice(p, p + n)
+    faces = [(inn, inn, hi), (inn, hi, inn), (hi, inn, inn), (inn, inn, lo), (inn, lo, inn), (lo, inn, inn)]
+    for slot in range(used):
+        for f in range(6):
+            b = int(boundaries[slot * 6 + f])
+            nd = b & 0xFFFFFFFF
+            target = (nd & 0xFFFFFF) - ((1 << 24) if nd & (1 << 23) else 0)
+            cd = -1 if (nd >> 28) == 15 else nd >> 28
+            if target == -1 or cd <= 0 or (s & ((1 << (md - cd)) - 1)) != 0:
+                continue
+            zs, ys, xs = faces[f]
+            m[slot, zs, ys, xs] = True
+    return m.reshape(-1)

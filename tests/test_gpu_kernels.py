@@ -113,8 +113,8 @@ def test_codec(am, cuda, orc):
     ref = ref_lib("n28p2")
     if ref is not None:
         r = torch.zeros(n, dtype=torch.int32, device="cuda")
-        assert ref.refd_cf3_encode_seeded(torch.from_numpy(xyz).cuda().data_ptr(), torch.from_numpy(seeds).cuda().data_ptr(),
-                                          n, r.data_ptr()) == 0
+        xd, sd = torch.from_numpy(xyz).cuda(), torch.from_numpy(seeds).cuda()   # alive while the kernel runs
+        assert ref.refd_cf3_encode_seeded(xd.data_ptr(), sd.data_ptr(), n, r.data_ptr()) == 0
         assert_same(host(out), host(r), "stochastic encode vs reference device build")
 
 
@@ -130,8 +130,8 @@ def test_codec_noise_rounding(am, cuda, orc):
     if ref is None:
         pytest.skip("reference checker unavailable")
     r = torch.zeros(len(seeds), dtype=torch.int32, device="cuda")
-    assert ref.refd_cf3_encode_seeded(torch.from_numpy(xyz).cuda().data_ptr(), torch.from_numpy(seeds).cuda().data_ptr(),
-                                      len(seeds), r.data_ptr()) == 0
+    xd, sd = torch.from_numpy(xyz).cuda(), torch.from_numpy(seeds).cuda()   # alive while the kernel runs
+    assert ref.refd_cf3_encode_seeded(xd.data_ptr(), sd.data_ptr(), len(seeds), r.data_ptr()) == 0
     fused = orc.cf3_encode_seeded(xyz, seeds, orc.FTZ | orc.FUSED_NOISE)
     plain = orc.cf3_encode_seeded(xyz, seeds, orc.FTZ)
     assert np.count_nonzero(fused != plain) == len(seeds)
@@ -292,8 +292,8 @@ def test_amr_data_movement(am, cuda, orc, cfgname, tree):
         torch.cuda.synchronize()
         assert_same(host(ro), o, f"{cfgname}/{tree}/s{s} restriction vs oracle")
         if ref is not None:
-            rr = c.dev(c.f_old)
-            assert ref.refd_copy_new_to_old(rr.data_ptr(), c.dev(c.f_new).data_ptr(), c.pos.data_ptr(), c.ch.data_ptr(),
+            rr, rn = c.dev(c.f_old), c.dev(c.f_new)
+            assert ref.refd_copy_new_to_old(rr.data_ptr(), rn.data_ptr(), c.pos.data_ptr(), c.ch.data_ptr(),
                                             c.used, s, c.md) == 0
             assert_same(host(ro), host(rr), "restriction vs reference")
     # prolongation into every node, in slot order (as node_ctor runs on add_node)

@@ -1,0 +1,114 @@
+"""CPU parity against fixtures made from the reference's own host code (tests/golden/host_golden.npz,
+written by tests/golden/gen_host_golden.py): the oracle's prng, codec, Morton arithmetic, boundary
+words and inverse, and this library's host octree, which must reproduce AMR<T>'s arrays bit for bit
+(AdaptiveMesh/AMR.h:118-294).  No GPU is used."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import cases
+from conftest import GOLDEN
+import gen_host_golden as hgen
+
+
+@pytest.fixture(scope="module")
+def hg():
+    return np.load(os.path.join(GOLDEN, "host_golden.npz"))
+
+
+def _u32(a):
+    return np.asarray(a).view(np.uint32)
+
+
+def test_prng_streams(orc, hg):
+    L = orc.lib()
+    for i, seed in enumerate(hg["prng/seeds"]):
+        assert np.array_equal(orc.prng_ints(int(seed), 64), hg["prng/ints"][i]), f"generate_int, seed {seed}"
+        s = ctypes.c_int32(int(seed))
+        floats = np.array([L.orc_prng_float(ctypes.byref(s)) for _ in range(64)], np.float32)
+        assert np.array_equal(_u32(floats), _u32(hg["prng/floats"][i])), f"generate_float, seed {seed}"
+        for j, (lo, hi) in enumerate(hg["prng/ranges"]):
+            s = ctypes.c_int32(int(seed))
+            got = np.array([L.orc_prng_ranged(ctypes.byref(s), int(lo), int(hi)) for _ in range(32)], np.int32)
+            assert np.array_equal(got, hg["prng/ranged"][i, j]), f"generate_int({lo},{hi}), seed {seed}"
+
+
+def test_codec_host_build(orc, hg):
+    """The oracle with the host build's float semantics (no flush, no contraction) reproduces the
+    reference's host encoder and decoder on every regime of cases.codec_inputs."""
+    xyz, seeds = cases.codec_inputs(12_000, 4321)
+    assert np.array_equal(orc.cf3_encode_seeded(xyz, seeds, orc.HOST_FLAGS), hg["codec/seeded"])
+    assert np.array_equal(orc.cf3_encode_det(xyz, orc.HOST_FLAGS), hg["codec/det"])
+    out = np.zeros(len(seeds), np.uint32)
+    final = orc.lib().orc_cf3_encode_stream(orc.P(xyz), len(seeds), 77, orc.P(out), orc.HOST_FLAGS)
+    assert np.array_equal(out, hg["codec/stream"])
+    assert final == int(hg["codec/stream_final_seed"][0])
+    dec = orc.cf3_decode(cases.codec_words(len(seeds), 4322))
+    assert np.array_equal(_u32(dec), _u32(hg["codec/decoded"]))
+
+
+def test_morton_arithmetic(orc, hg):
+    L = orc.lib()
+    a, b = hg["morton/a"], hg["morton/b"]
+    for ov in (0, 1):
+        s = np.array([L.orc_sum_coordinates(int(x), int(y), ov) for x, y in zip(a, b)], np.uint32)
+        d = np.array([L.orc_diff_coordinates(int(x), int(y), ov) for x, y in zip(a, b)], np.uint32)
+        assert np.array_equal(s, hg[f"morton/sum{ov}"]), f"yield_sum_coordinates overflow={ov}"
+        assert np.array_equal(d, hg[f"morton/diff{ov}"]), f"yield_diff_coordinates overflow={ov}"
+    r = np.array([L.orc_reverse_bits(int(x)) for x in hg["morton/rev_in"]], np.uint32)
+    assert np.array_equal(r, hg["morton/rev"])
+
+
+@pytest.mark.parametrize("tree", ["bssn", "uneven"])
+def test_boundary_words(orc, hg, tree):
+    L = orc.lib()
+    pos = hg[f"tree/{tree}/positions"]
+    words = np.array([L.orc_boundary(int(pos[i]), int(pos[j]), int(j)) for i, j in hg[f"boundary/{tree}/pairs"]],
+                     np.uint64)
+    assert np.array_equal(words, hg[f"boundary/{tree}/words"])
+
+
+def test_inverse_within_contraction_noise(orc, hg):
+    """The oracle's inverse follows the device build's contraction; against the host build it
+    agrees to within a few ulp of the largest entry (the bound is written here: 2e-6 relative)."""
+    L = orc.lib()
+    m, ref = hg["inverse/in"], hg["inverse/out"]
+    out = np.zeros_like(m)
+    for i in range(len(m)):
+        L.orc_sym_inverse(m[i].ctypes.data, out[i].ctypes.data)
+    scale = np.abs(ref).max(axis=1, keepdims=True)
+    assert np.all(np.abs(out - ref) <= 2e-6 * scale)
+
+
+@pytest.mark.parametrize("tree", ["wave", "bssn", "uneven", "uniform2"])
+def test_octree_matches_reference(am, hg, tree):
+    o = am.Octree(80 if tree == "uniform2" else hgen.SLOTS)
+    if tree == "uniform2":
+        cases.tree_uniform(o, 2)
+    else:
+        cases.TREES[tree](o)
+    st = o.state()
+    for k in ("positions", "parent", "children", "boundaries", "lifetime"):
+        assert np.array_equal(st[k], hg[f"tree/{tree}/{k}"]), f"{tree}: {k}"
+    assert np.array_equal(np.array([st["timer"], st["max_depth"], st["first_free"], st["used_slots"]], np.uint32),
+                          hg[f"tree/{tree}/scalars"])
+    o.close()
+
+
+def test_octree_script_matches_reference(am, hg):
+    """400 random add / remove / increment_timer / find operations: the state after every one of
+    them equals the reference octree's."""
+    o = am.Octree(hgen.SLOTS)
+    digests, finds = hgen.run_script(o, hg["tree/script/ops"])
+    want = hg["tree/script/digests"]
+    bad = np.nonzero(digests != want)[0]
+    assert bad.size == 0, f"first divergent operation: {bad[0]} {tuple(hg['tree/script/ops'][bad[0]])}"
+    assert np.array_equal(finds, hg["tree/script/finds"])
+    st = o.state()
+    for k in ("positions", "parent", "children", "boundaries", "lifetime"):
+        assert np.array_equal(st[k], hg[f"tree/script/final/{k}"]), k
+    o.close()

@@ -60,8 +60,9 @@ def test_noalloc_rejects_cases_beyond_its_array(am, cuda):
     cfg = am.Config(16, 3, 100.0)
     dummy = torch.zeros(16, dtype=torch.float32, device="cuda")
     bd = torch.zeros(16, dtype=torch.int64, device="cuda")
-    # 228 slots of 16^3 with padding 3 need more than the 2^21 staging floats
-    assert lib.amr_copy_boundaries_noalloc(ctypes.byref(cfg), dummy.data_ptr(), dummy.data_ptr(), bd.data_ptr(), 228,
+    # 1366 slots of 16^3 stage 1366 * 2 * 3 * 16^2 floats, more than the array's 2^21: rejected
+    # before anything is launched (the dummy buffers are never touched)
+    assert lib.amr_copy_boundaries_noalloc(ctypes.byref(cfg), dummy.data_ptr(), dummy.data_ptr(), bd.data_ptr(), 1366,
                                            0, 3, 1, None) == am.ERR_CAPACITY
     assert lib.amr_copy_boundaries_noalloc(None, dummy.data_ptr(), dummy.data_ptr(), bd.data_ptr(), 1, 0, 0, 1,
                                            None) == am.ERR_INVALID
