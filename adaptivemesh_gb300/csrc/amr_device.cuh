@@ -51,25 +51,43 @@ __device__ __forceinline__ int32_t cell_rng(int32_t seed, uint32_t x, uint32_t y
 
 // ------------------------------------------------------------------ compressed_float3 (tensors.h:305-394)
 // word = E<<27 | s3<<26 | m3<<18 | s2<<17 | m2<<9 | s1<<8 | m1 ;  value_i = (1 - 2 s_i) m_i 2^(E-22)
-// Mantissa of one component: trunc(|clamp(v, -255, 255)| + 0.5) (tensors.h:369-372).  For every
-// value the encoder produces -- NaN and +-Inf included -- this equals min(trunc(|v| + 0.5), 255):
-// adding 2^23 with round-toward-zero leaves trunc(q) in the low mantissa bits of q + 2^23, an
-// integer min against the bits of 2^23 + 255 saturates (NaN and Inf bits compare above it), and
-// the sign is (v < 0) as for the clamped value.  Returns the raw sum bits (2^23 + m as a float).
-__device__ __forceinline__ uint32_t cf3_mantissa_bits(float v) {
-    const float q = __fadd_rn(fabsf(v), .5f);
-    return min(__float_as_uint(__fadd_rz(q, 8388608.f)), 0x4B0000FFu);
+// One component's 9-bit field, sign << 8 | mantissa, from the scaled (and noised) value v:
+// mantissa = trunc(|clamp(v, -255, 255)| + 0.5), sign = (clamped v < 0) (tensors.h:369-372).  For
+// every v -- NaN and +-Inf included -- |clamp(v)| = fminf(|v|, 255) (NaN gives 255, as clamp's
+// fminf/fmaxf do) and the sign is (v < 0), false for NaN.  q = fminf(|v|, 255) + 0.5 lies in
+// [0.5, 255.5], so adding k = 2^23 + 256*sign with round-toward-zero leaves
+// 2^23 + 256*sign + trunc(q) in the float's bits: the field is the low 9 bits.  Returns those bits
+// and k (so that bits - k is the mantissa).
+struct Cf3Field {
+    uint32_t bits;   // 0x4B000000 + field
+    float k;         // 2^23 + 256 * sign
+    float sign;      // 1.0 or 0.0
+};
+__device__ __forceinline__ Cf3Field cf3_field(float v) {
+    Cf3Field c;
+    const float q = __fadd_rn(fminf(fabsf(v), 255.f), .5f);
+    c.sign = v < 0.f ? 1.f : 0.f;
+    c.k = __fmaf_rn(c.sign, 256.f, 8388608.f);
+    c.bits = __float_as_uint(__fadd_rz(q, c.k));
+    return c;
+}
+// The largest biased exponent of three floats, as the integer maximum of their exponent fields
+// would give it: a NaN among them (exponent field 255) wins, which max.NaN reproduces by
+// returning a NaN; otherwise |x| orders as its bits do.
+__device__ __forceinline__ uint32_t max_exponent3(float x, float y, float z) {
+    float m;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(m) : "f"(fabsf(x)), "f"(fabsf(y)));
+    asm("max.NaN.f32 %0, %0, %1;" : "+f"(m) : "f"(fabsf(z)));
+    return (__float_as_uint(m) >> 23) & 255u;
 }
 struct Cf3Quantised {
     uint32_t word;
     float3 value;   // the decoded value of `word`
 };
+// word = E<<27 | s3<<26 | m3<<18 | s2<<17 | m2<<9 | s1<<8 | m1 ;  value_i = (1 - 2 s_i) m_i 2^(E-22)
 template <bool STOCHASTIC, bool WANT_VALUE>
 __device__ __forceinline__ Cf3Quantised cf3_encode_impl(float x, float y, float z, int32_t& rng) {
-    // largest biased exponent of the three: the exponent field of the largest magnitude's bits
-    const uint32_t amax = max(__float_as_uint(x) & 0x7FFFFFFFu, max(__float_as_uint(y) & 0x7FFFFFFFu,
-                                                                    __float_as_uint(z) & 0x7FFFFFFFu));
-    const uint32_t E = min(max(amax >> 23, 112u) - 112u, 31u);
+    const uint32_t E = min(max(max_exponent3(x, y, z), 112u) - 112u, 31u);
     const float scale = __uint_as_float((149u - E) << 23);          // 2^(22-E), exact
     x = __fmul_rn(x, scale);
     y = __fmul_rn(y, scale);
@@ -79,15 +97,15 @@ __device__ __forceinline__ Cf3Quantised cf3_encode_impl(float x, float y, float 
         y = __fadd_rn(y, prng_noise(rng));
         z = __fadd_rn(z, prng_noise(rng));
     }
-    const uint32_t bx = cf3_mantissa_bits(x), by = cf3_mantissa_bits(y), bz = cf3_mantissa_bits(z);
-    const uint32_t sx = x < 0.f, sy = y < 0.f, sz = z < 0.f;
+    const Cf3Field fx = cf3_field(x), fy = cf3_field(y), fz = cf3_field(z);
     Cf3Quantised r;
-    r.word = (E << 27) | (bx & 255u) | (sx << 8) | ((by & 255u) << 9) | (sy << 17) | ((bz & 255u) << 18) | (sz << 26);
-    if (WANT_VALUE) {   // (2^23 + m) - 2^23 = m exactly; times 2^(E-22); sign applied last
+    // (0x4B000000 + f) * 2^9 and * 2^18 wrap to f << 9 and f << 18: the high bits fall off
+    r.word = (E << 27) + (fx.bits & 511u) + fy.bits * 512u + fz.bits * 262144u;
+    if (WANT_VALUE) {   // (bits - k) = m exactly; times +-2^(E-22), the sign applied by the factor
         const float back = __uint_as_float((105u + E) << 23);
-        r.value = make_float3(__uint_as_float(__float_as_uint(__fmul_rn(__fsub_rn(__uint_as_float(bx), 8388608.f), back)) | (sx << 31)),
-                              __uint_as_float(__float_as_uint(__fmul_rn(__fsub_rn(__uint_as_float(by), 8388608.f), back)) | (sy << 31)),
-                              __uint_as_float(__float_as_uint(__fmul_rn(__fsub_rn(__uint_as_float(bz), 8388608.f), back)) | (sz << 31)));
+        r.value = make_float3(__fmul_rn(__fsub_rn(__uint_as_float(fx.bits), fx.k), __fmaf_rn(fx.sign, -2.f * back, back)),
+                              __fmul_rn(__fsub_rn(__uint_as_float(fy.bits), fy.k), __fmaf_rn(fy.sign, -2.f * back, back)),
+                              __fmul_rn(__fsub_rn(__uint_as_float(fz.bits), fz.k), __fmaf_rn(fz.sign, -2.f * back, back)));
     }
     return r;
 }
@@ -214,14 +232,13 @@ template <> struct FD<3> {
 };
 
 // ------------------------------------------------------------------ 10-point interpolation (AMR.h:672-699)
-// d points at the nearest source cell; strides 1, T, T^2; r = offset from it in cells.
-template <int T>
-__device__ __forceinline__ float interp10(const float* __restrict__ d, float rx, float ry, float rz) {
-    constexpr int T2 = T * T;
+// d points at the nearest source cell; strides 1, sy, sz; r = offset from it in cells.
+template <class S>
+__device__ __forceinline__ float interp10_strided(const float* __restrict__ d, S sy, S sz, float rx, float ry, float rz) {
     const float f = d[0];
-    float fx = d[1], fy = d[T], fz = d[T2];
-    float fxx = d[-1], fyy = d[-T], fzz = d[-T2];
-    float fxy = d[T + 1], fxz = d[T2 + 1], fyz = d[T2 + T];
+    float fx = d[1], fy = d[sy], fz = d[sz];
+    float fxx = d[-1], fyy = d[-sy], fzz = d[-sz];
+    float fxy = d[sy + 1], fxz = d[sz + 1], fyz = d[sz + sy];
     fxy = __fadd_rn(fxy, __fsub_rn(__fsub_rn(f, fx), fy));
     fxz = __fadd_rn(fxz, __fsub_rn(__fsub_rn(f, fx), fz));
     fyz = __fadd_rn(fyz, __fsub_rn(__fsub_rn(f, fy), fz));
@@ -238,6 +255,11 @@ __device__ __forceinline__ float interp10(const float* __restrict__ d, float rx,
     acc = __fmaf_rn(__fmul_rn(fxz, rx), rz, acc);
     acc = __fmaf_rn(__fmul_rn(fyz, ry), rz, acc);
     return acc;
+}
+// The same on a padded domain (strides T, T^2).
+template <int T>
+__device__ __forceinline__ float interp10(const float* __restrict__ d, float rx, float ry, float rz) {
+    return interp10_strided(d, T, T * T, rx, ry, rz);
 }
 
 }  // namespace amr

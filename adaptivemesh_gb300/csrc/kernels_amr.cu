@@ -23,7 +23,7 @@ inline uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kBlock - 1) / kB
 // child's 2x2x2 cells and the rest is copied.
 constexpr uint32_t kSlabs = 4;
 template <int N, int P>
-__global__ void __launch_bounds__(kBlock) k_copy_new_to_old(FieldSet f, const uint32_t* __restrict__ positions,
+__global__ void __launch_bounds__(kBlock) k_copy_new_to_old(const __grid_constant__ FieldSet f, const uint32_t* __restrict__ positions,
                                                         const int32_t* __restrict__ children,
                                                         const uint32_t* __restrict__ items, uint32_t substep,
                                                         uint32_t max_depth) {
@@ -163,56 +163,183 @@ __device__ __forceinline__ GhostJob ghost_job(uint64_t bd, uint32_t substep, uin
     return j;
 }
 
-// Phase 1: interpolate every ghost value of every component from the fields; write it, or stage
-// it if it lies in an innermost lower layer (per component: old values, then new values).
+// Source index (nearest cell) and offset from it along one axis for written coordinate w
+// (AMR.h:737-753).  Each step is monotone in w, so over a face the extreme indices come from the
+// extreme coordinates.
 template <int N, int P>
-__global__ void __launch_bounds__(256) k_ghost_fill(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
-                                                   uint32_t substep, uint32_t max_depth, int copy_only_new,
-                                                   float* __restrict__ stage) {
-    using G = GhostShape<N, P>;
-    constexpr uint32_t T = G::T;
+__device__ __forceinline__ void ghost_source(uint32_t w, float rel_scale, float relp, bool root, uint32_t& ri, float& r) {
+    constexpr uint32_t T = N + 2 * P;
     constexpr float inv_n = 1.f / N;
-    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (uint64_t)used * G::SLOT) return;
-    uint32_t slot, face, u, v, w[3];
-    ghost_decode<N, P>(gid, slot, face, u, v, w);
-    const uint64_t bd = bds[slot * 6u + face];
+    float rp = __fmaf_rn(__fadd_rn(__fsub_rn((float)w, (float)P), .5f), inv_n, -.5f);
+    rp = __fmaf_rn(rp, rel_scale, relp);
+    rp = __fsub_rn(__fmaf_rn(__fadd_rn(rp, .5f), (float)N, (float)P), .5f);
+    ri = root ? min(__float2uint_rz(__fadd_rn(fmaxf(rp, 0.f), .5f)), T - 2u)
+              : min(__float2uint_rz(__fadd_rn(fmaxf(rp, (float)P), .5f)), T - P - 2u);
+    r = __fsub_rn(rp, (float)ri);
+}
+// n / d for n * d < 2^32 with m = ceil(2^32 / d), d >= 2
+struct FastDiv {
+    uint32_t d, m;
+    __device__ void init(uint32_t dv) { d = dv; m = (uint32_t)(0xFFFFFFFFu / dv) + 1u; }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const { return __umulhi(n, m); }
+};
+// Largest source box of one face and component: P+2 cells along the normal, N+2 along the others.
+template <int N, int P>
+struct GhostBox {
+    static constexpr uint32_t MAX = (P + 2) * (N + 2) * (N + 2);
+    static constexpr size_t SMEM = 4u * MAX * sizeof(float);   // two buffers of (old, new)
+};
+
+// Phase 1, one CTA per (slot, face).  The source cells that the face's ghost cells interpolate
+// from lie in a box one cell wider than the range of their nearest source indices.  Per
+// component, the CTA copies the old and new values of that box into shared memory (double
+// buffered, so the next component loads while this one is interpolated), then computes every
+// ghost value of the face from there and writes it in place, or to the staging buffer if it lies
+// in an innermost lower layer.  The box never holds a cell that phase 1 writes (see above), and the
+// arithmetic is the reference's per cell, so the values equal a fill of the pre-fill state.  A
+// box that would leave the domain's cube (only a root source can come near) or exceed the
+// shared-memory buffer is read from global memory instead.
+template <int N, int P>
+__global__ void __launch_bounds__(kBlock) k_ghost_face(const __grid_constant__ FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
+                                                      uint32_t substep, uint32_t max_depth, int copy_only_new,
+                                                      float* __restrict__ stage) {
+    using G = GhostShape<N, P>;
+    constexpr uint32_t T = G::T, BOX = GhostBox<N, P>::MAX;
+    extern __shared__ float sbox[];
+    __shared__ uint32_t s_off[3][T];   // per axis and written coordinate: box-relative source index
+    __shared__ float s_r[3][T];        // and offset from it
+    const uint32_t slot = blockIdx.x / 6u, face = blockIdx.x - slot * 6u;
+    const uint64_t bd = bds[(size_t)slot * 6u + face];
     const GhostJob j = ghost_job(bd, substep, max_depth);
-    if (!j.active) return;
+    if (!j.active) return;   // uniform in the CTA
     const float rel_scale = __uint_as_float((127u - j.dd) << 23);         // 1 / 2^depth_diff
     const float3 rel_pos = cf3_decode((uint32_t)(bd >> 32));
     const float relp[3] = {rel_pos.x, rel_pos.y, rel_pos.z};
-    uint32_t ri[3];
-    float r[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {                                          // AMR.h:737-753
-        float rp = __fmaf_rn(__fadd_rn(__fsub_rn((float)w[a], (float)P), .5f), inv_n, -.5f);
-        rp = __fmaf_rn(rp, rel_scale, relp[a]);
-        rp = __fsub_rn(__fmaf_rn(__fadd_rn(rp, .5f), (float)N, (float)P), .5f);
-        const uint32_t idx = j.target == 0 ? min(__float2uint_rz(__fadd_rn(fmaxf(rp, 0.f), .5f)), T - 2u)
-                                           : min(__float2uint_rz(__fadd_rn(fmaxf(rp, (float)P), .5f)), T - P - 2u);
-        ri[a] = idx;
-        r[a] = __fsub_rn(rp, (float)idx);
-    }
-    const uint64_t rin = (uint64_t)j.target * G::CELLS + ri[0] + (ri[1] + ri[2] * T) * T;
+    const bool root = j.target == 0;
     const float tm = (float)((substep >> (max_depth - (uint32_t)j.cd)) & ((1u << j.dd) - 1u));   // AMR.h:634-639
     const float t0 = __fmul_rn(tm, rel_scale), t1 = __fmul_rn(__fadd_rn(tm, 1.f), rel_scale);
-    const bool staged = face >= 3u && w[face - 3u] == P - 1u;
+    const uint32_t normal = face % 3u;
     const uint64_t n_staged = (uint64_t)used * G::STAGED;
-    const uint64_t out = staged ? ((uint64_t)slot * 3u + (face - 3u)) * (N * N) + u + v * N
-                                : (uint64_t)slot * G::CELLS + w[0] + (w[1] + w[2] * T) * T;
+    const bool staged_face = face >= 3u;
+
+    // written coordinate range and source box per axis
+    uint32_t wlo[3], whi[3], ext[3];
+    int32_t lo[3];
+    bool boxed = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        wlo[a] = a == (int)normal ? (face < 3u ? P + N : 0u) : P;
+        whi[a] = a == (int)normal ? wlo[a] + P - 1u : P + N - 1u;
+        uint32_t r0, r1;
+        float unused;
+        ghost_source<N, P>(wlo[a], rel_scale, relp[a], root, r0, unused);
+        ghost_source<N, P>(whi[a], rel_scale, relp[a], root, r1, unused);
+        lo[a] = (int32_t)r0 - 1;
+        ext[a] = r1 - r0 + 3u;
+        boxed &= lo[a] >= 0;
+    }
+    boxed &= ext[0] * ext[1] * ext[2] <= BOX;
+
+    if (!boxed) {   // global-memory path, one ghost cell per thread and pass
+        for (uint32_t g = threadIdx.x; g < G::FACE; g += kBlock) {
+            uint32_t sl, fc, u, v, w[3];
+            ghost_decode<N, P>((uint64_t)slot * G::SLOT + (uint64_t)face * G::FACE + g, sl, fc, u, v, w);
+            uint32_t ri[3];
+            float r[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) ghost_source<N, P>(w[a], rel_scale, relp[a], root, ri[a], r[a]);
+            const uint64_t rin = (uint64_t)j.target * G::CELLS + ri[0] + (ri[1] + ri[2] * T) * T;
+            const bool staged = staged_face && (normal == 0u ? w[0] : normal == 1u ? w[1] : w[2]) == P - 1u;
+            const uint64_t out = staged ? ((uint64_t)slot * 3u + (face - 3u)) * (N * N) + u + v * N
+                                        : (uint64_t)slot * G::CELLS + w[0] + (w[1] + w[2] * T) * T;
+            for (int k = 0; k < f.ncomp; k++) {
+                const float od = interp10<T>(f.old_f[k] + rin, r[0], r[1], r[2]);
+                const float nw = interp10<T>(f.new_f[k] + rin, r[0], r[1], r[2]);
+                float* dst_old = staged ? stage + (uint64_t)k * 2u * n_staged : f.old_f[k];
+                float* dst_new = staged ? stage + ((uint64_t)k * 2u + 1u) * n_staged : f.new_f[k];
+                if (!copy_only_new) dst_old[out] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
+                dst_new[out] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
+            }
+        }
+        return;
+    }
+
+    for (uint32_t i = threadIdx.x; i < 3u * T; i += kBlock) {
+        const uint32_t a = i / T, w = i - a * T;   // selects, not indexing: the arrays stay in registers
+        const uint32_t wl = a == 0u ? wlo[0] : a == 1u ? wlo[1] : wlo[2];
+        const uint32_t wh = a == 0u ? whi[0] : a == 1u ? whi[1] : whi[2];
+        if (w < wl || w > wh) continue;
+        uint32_t ri;
+        float r;
+        ghost_source<N, P>(w, rel_scale, a == 0u ? relp[0] : a == 1u ? relp[1] : relp[2], root, ri, r);
+        s_off[a][w] = ri - (uint32_t)(a == 0u ? lo[0] : a == 1u ? lo[1] : lo[2]);
+        s_r[a][w] = r;
+    }
+    const uint32_t sy = ext[0], sz = ext[0] * ext[1], box = sz * ext[2];
+    const size_t src0 = (size_t)j.target * G::CELLS + (uint32_t)lo[0] + ((uint32_t)lo[1] + (uint32_t)lo[2] * T) * T;
+    // Box element i = tid + n*kBlock as (bx, by, bz) and its cell offset gi from src0; stepping by
+    // kBlock adds (A, B, C) with one carry per axis at most.
+    FastDiv div_x, div_xy;
+    div_x.init(sy);
+    div_xy.init(sz);
+    const uint32_t bz0 = div_xy.div(threadIdx.x), by0 = div_x.div(threadIdx.x - bz0 * sz), bx0 = threadIdx.x - bz0 * sz - by0 * sy;
+    const uint32_t C = div_xy.div(kBlock), B = div_x.div(kBlock - C * sz), A = kBlock - C * sz - B * sy;
+
+    // per ghost cell of this thread: box offset of its nearest source cell, offsets, destination
+    constexpr uint32_t CPT = (G::FACE + kBlock - 1) / kBlock;
+    uint32_t c_o[CPT], c_dst[CPT];
+    float c_rx[CPT], c_ry[CPT], c_rz[CPT];
+    const uint64_t stage_base = ((uint64_t)slot * 3u + (face - 3u)) * (N * N);   // used for lower faces only
+    const uint64_t slot_base = (uint64_t)slot * G::CELLS;
+
     for (int k = 0; k < f.ncomp; k++) {
-        const float od = interp10<T>(f.old_f[k] + rin, r[0], r[1], r[2]);
-        const float nw = interp10<T>(f.new_f[k] + rin, r[0], r[1], r[2]);
-        float* dst_old = staged ? stage + (uint64_t)k * 2u * n_staged : f.old_f[k];
-        float* dst_new = staged ? stage + ((uint64_t)k * 2u + 1u) * n_staged : f.new_f[k];
-        if (!copy_only_new) dst_old[out] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
-        dst_new[out] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
+        float* buf = sbox + (k & 1) * 2u * BOX;
+        const float* __restrict__ go = f.old_f[k] + src0;
+        const float* __restrict__ gn = f.new_f[k] + src0;
+        uint32_t bx = bx0, by = by0, bz = bz0;
+        for (uint32_t i = threadIdx.x; i < box; i += kBlock) {
+            const uint32_t gi = bx + (by + bz * T) * T;
+            buf[i] = __ldg(go + gi);
+            buf[BOX + i] = __ldg(gn + gi);
+            bx += A; by += B; bz += C;
+            if (bx >= sy) { bx -= sy; by++; }
+            if (by >= ext[1]) { by -= ext[1]; bz++; }
+        }
+        __syncthreads();   // this buffer is complete; the other one is free for the next component
+        if (k == 0) {
+#pragma unroll
+            for (uint32_t c = 0; c < CPT; c++) {
+                const uint32_t g = threadIdx.x + c * kBlock;
+                if (g >= G::FACE) break;
+                uint32_t layer, u, v, w[3];
+                if (normal == 0u) { layer = g % P; u = (g / P) % N; v = g / (P * N); }
+                else { u = g % N; v = (g / N) % N; layer = g / (N * N); }
+                ghost_cell<N, P>(face, layer, u, v, w);
+                c_o[c] = s_off[0][w[0]] + s_off[1][w[1]] * sy + s_off[2][w[2]] * sz;
+                c_rx[c] = s_r[0][w[0]]; c_ry[c] = s_r[1][w[1]]; c_rz[c] = s_r[2][w[2]];
+                // destination: bit 31 marks a staged cell, the rest is its offset from the base
+                c_dst[c] = staged_face && layer == P - 1u ? 0x80000000u | (u + v * N) : w[0] + (w[1] + w[2] * T) * T;
+            }
+        }
+        float* const stage_old = stage + (uint64_t)k * 2u * n_staged + stage_base;
+        float* const stage_new = stage + ((uint64_t)k * 2u + 1u) * n_staged + stage_base;
+        float* const field_old = f.old_f[k] + slot_base;
+        float* const field_new = f.new_f[k] + slot_base;
+#pragma unroll
+        for (uint32_t c = 0; c < CPT; c++) {
+            if (threadIdx.x + c * kBlock >= G::FACE) break;
+            const float od = interp10_strided(buf + c_o[c], (int)sy, (int)sz, c_rx[c], c_ry[c], c_rz[c]);
+            const float nw = interp10_strided(buf + BOX + c_o[c], (int)sy, (int)sz, c_rx[c], c_ry[c], c_rz[c]);
+            const bool staged = (c_dst[c] & 0x80000000u) != 0u;
+            const uint32_t off = c_dst[c] & 0x7FFFFFFFu;
+            if (!copy_only_new) (staged ? stage_old : field_old)[off] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
+            (staged ? stage_new : field_new)[off] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
+        }
     }
 }
 // Phase 2: write the staged innermost lower layers into the fields.
 template <int N, int P>
-__global__ void __launch_bounds__(256) k_ghost_commit(FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
+__global__ void __launch_bounds__(256) k_ghost_commit(const __grid_constant__ FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
                                                      uint32_t substep, uint32_t max_depth, int copy_only_new,
                                                      const float* __restrict__ stage) {
     using G = GhostShape<N, P>;
@@ -258,12 +385,18 @@ size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp) {
 cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* boundaries, uint32_t used,
                                    uint32_t substep, uint32_t max_depth, int copy_only_new, float* scratch,
                                    cudaStream_t st) {
-    const uint64_t total = (uint64_t)used * 6u * d.p * d.n * d.n;
-    if (total == 0 || f.ncomp == 0) return cudaSuccess;
 #define AMR_GHOST(N, P)                                                                                     \
     if (d.n == N && d.p == P) {                                                                             \
-        k_ghost_fill<N, P><<<blocks_for(total), kBlock, 0, st>>>(f, boundaries, used, substep, max_depth,    \
-                                                                 copy_only_new, scratch);                  \
+        static bool configured = false;                                                                     \
+        if (!configured) {                                                                                  \
+            cudaError_t e = cudaFuncSetAttribute(k_ghost_face<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                                 (int)GhostBox<N, P>::SMEM);                                \
+            if (e != cudaSuccess) return e;                                                                 \
+            configured = true;                                                                              \
+        }                                                                                                   \
+        if (used == 0 || f.ncomp == 0) return cudaSuccess;                                                  \
+        k_ghost_face<N, P><<<used * 6u, kBlock, GhostBox<N, P>::SMEM, st>>>(f, boundaries, used, substep,     \
+                                                                          max_depth, copy_only_new, scratch); \
         cudaError_t e = cudaGetLastError();                                                                 \
         if (e != cudaSuccess) return e;                                                                     \
         k_ghost_commit<N, P><<<blocks_for((uint64_t)used * 3u * N * N), kBlock, 0, st>>>(                   \

@@ -70,6 +70,9 @@ public:
                 e = launch_stencil(cfg, kind, none, 0, stream);
                 if (e != cudaSuccess) break;
             }
+            FieldSet nofields;
+            std::memset(&nofields, 0, sizeof(nofields));
+            if (e == cudaSuccess) e = launch_copy_boundaries(dims, nofields, nullptr, 0, 0, 0, 1, nullptr, stream);
         }
         return cuda_status(e);
     }
