@@ -66,7 +66,7 @@ struct Cf3Field {
 __device__ __forceinline__ Cf3Field cf3_field(float v) {
     Cf3Field c;
     const float q = __fadd_rn(fminf(fabsf(v), 255.f), .5f);
-    c.sign = v < 0.f ? 1.f : 0.f;
+    asm("set.lt.f32.f32 %0, %1, 0f00000000;" : "=f"(c.sign) : "f"(v));   // 1.0 if v < 0 (false for NaN)
     c.k = __fmaf_rn(c.sign, 256.f, 8388608.f);
     c.bits = __float_as_uint(__fadd_rz(q, c.k));
     return c;
@@ -89,13 +89,19 @@ template <bool STOCHASTIC, bool WANT_VALUE>
 __device__ __forceinline__ Cf3Quantised cf3_encode_impl(float x, float y, float z, int32_t& rng) {
     const uint32_t E = min(max(max_exponent3(x, y, z), 112u) - 112u, 31u);
     const float scale = __uint_as_float((149u - E) << 23);          // 2^(22-E), exact
-    x = __fmul_rn(x, scale);
-    y = __fmul_rn(y, scale);
-    z = __fmul_rn(z, scale);
-    if (STOCHASTIC) {   // the noise product is rounded before it is added (not fused)
-        x = __fadd_rn(x, prng_noise(rng));
-        y = __fadd_rn(y, prng_noise(rng));
-        z = __fadd_rn(z, prng_noise(rng));
+    if (STOCHASTIC) {
+        // The noise product is rounded before it is added (not fused).  x * scale is exact (a
+        // power-of-two scaling), so one fused multiply-add gives the reference's rounded sum
+        // x * scale + noise, except where x * scale is subnormal: flushed first, it leaves the
+        // sum +0, while fused it can leave -0 (when the noise is 0); the field below reads |v| and
+        // (v < 0) only, the same for both zeros.
+        x = __fmaf_rn(x, scale, prng_noise(rng));
+        y = __fmaf_rn(y, scale, prng_noise(rng));
+        z = __fmaf_rn(z, scale, prng_noise(rng));
+    } else {
+        x = __fmul_rn(x, scale);
+        y = __fmul_rn(y, scale);
+        z = __fmul_rn(z, scale);
     }
     const Cf3Field fx = cf3_field(x), fy = cf3_field(y), fz = cf3_field(z);
     Cf3Quantised r;

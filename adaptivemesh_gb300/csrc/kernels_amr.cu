@@ -183,24 +183,34 @@ struct FastDiv {
     __device__ void init(uint32_t dv) { d = dv; m = (uint32_t)(0xFFFFFFFFu / dv) + 1u; }
     __device__ __forceinline__ uint32_t div(uint32_t n) const { return __umulhi(n, m); }
 };
+// 4-byte asynchronous global -> shared copies (completion tracked per thread by commit groups)
+__device__ __forceinline__ void cp_async4(float* smem_dst, const float* gsrc) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }
 // Largest source box of one face and component: P+2 cells along the normal, N+2 along the others.
 template <int N, int P>
 struct GhostBox {
     static constexpr uint32_t MAX = (P + 2) * (N + 2) * (N + 2);
     static constexpr size_t SMEM = 4u * MAX * sizeof(float);   // two buffers of (old, new)
+    // resident CTAs per SM the register budget is set for: more ghost cells per thread at larger N
+    static constexpr int MIN_CTAS = N <= 16 ? 4 : 2;
 };
 
 // Phase 1, one CTA per (slot, face).  The source cells that the face's ghost cells interpolate
 // from lie in a box one cell wider than the range of their nearest source indices.  Per
 // component, the CTA copies the old and new values of that box into shared memory (double
-// buffered, so the next component loads while this one is interpolated), then computes every
+// buffered, asynchronous copies: the next component loads while this one is interpolated), then computes every
 // ghost value of the face from there and writes it in place, or to the staging buffer if it lies
 // in an innermost lower layer.  The box never holds a cell that phase 1 writes (see above), and the
 // arithmetic is the reference's per cell, so the values equal a fill of the pre-fill state.  A
 // box that would leave the domain's cube (only a root source can come near) or exceed the
 // shared-memory buffer is read from global memory instead.
 template <int N, int P>
-__global__ void __launch_bounds__(kBlock) k_ghost_face(const __grid_constant__ FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
+__global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face(const __grid_constant__ FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
                                                       uint32_t substep, uint32_t max_depth, int copy_only_new,
                                                       float* __restrict__ stage) {
     using G = GhostShape<N, P>;
@@ -292,20 +302,28 @@ __global__ void __launch_bounds__(kBlock) k_ghost_face(const __grid_constant__ F
     const uint64_t stage_base = ((uint64_t)slot * 3u + (face - 3u)) * (N * N);   // used for lower faces only
     const uint64_t slot_base = (uint64_t)slot * G::CELLS;
 
-    for (int k = 0; k < f.ncomp; k++) {
+    // Component k's box goes to buffer k & 1 by asynchronous copies, issued one component ahead.
+    auto issue = [&](int k) {
         float* buf = sbox + (k & 1) * 2u * BOX;
-        const float* __restrict__ go = f.old_f[k] + src0;
-        const float* __restrict__ gn = f.new_f[k] + src0;
+        const float* go = f.old_f[k] + src0;
+        const float* gn = f.new_f[k] + src0;
         uint32_t bx = bx0, by = by0, bz = bz0;
         for (uint32_t i = threadIdx.x; i < box; i += kBlock) {
             const uint32_t gi = bx + (by + bz * T) * T;
-            buf[i] = __ldg(go + gi);
-            buf[BOX + i] = __ldg(gn + gi);
+            cp_async4(buf + i, go + gi);
+            cp_async4(buf + BOX + i, gn + gi);
             bx += A; by += B; bz += C;
             if (bx >= sy) { bx -= sy; by++; }
             if (by >= ext[1]) { by -= ext[1]; bz++; }
         }
-        __syncthreads();   // this buffer is complete; the other one is free for the next component
+        cp_async_commit();
+    };
+    issue(0);
+    for (int k = 0; k < f.ncomp; k++) {
+        const float* buf = sbox + (k & 1) * 2u * BOX;
+        if (k + 1 < f.ncomp) { issue(k + 1); cp_async_wait<1>(); }
+        else cp_async_wait<0>();
+        __syncthreads();   // component k's box is complete in every thread's view
         if (k == 0) {
 #pragma unroll
             for (uint32_t c = 0; c < CPT; c++) {
@@ -335,6 +353,7 @@ __global__ void __launch_bounds__(kBlock) k_ghost_face(const __grid_constant__ F
             if (!copy_only_new) (staged ? stage_old : field_old)[off] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
             (staged ? stage_new : field_new)[off] = __fmaf_rn(od, __fsub_rn(1.f, t1), __fmul_rn(nw, t1));
         }
+        __syncthreads();   // everyone is done with buffer k & 1 before component k + 2 is copied into it
     }
 }
 // Phase 2: write the staged innermost lower layers into the fields.

@@ -27,11 +27,16 @@ template <int N, int P, int KIND>
 struct StencilShape {
     static constexpr int T = N + 2 * P;
     static constexpr int NC = KIND == SK_BSSN ? 6 : 1;
-    static constexpr int R = 2 * P + 3;                          // ring slots: 2P+1 in use, 2 in flight
+    // ring slots: 2P+1 in use and 2 in flight; the fused kind keeps one in flight so that two
+    // CTAs (with their generator and gradient tables) fit in one SM's shared memory
+    static constexpr int R = KIND == SK_BSSN ? 2 * P + 2 : 2 * P + 3;
     static constexpr uint32_t PLANE = (uint32_t)(T * T);         // floats per plane
     static constexpr uint32_t PLANE_BYTES = PLANE * 4u;
     static constexpr size_t RING_BYTES = (size_t)NC * R * PLANE_BYTES;
-    static constexpr size_t SMEM = RING_BYTES + (size_t)R * 8u;
+    static constexpr size_t BAR_BYTES = (size_t)R * 8u;
+    // SK_BSSN: per thread, the 13 generator prefixes (d0, m0, d1, m1, ..., c) and the six gradient words
+    static constexpr size_t TABLE_BYTES = KIND == SK_BSSN ? (size_t)(13 + 6) * N * N * 4u : 0u;
+    static constexpr size_t SMEM = RING_BYTES + BAR_BYTES + TABLE_BYTES;
     static_assert(PLANE_BYTES % 16u == 0u, "bulk copies move whole planes of 16-byte multiples");
 };
 
@@ -131,13 +136,15 @@ __device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M
 
 // ---------------------------------------------------------------- the streaming kernel
 template <int N, int P, int KIND>
-__global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
+__global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const __grid_constant__ StencilArgs a) {
     using S = StencilShape<N, P, KIND>;
     constexpr int T = S::T, NC = S::NC, R = S::R;
-    constexpr uint32_t PLANE = S::PLANE;
+    constexpr uint32_t PLANE = S::PLANE, NN = N * N;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* ring = reinterpret_cast<float*>(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S::RING_BYTES);
+    int32_t* s_pre = reinterpret_cast<int32_t*>(smem_raw + S::RING_BYTES + S::BAR_BYTES);   // [13][NN]
+    uint32_t* s_grad = reinterpret_cast<uint32_t*>(s_pre + 13 * NN);                       // [6][NN]
     __shared__ int s_abort;
 
     const uint32_t tid = threadIdx.x;
@@ -169,6 +176,11 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
 #pragma unroll
         for (int k = 0; k < NC; k++) { pre_d[k] = cell_rng_prefix(seed_d[k], x, y); pre_m[k] = cell_rng_prefix(seed_m[k], x, y); }
         pre_c = cell_rng_prefix(seed_c, x, y);
+        if (KIND == SK_BSSN) {   // the fused kind's component loop is not unrolled: it reads them here
+#pragma unroll
+            for (int k = 0; k < NC; k++) { s_pre[(2 * k) * NN + tid] = pre_d[k]; s_pre[(2 * k + 1) * NN + tid] = pre_m[k]; }
+            s_pre[12 * NN + tid] = pre_c;
+        }
     }
 
     uint32_t seq0 = 0;   // sequence number of plane 0 of the current domain (ring slot = seq % R)
@@ -226,25 +238,30 @@ __global__ void __launch_bounds__(N * N, 1) k_stencil(const StencilArgs a) {
                     const Sym g{ring[0 * R * PLANE + cz], ring[1 * (size_t)R * PLANE + cz], ring[2 * (size_t)R * PLANE + cz],
                                 ring[3 * (size_t)R * PLANE + cz], ring[4 * (size_t)R * PLANE + cz], ring[5 * (size_t)R * PLANE + cz]};
                     const Sym ginv = sym_inverse(g);
-                    uint32_t G[6];
-#pragma unroll
+                    // two components per pass: six unrolled copies of the body overflow the
+                    // instruction cache, a rolled loop spends instructions on addressing
+#pragma unroll 2
                     for (int k = 0; k < 6; k++) {
                         const float* base = ring + (size_t)k * R * PLANE;
                         auto pl = [&](int j) { return base + (size_t)slot[j] * PLANE; };
                         float gx, gy, gz, hx, hy, hz;
                         fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
-                        int32_t rd = cell_rng_at(pre_d[k], zg);
+                        int32_t rd = cell_rng_at(s_pre[(2 * k) * NN + tid], zg);
                         // the Hessians are quantised exactly as the reference writes and re-reads them
                         const Cf3Quantised hq = cf3_encode_quantised(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
-                        G[k] = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
-                        a.grad[k][o] = G[k];
+                        const uint32_t gk = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
+                        a.grad[k][o] = gk;
+                        s_grad[k * NN + tid] = gk;
                         const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
-                        int32_t rm = cell_rng_at(pre_m[k], zg);
+                        int32_t rm = cell_rng_at(s_pre[(2 * k + 1) * NN + tid], zg);
                         const Cf3Quantised oq = cf3_encode_quantised(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
                         const Sym H{hq.value.x, oq.value.x, oq.value.y, hq.value.y, oq.value.z, hq.value.z};   // tensors.h:430-435
                         a.lap[k][o] = trace_contra(H, ginv);
                     }
-                    int32_t rc = cell_rng_at(pre_c, zg);
+                    uint32_t G[6];
+#pragma unroll
+                    for (int k = 0; k < 6; k++) G[k] = s_grad[k * NN + tid];
+                    int32_t rc = cell_rng_at(s_pre[12 * NN + tid], zg);
                     uint32_t out[6];
                     christoffel_cell(G, a.christoffel_mode == AMR_CHRISTOFFEL_RAISED ? ginv : g, rc, out);
 #pragma unroll
