@@ -185,7 +185,7 @@ def reference_arm(args) -> None:
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 512 * N ** 3 / v * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "global_batch": 512, "seq_len": N ** 3, "parallelism": "replicas"},
+            "config": {"workload": WORKLOAD, "leaf_domains": 512, "zones_per_domain": N ** 3, "parallelism": "replicas"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
                              "sample": vals[0]["sample"]},
@@ -320,16 +320,17 @@ def main() -> None:
                 "frac": achieved / pk["hbm_gbs"] if achieved else None, "traffic": None,
                 "kernel": "k_stencil<16,3,SK_BSSN> (fused BSSN derivatives)", "peak_source": pk["source"],
                 "avg_launch_ms": k_ms / k_n if k_n else None, "launches_timed": k_n}
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            roofline["traffic"] = json.load(f).get("bssn_fused_bytes_per_launch")
-    except Exception:
+    try:   # DRAM bytes per domain from an ncu capture of the same kernel and workload, scaled per launch
+        with open(os.path.join(ROOT, "profiles", "k_stencil_bssn_16p3.traffic.json")) as f:
+            per_domain = json.load(f)["dram_bytes_per_domain"]
+        roofline["traffic"] = per_domain * per_step / (2 << md)
+    except (OSError, KeyError, ValueError):
         pass
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "global_batch": 512 * world, "seq_len": N ** 3,
+            "config": {"workload": WORKLOAD, "leaf_domains": 512 * world, "zones_per_domain": N ** 3,
                        "parallelism": "replicas" if world > 1 else "single", "mode": args.mode,
                        "l2": "state 299 MB > L2 129 MB, no flush"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
