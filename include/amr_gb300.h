@@ -107,6 +107,28 @@ int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_f, const
 int amr_copy_boundaries_noalloc(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,
                                 uint32_t used_slots, uint32_t substep, uint32_t max_depth, int copy_only_new,
                                 void* stream);
+/* ---- sharding by domain (no counterpart in the reference, which runs on one GPU) ----
+ * Ranks own contiguous ranges of the live slots in the preorder (Morton) order of their positions
+ * (octree_abs_pos, AMR.h:22-55), balanced by count; owner[s] = rank, or -1 for a free slot
+ * (positions[s] == 0xFFFFFFFF).  Host only. */
+int amr_partition_morton(const uint32_t* positions, uint32_t used_slots, uint32_t ranks, int32_t* owner);
+/* The source boxes that `rank` must receive before the ghost fill of `substep`
+ * (amr_copy_boundaries; AMR.h:701-762): for every active face of a slot it owns whose source slot
+ * another rank owns, the cells that the fill's interpolation reads, computed with the device's
+ * arithmetic.  Each box is 8 uint32: {source slot, source rank, lo x, lo y, lo z, extent x, extent y,
+ * extent z} in padded-domain cells; duplicates are merged.  Writes at most `capacity` boxes and sets
+ * *n_boxes to the number needed (AMR_ERR_CAPACITY if larger than capacity).  The sender of a box
+ * calls this for each receiving rank.  Host only. */
+int amr_ghost_exchange_plan(const amr_config* cfg, const uint64_t* boundaries, const int32_t* owner,
+                            uint32_t used_slots, uint32_t substep, uint32_t max_depth, uint32_t rank,
+                            uint32_t* boxes, uint32_t capacity, uint32_t* n_boxes);
+/* Copy the boxes of one padded field (used_slots domains) into `out` (box b, x fastest, at float
+ * offset offsets[b]), or back from `in`.  boxes / offsets are device arrays; a record outside the
+ * slot range or its cube is skipped. */
+int amr_pack_boxes(const amr_config* cfg, const float* field, uint32_t used_slots, const uint32_t* boxes,
+                   const uint64_t* offsets, uint32_t n_boxes, float* out, void* stream);
+int amr_unpack_boxes(const amr_config* cfg, float* field, uint32_t used_slots, const uint32_t* boxes,
+                     const uint64_t* offsets, uint32_t n_boxes, const float* in, void* stream);
 /* old <- new for active domains; cells covered by a child <- mean of the child's 2x2x2 cells.
  * Replaces copy_new_to_old(), AMR.h:998-1018. */
 int amr_copy_new_to_old(const amr_config* cfg, float* old_f, const float* new_f, const uint32_t* positions,

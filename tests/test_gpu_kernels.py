@@ -354,3 +354,41 @@ def test_wave_update_and_criterion(am, cuda, orc, cfgname, tree):
             r = host(rc)
             assert np.array_equal(np.isnan(g), np.isnan(r))
             assert_same(g[m], r[m], "criterion vs reference")
+
+
+# ----------------------------------------------------------------------------- sharding
+@pytest.mark.parametrize("cfgname,tree", [("n16p3", "bssn"), ("n28p2", "uneven"), ("n32p3", "uneven")])
+def test_pack_unpack_boxes(am, cuda, cfgname, tree):
+    """amr_pack_boxes / amr_unpack_boxes move exactly the plan's boxes (against host slicing)."""
+    import torch
+    from adaptivemesh_gb300 import sharding
+    c = Case(am, cfgname, tree)
+    owner = sharding.partition_morton(c.st["positions"], c.used, 3)
+    boxes = np.concatenate([sharding.exchange_plan(c.cfg, c.st["boundaries"], owner, c.used, s, c.md, r)
+                            for s in substeps_for(c.md) for r in range(3)])
+    assert len(boxes) > 0
+    offsets = sharding.box_offsets(boxes)
+    cube = c.f_old.reshape(-1, c.t, c.t, c.t)
+    want = np.concatenate([cube[b[0], b[4]:b[4] + b[7], b[3]:b[3] + b[6], b[2]:b[2] + b[5]].reshape(-1) for b in boxes])
+    bd, od = torch.from_numpy(boxes.view(np.int32)).cuda(), torch.from_numpy(offsets.view(np.int64)).cuda()
+    field = c.dev(c.f_old)
+    packed = torch.full((int(offsets[-1]),), float("nan"), dtype=torch.float32, device="cuda")
+    sharding.pack_boxes(c.cfg, field, c.used, bd, od, len(boxes), packed)
+    torch.cuda.synchronize()
+    assert_same(host(packed), want, "packed boxes vs host slicing")
+    target = torch.zeros_like(field)
+    sharding.unpack_boxes(c.cfg, target, c.used, bd, od, len(boxes), packed)
+    torch.cuda.synchronize()
+    got = host(target).reshape(-1, c.t, c.t, c.t)
+    mask = np.zeros(got.shape, bool)
+    for b in boxes:
+        mask[b[0], b[4]:b[4] + b[7], b[3]:b[3] + b[6], b[2]:b[2] + b[5]] = True
+    assert_same(got[mask], cube[mask], "unpacked cells")
+    assert not got[~mask].any(), "cells outside the boxes were written"
+    # a record outside the cube is skipped, not written
+    bad = boxes[:1].copy()
+    bad[0, 2] = c.t
+    bdd = torch.from_numpy(bad.view(np.int32)).cuda()
+    sharding.unpack_boxes(c.cfg, target, c.used, bdd, od[:2], 1, packed)
+    torch.cuda.synchronize()
+    assert_same(host(target).reshape(got.shape), got, "an invalid record changed the field")
