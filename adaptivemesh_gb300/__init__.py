@@ -66,6 +66,7 @@ EXPORTS = {
     "amr_christoffel": (ctypes.c_int, [CP, VP, VP, I32, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
     "amr_copy_boundaries": (ctypes.c_int, [CP, VP, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
     "amr_copy_boundaries_noalloc": (ctypes.c_int, [CP, VP, VP, VP, U32, U32, U32, ctypes.c_int, VP]),
+    "amr_rasterise": (ctypes.c_int, [CP, VP, VP, U32, U32, U32, ctypes.c_float, VP, VP]),
     "amr_partition_morton": (ctypes.c_int, [VP, U32, U32, VP]),
     "amr_ghost_exchange_plan": (ctypes.c_int, [CP, VP, VP, U32, U32, U32, U32, VP, U32, VP]),
     "amr_pack_boxes": (ctypes.c_int, [CP, VP, U32, VP, VP, U32, VP, VP]),
@@ -93,6 +94,8 @@ EXPORTS = {
     "amr_sim_copy_to_host": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, VP, U64]),
     "amr_sim_event_record": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_event_elapsed": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "amr_sim_save": (ctypes.c_int, [VP, ctypes.c_char_p]),
+    "amr_sim_load": (ctypes.c_int, [VP, ctypes.c_char_p]),
     "amr_sim_timestep": (ctypes.c_int, [VP]),
     "amr_sim_copy_bounds": (ctypes.c_int, [VP]),
     "amr_sim_rng": (ctypes.c_int, [VP, ctypes.POINTER(I32)]),

@@ -10,7 +10,7 @@
 // Compiled (size_domain, padding_domain) pairs.  (28, 2) is the reference as shipped; (16, 3) and
 // (32, 3) are the benchmark sizes; (8, 2) keeps small test cases cheap.
 #define AMR_FOR_EACH_CONFIG(X) X(16, 3) X(28, 2) X(32, 3) X(8, 2)
-// Pairs whose six-component fused kernel fits in shared memory (6 x (2p+3) padded planes).
+// Pairs whose six-component fused kernel fits in shared memory (six rings of 2p+2 padded planes).
 #define AMR_FOR_EACH_BSSN_CONFIG(X) X(16, 3) X(28, 2) X(8, 2)
 
 namespace amr {
@@ -60,6 +60,8 @@ cudaError_t launch_christoffel(Dims d, float* const* metric6, uint32_t* const* d
 cudaError_t launch_wave_step(Dims d, const Geo& g, int corrector, const float* old_f, const uint32_t* der,
                              const uint32_t* hess, float* new_f, const uint32_t* positions, uint32_t used,
                              uint32_t substep, uint32_t max_depth, cudaStream_t st);
+cudaError_t launch_rasterise(Dims d, const float* data, const int32_t* children, uint32_t used, uint32_t width,
+                             uint32_t height, float z_slice, float* raster, cudaStream_t st);
 cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const uint32_t* hess, float* crit,
                              const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
                              cudaStream_t st);
@@ -75,7 +77,8 @@ cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* po
                                    const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
                                    cudaStream_t st);
 cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t child, int32_t parent, cudaStream_t st);
-// Ghost values per (slot, face, layer, v, u): 2 * ncomp * 6 * p * n^2 floats per slot.
+// Staging for the ghost fill (the innermost layer of the three lower faces, old and new):
+// 2 * ncomp * 3 * n^2 floats per slot.
 size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp);
 cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* boundaries, uint32_t used,
                                    uint32_t substep, uint32_t max_depth, int copy_only_new, float* scratch,

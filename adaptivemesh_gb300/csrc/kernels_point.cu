@@ -169,6 +169,48 @@ __global__ void k_criterion_octants(Dims d, float* __restrict__ crit, uint32_t u
     crit[base] = cr;
 }
 
+
+// ---------------------------------------------------------------- slice rasteriser, AMR.h:1313-1352
+// One thread per pixel of a z-slice through the unit cube: descend the octree to the leaf holding
+// the point, interpolate the padded field there (10-point, AMR.h:672-699) and write grey RGBA.
+// The division is the approximate one of the reference's fast-math build; the descent stops at
+// kDepthLimit levels or at a child index outside the used slots.
+__device__ __forceinline__ float div_fast(float a, float b) {
+    float r;
+    asm("div.full.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__global__ void k_rasterise(Dims d, const float* __restrict__ data, const int32_t* __restrict__ children,
+                            uint32_t used, uint32_t width, uint32_t height, float z_slice, float4* __restrict__ raster) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= width || py >= height) return;
+    float tp[3] = {__fsub_rn(div_fast((float)px, (float)width), .5f), __fsub_rn(div_fast((float)py, (float)height), .5f),
+                   z_slice};
+    auto octant = [&]() { return (uint32_t)(tp[0] > 0.f) | ((uint32_t)(tp[1] > 0.f) << 1) | ((uint32_t)(tp[2] > 0.f) << 2); };
+    uint32_t curr = 0;
+    int32_t child = children[octant()];
+    for (uint32_t level = 0; child != -1 && (uint32_t)child < used && level < kDepthLimit; level++) {
+        curr = (uint32_t)child;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {   // fracf(2 t) - 0.5, helper_math.h:1475-1478
+            const float v = __fmul_rn(tp[a], 2.f);
+            tp[a] = __fsub_rn(__fsub_rn(v, floorf(v)), .5f);
+        }
+        child = children[curr * 8u + octant()];
+    }
+    uint32_t ri[3];
+    float r[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float q = __fmaf_rn(__fadd_rn(tp[a], .5f), (float)d.n, (float)d.p);
+        ri[a] = __float2uint_rz(__fadd_rn(q, .5f));
+        r[a] = __fsub_rn(q, (float)ri[a]);
+    }
+    const uint64_t rin = (((uint64_t)curr * d.t + ri[2]) * d.t + ri[1]) * d.t + ri[0];
+    const float v = __fadd_rn(interp10_strided(data + rin, (int)d.t, (int)(d.t * d.t), r[0], r[1], r[2]), .5f);
+    raster[(size_t)py * width + px] = make_float4(v, v, v, 1.f);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
@@ -220,6 +262,14 @@ cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const ui
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_criterion_octants<<<blocks_for((uint64_t)used * 8u), kBlock, 0, st>>>(d, crit, used);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rasterise(Dims d, const float* data, const int32_t* children, uint32_t used, uint32_t width,
+                             uint32_t height, float z_slice, float* raster, cudaStream_t st) {
+    if (width == 0 || height == 0) return cudaSuccess;
+    const dim3 threads(32, 8), grid((width + 31) / 32, (height + 7) / 8);
+    k_rasterise<<<grid, threads, 0, st>>>(d, data, children, used, width, height, z_slice, reinterpret_cast<float4*>(raster));
     return cudaGetLastError();
 }
 

@@ -83,6 +83,20 @@ Octree::Octree(uint32_t node_slots, NodeHooks* hooks)
     positions_[0] = 0u;   // the root
 }
 
+void Octree::restore(const uint32_t* positions, const int32_t* parent, const int32_t* children,
+                     const uint64_t* boundaries, const uint32_t* lifetime, uint32_t timer, int max_depth,
+                     uint32_t first_free, uint32_t final_used) {
+    positions_.assign(positions, positions + max_slots_);
+    parent_.assign(parent, parent + max_slots_);
+    children_.assign(children, children + (size_t)max_slots_ * 8u);
+    boundaries_.assign(boundaries, boundaries + (size_t)max_slots_ * 6u);
+    lifetime_.assign(lifetime, lifetime + max_slots_);
+    timer_ = timer;
+    max_depth_ = max_depth;
+    first_free_slot_ = first_free;
+    final_used_slot_ = final_used;
+    dirty_ = true;
+}
 void Octree::increment_timer() {
     for (uint32_t i = 0; i <= final_used_slot_; i++) {
         const int depth = pos_depth_host(positions_[i]);

@@ -54,6 +54,12 @@ public:
     uint32_t timer() const { return timer_; }
     void set_timer(uint32_t t) { timer_ = t; }
 
+    // Replace the whole state (a checkpoint being resumed); arrays hold max_slots() entries
+    // (children 8x, boundaries 6x).
+    void restore(const uint32_t* positions, const int32_t* parent, const int32_t* children, const uint64_t* boundaries,
+                 const uint32_t* lifetime, uint32_t timer, int max_depth, uint32_t first_free, uint32_t final_used);
+    uint32_t final_used_slot() const { return final_used_slot_; }
+
     // True when the arrays changed since the last mark_clean() (the reference's `dirty`).
     bool dirty() const { return dirty_; }
     void mark_clean() { dirty_ = false; }

@@ -11,8 +11,10 @@
 // BATCHED issues one launch per phase for all components over the list of domains active at the
 // substep; GRAPH replays a captured CUDA graph of one whole BSSN timestep (all substeps).
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "capi_internal.h"
@@ -689,6 +691,117 @@ AMR_API int amr_sim_event_elapsed(amr_sim* s, int first, int second, float* ms) 
     if (st) return st;
     return cuda_status(cudaEventElapsedTime(ms, b->user_events[first], b->user_events[second]));
 }
+// ---------------------------------------------------------------- checkpoint
+// Raw little-endian files, one per array, in the reference's io_helper.h:9-40 format (the buffer's
+// bytes and nothing else), plus state.bin: kCheckpointWords uint32 words of identity and counters.
+namespace {
+constexpr uint32_t kCheckpointMagic = 0x54504B43u;   // "CKPT"
+constexpr int kCheckpointWords = 16;
+
+bool write_file(const std::string& path, const void* data, size_t bytes) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const bool ok = std::fwrite(data, 1, bytes, f) == bytes;
+    return std::fclose(f) == 0 && ok;
+}
+bool read_file(const std::string& path, void* data, size_t bytes) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    bool ok = std::fread(data, 1, bytes, f) == bytes;
+    ok = ok && std::fgetc(f) == EOF;   // exactly the expected size
+    std::fclose(f);
+    return ok;
+}
+int sim_kind(const SimBase* b) { return dynamic_cast<const WaveSim*>(b) ? AMR_SIM_WAVE : AMR_SIM_BSSN; }
+}  // namespace
+
+AMR_API int amr_sim_save(amr_sim* s, const char* dir) {
+    if (!s || !dir) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    int st = cuda_status(cudaStreamSynchronize(b->stream));
+    if (st) return st;
+    const std::string d(dir);
+    const Octree& t = b->tree;
+    const uint32_t slots = t.max_slots();
+    uint32_t words[kCheckpointWords] = {};
+    float outer = b->cfg.outer_size;
+    words[0] = kCheckpointMagic; words[1] = 1u; words[2] = (uint32_t)sim_kind(b);
+    words[3] = b->cfg.size_domain; words[4] = b->cfg.padding_domain; std::memcpy(&words[5], &outer, 4);
+    words[6] = slots; words[7] = t.timer(); words[8] = (uint32_t)t.read_max_depth();
+    words[9] = t.read_first_free_slot(); words[10] = t.final_used_slot(); words[11] = (uint32_t)b->rng;
+    if (!write_file(d + "/state.bin", words, sizeof(words)) ||
+        !write_file(d + "/positions.bin", t.positions().data(), slots * 4u) ||
+        !write_file(d + "/parent.bin", t.parents().data(), slots * 4u) ||
+        !write_file(d + "/children.bin", t.children().data(), (size_t)slots * 32u) ||
+        !write_file(d + "/boundaries.bin", t.boundaries().data(), (size_t)slots * 48u) ||
+        !write_file(d + "/lifetime.bin", t.lifetime().data(), slots * 4u))
+        return AMR_ERR_INVALID;
+    std::vector<uint8_t> host;
+    for (int which = 0; which < 6; which++)
+        for (int comp = 0; comp < 6; comp++) {
+            void* ptr = nullptr;
+            uint64_t count = 0;
+            if (b->buffer(which, comp, &ptr, &count) != AMR_OK) continue;
+            host.resize(count * 4u);
+            if ((st = cuda_status(cudaMemcpy(host.data(), ptr, count * 4u, cudaMemcpyDeviceToHost)))) return st;
+            if (!write_file(d + "/field_" + std::to_string(which) + "_" + std::to_string(comp) + ".bin", host.data(),
+                            host.size()))
+                return AMR_ERR_INVALID;
+        }
+    return AMR_OK;
+}
+
+AMR_API int amr_sim_load(amr_sim* s, const char* dir) {
+    if (!s || !dir) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    int st = cuda_status(cudaStreamSynchronize(b->stream));
+    if (st) return st;
+    const std::string d(dir);
+    const uint32_t slots = b->tree.max_slots();
+    uint32_t words[kCheckpointWords];
+    float outer = b->cfg.outer_size;
+    uint32_t outer_bits;
+    std::memcpy(&outer_bits, &outer, 4);
+    if (!read_file(d + "/state.bin", words, sizeof(words))) return AMR_ERR_INVALID;
+    if (words[0] != kCheckpointMagic || words[1] != 1u || words[2] != (uint32_t)sim_kind(b) ||
+        words[3] != b->cfg.size_domain || words[4] != b->cfg.padding_domain || words[5] != outer_bits ||
+        words[6] != slots || words[8] > kDepthLimit || words[10] >= slots || words[9] > slots)
+        return AMR_ERR_INVALID;
+    std::vector<uint32_t> pos(slots), life(slots);
+    std::vector<int32_t> par(slots), ch((size_t)slots * 8u);
+    std::vector<uint64_t> bd((size_t)slots * 6u);
+    if (!read_file(d + "/positions.bin", pos.data(), slots * 4u) || !read_file(d + "/parent.bin", par.data(), slots * 4u) ||
+        !read_file(d + "/children.bin", ch.data(), (size_t)slots * 32u) ||
+        !read_file(d + "/boundaries.bin", bd.data(), (size_t)slots * 48u) ||
+        !read_file(d + "/lifetime.bin", life.data(), slots * 4u))
+        return AMR_ERR_INVALID;
+    // the device kernels index with these: children and boundary targets must name slots
+    for (int32_t c : ch)
+        if (c < -1 || c >= (int32_t)slots) return AMR_ERR_INVALID;
+    for (uint64_t v : bd) {
+        const uint32_t nd = (uint32_t)v;
+        const int32_t target = (int32_t)((nd & 16777215u) | ((nd & (1u << 23)) ? 4278190080u : 0u));
+        if (target < -1 || target >= (int32_t)slots) return AMR_ERR_INVALID;
+    }
+    std::vector<uint8_t> host;
+    for (int which = 0; which < 6; which++)
+        for (int comp = 0; comp < 6; comp++) {
+            void* ptr = nullptr;
+            uint64_t count = 0;
+            if (b->buffer(which, comp, &ptr, &count) != AMR_OK) continue;
+            host.resize(count * 4u);
+            if (!read_file(d + "/field_" + std::to_string(which) + "_" + std::to_string(comp) + ".bin", host.data(),
+                           host.size()))
+                return AMR_ERR_INVALID;
+            if ((st = cuda_status(cudaMemcpy(ptr, host.data(), count * 4u, cudaMemcpyHostToDevice)))) return st;
+        }
+    b->tree.restore(pos.data(), par.data(), ch.data(), bd.data(), life.data(), words[7], (int)words[8], words[9],
+                    words[10]);
+    b->rng = (int32_t)words[11];
+    b->graph_valid = false;
+    return AMR_OK;
+}
+
 AMR_API int amr_sim_timestep(amr_sim* s) { return s ? s->impl->timestep() : AMR_ERR_INVALID; }
 AMR_API int amr_sim_copy_bounds(amr_sim* s) { return s ? s->impl->copy_bounds() : AMR_ERR_INVALID; }
 AMR_API int amr_sim_rng(const amr_sim* s, int32_t* seed) {

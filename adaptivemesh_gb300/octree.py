@@ -123,6 +123,14 @@ class Sim:
         check(load().amr_sim_event_elapsed(self.h, first, second, ctypes.byref(ms)), "amr_sim_event_elapsed")
         return float(ms.value)
 
+    def save_checkpoint(self, directory: str) -> None:
+        """Checkpoint into an existing directory (amr_sim_save)."""
+        check(load().amr_sim_save(self.h, directory.encode()), "amr_sim_save")
+
+    def load_checkpoint(self, directory: str) -> None:
+        """Resume from a checkpoint of a simulation of the same kind and size (amr_sim_load)."""
+        check(load().amr_sim_load(self.h, directory.encode()), "amr_sim_load")
+
     def timestep(self) -> None:
         check(load().amr_sim_timestep(self.h), "amr_sim_timestep")
 

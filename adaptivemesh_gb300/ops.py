@@ -89,3 +89,12 @@ def criterion(cfg: Config, derivs, hess, crit, positions, used: int, substep: in
     """The device half of amr_criterion() (SimpleWave.h:142-150)."""
     check(load().amr_criterion(ctypes.byref(cfg), _p(derivs), _p(hess), _p(crit), _p(positions), used, substep,
                                max_depth, _s(stream)), "amr_criterion")
+
+
+def rasterise(cfg: Config, field, children, used: int, width: int, height: int, raster, z_slice: float = 1e-9,
+              stream=None) -> None:
+    """Slice image of a padded field (rasterise_to_image, AdaptiveMesh/AMR.h:1313-1365): `raster`
+    holds width * height RGBA floats; the reference's default slice is z = 1e-9."""
+    check(load().amr_rasterise(ctypes.byref(cfg), _p(field), _p(children), used, width, height, z_slice, _p(raster),
+                               _s(stream)))
+

@@ -107,6 +107,13 @@ int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_f, const
 int amr_copy_boundaries_noalloc(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,
                                 uint32_t used_slots, uint32_t substep, uint32_t max_depth, int copy_only_new,
                                 void* stream);
+/* Rasterise the z = z_slice plane of the unit cube ([-0.5, 0.5]^3, the root's extent) into a
+ * width x height RGBA float image (16-byte aligned, row-major, y rows): per pixel, descend the
+ * octree (children, used_slots) to the leaf containing the point and interpolate `field` (a padded
+ * field) there; the grey value is the interpolated value + 0.5, alpha 1.  Replaces
+ * rasterise_to_image (AMR.h:1313-1365), bit for bit; width, height <= 65536. */
+int amr_rasterise(const amr_config* cfg, const float* field, const int32_t* children, uint32_t used_slots,
+                  uint32_t width, uint32_t height, float z_slice, float* raster_rgba, void* stream);
 /* ---- sharding by domain (no counterpart in the reference, which runs on one GPU) ----
  * Ranks own contiguous ranges of the live slots in the preorder (Morton) order of their positions
  * (octree_abs_pos, AMR.h:22-55), balanced by count; owner[s] = rank, or -1 for a free slot
@@ -199,6 +206,17 @@ int amr_sim_buffer(amr_sim* s, int which, int comp, void** dev_ptr, uint64_t* co
  * (CUDA_memory.h:177-184).  `count` elements (4 bytes each) from the start of the buffer. */
 int amr_sim_copy_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count);
 int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, uint64_t count);
+/* Checkpoint of a simulation into the existing directory `dir`: the octree arrays
+ * (positions.bin, parent.bin, children.bin, boundaries.bin, lifetime.bin), every field buffer
+ * amr_sim_buffer names (field_<which>_<comp>.bin), each the raw little-endian bytes of the whole
+ * array as the reference's write_to_file (io_helper.h:9-17) writes a buffer, and state.bin
+ * (16 uint32: "CKPT", version 1, kind, size_domain, padding_domain, outer_size bits, node_slots,
+ * timer, max depth, first free slot, final used slot, generator state, 0...).  amr_sim_load restores
+ * them into a simulation of the same kind, configuration and node_slots (else AMR_ERR_INVALID);
+ * a resumed timestep is bit-identical to an uninterrupted one.  Both synchronise the stream.  The
+ * reference has no checkpoint of its own. */
+int amr_sim_save(amr_sim* sim, const char* dir);
+int amr_sim_load(amr_sim* sim, const char* dir);
 /* Timing events on the simulation's stream: record event `slot` (0..15), and read the
  * milliseconds between two recorded events (waits for the later one). */
 int amr_sim_event_record(amr_sim* s, int slot);

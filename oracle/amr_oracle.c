@@ -541,6 +541,43 @@ void orc_copy_to_child(const orc_cfg* c, float* buf, uint32_t offset, int32_t ch
     }
 }
 
+/* ------------------------------------------------------------------ slice rasteriser, AMR.h:1313-1352 */
+/* The device build divides px / width with its approximate division; this restatement divides
+ * exactly, which is the same for power-of-two widths and heights. */
+void orc_rasterise(const orc_cfg* c, const float* data, const int32_t* children, uint32_t width, uint32_t height,
+                   float z_slice, float* rgba) {
+    const uint32_t n = c->n, p = c->p, t = n + 2 * p;
+    #pragma omp parallel for schedule(static)
+    for (int64_t yy = 0; yy < (int64_t)height; yy++) {
+        const uint32_t py = (uint32_t)yy;
+        for (uint32_t px = 0; px < width; px++) {
+            float tp[3] = {(float)px / (float)width - .5f, (float)py / (float)height - .5f, z_slice};
+            uint32_t curr = 0;
+            uint32_t off = (uint32_t)(tp[0] > 0.f) | ((uint32_t)(tp[1] > 0.f) << 1) | ((uint32_t)(tp[2] > 0.f) << 2);
+            int32_t child = children[off];
+            while (child != -1) {
+                curr = (uint32_t)child;
+                for (int a = 0; a < 3; a++) {       /* fracf(2 t) - 0.5, helper_math.h:1475-1478 */
+                    const float v = tp[a] * 2.f;
+                    tp[a] = (v - floorf(v)) - .5f;
+                }
+                off = (uint32_t)(tp[0] > 0.f) | ((uint32_t)(tp[1] > 0.f) << 1) | ((uint32_t)(tp[2] > 0.f) << 2);
+                child = children[curr * 8u + off];
+            }
+            uint32_t ri[3]; float r[3];
+            for (int a = 0; a < 3; a++) {           /* nearest cell, USE_LAGRANGE_POLYNOMIAL (AMR.h:4, 1340-1344) */
+                const float q = fmaf(tp[a] + .5f, (float)n, (float)p);
+                ri[a] = f2u(q + .5f);
+                r[a] = q - (float)ri[a];
+            }
+            const int64_t rin = (((int64_t)curr * t + ri[2]) * t + ri[1]) * t + ri[0];
+            const float v = interp10(data, rin, t, r) + .5f;
+            float* o = rgba + 4 * ((uint64_t)py * width + px);
+            o[0] = v; o[1] = v; o[2] = v; o[3] = 1.f;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------ SimpleWave update, SimpleWave.h:7-46 */
 void orc_wave_step(const orc_cfg* c, int corrector, const float* old_f, const uint32_t* derivs, const uint32_t* hess,
                    float* new_f, const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth) {

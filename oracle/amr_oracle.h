@@ -89,6 +89,9 @@ void orc_copy_new_to_old(const orc_cfg* c, float* old_f, const float* new_f, con
 /* __copy_to_child, AMR.h:1053-1073 */
 void orc_copy_to_child(const orc_cfg* c, float* buf, uint32_t offset, int32_t child, int32_t parent);
 /* __predictor_step / __corrector_step, SimpleWave.h:7-46 */
+/* rasterise_to_image, AMR.h:1313-1365: width x height RGBA floats of the z = z_slice plane */
+void orc_rasterise(const orc_cfg* c, const float* data, const int32_t* children, uint32_t width, uint32_t height,
+                   float z_slice, float* rgba);
 void orc_wave_step(const orc_cfg* c, int corrector, const float* old_f, const uint32_t* derivs, const uint32_t* hess,
                    float* new_f, const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth);
 /* __amr_criterion_1 and __amr_criterion_2, SimpleWave.h:91-139 */

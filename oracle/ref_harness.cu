@@ -326,6 +326,16 @@ REF_API int refd_criterion(const uint32_t* derivs, const uint32_t* hess, float* 
     return launch_status();
 }
 
+// rasterise_to_image, AMR.h:1356-1365 (the wrapper's launch shape)
+REF_API int refd_rasterise(const float* data, float* raster, const int32_t* children, uint32_t width, uint32_t height,
+                           float z_slice) {
+    dim3 threads(min_uint(width, 32u), min_uint(height, 32u), 1u);
+    dim3 blocks((uint32_t)ceilf(float(width) / threads.x), (uint32_t)ceilf(float(height) / threads.y), 1u);
+    __rasterise_to_image<<<blocks, threads>>>(data, (float4*)raster, children, width, height, size_domain,
+                                              padding_domain, z_slice);
+    return launch_status();
+}
+
 // ------------------------------------------------------------------ device: whole plugins
 struct RefBssn { AMR<BSSN_AMR_data> amr; explicit RefBssn(uint32_t s) : amr(s) { amr.timer_helper = 0u; } };
 REF_API void* refd_bssn_create(uint32_t slots) { return new RefBssn(slots); }

@@ -392,3 +392,30 @@ def test_pack_unpack_boxes(am, cuda, cfgname, tree):
     sharding.unpack_boxes(c.cfg, target, c.used, bdd, od[:2], 1, packed)
     torch.cuda.synchronize()
     assert_same(host(target).reshape(got.shape), got, "an invalid record changed the field")
+
+
+# ----------------------------------------------------------------------------- slice rasteriser
+@pytest.mark.parametrize("cfgname,tree", [("n16p3", "uneven"), ("n28p2", "bssn"), ("n28p2", "uneven")])
+@pytest.mark.parametrize("width,height,z_slice", [(1024, 1024, 1e-9), (256, 128, -0.3), (1000, 600, 0.2)])
+def test_rasterise(am, cuda, orc, cfgname, tree, width, height, z_slice):
+    """rasterise_to_image (AMR.h:1313-1365): bit-identical to the reference's kernel; equal to the
+    oracle where its exact division agrees with the device's (power-of-two sizes)."""
+    import torch
+    c = Case(am, cfgname, tree)
+    field = c.dev(c.f_new)
+    raster = torch.full((height * width * 4,), float("nan"), dtype=torch.float32, device="cuda")
+    am.ops.rasterise(c.cfg, field, c.ch, c.used, width, height, raster, z_slice)
+    torch.cuda.synchronize()
+    mine = host(raster)
+    assert np.isfinite(mine).all()
+    ref = ref_lib(cfgname)
+    if ref is not None:
+        rr = torch.full_like(raster, float("nan"))
+        assert ref.refd_rasterise(field.data_ptr(), rr.data_ptr(), c.ch.data_ptr(), width, height, z_slice) == 0
+        torch.cuda.synchronize()
+        assert_same(mine, host(rr), f"raster {width}x{height} vs reference")
+    if width & (width - 1) == 0 and height & (height - 1) == 0:
+        o = np.zeros(height * width * 4, np.float32)
+        orc.lib().orc_rasterise(ctypes.byref(orc.cfg(c.n, c.p, OUTER)), orc.P(c.f_new), orc.P(c.st["children"]),
+                                width, height, z_slice, orc.P(o))
+        assert_same(mine, o, f"raster {width}x{height} vs oracle")

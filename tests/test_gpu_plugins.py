@@ -213,3 +213,86 @@ def test_wave_plugin_matches_reference(am, cuda, ref28):
         assert sim.rng == int(ref28.refd_wave_rng_seed(h))
     ref28.refd_wave_destroy(h)
     sim.close()
+
+
+# ----------------------------------------------------------------------------- checkpoint / resume
+def _full_state(am, sim, kind):
+    """Every buffer the simulation names, the octree and the generator, as host arrays."""
+    out = {f"tree_{k}": v for k, v in sim.state().items()}
+    out["rng"] = sim.rng
+    comps = range(6) if kind == am.SIM_BSSN else [0]
+    for which in range(6):
+        for k in comps:
+            try:
+                t = sim.tensor(which, k)
+            except am.AmrError:
+                continue
+            out[f"buf{which}_{k}"] = t.cpu().numpy().view(np.uint32)
+    return out
+
+
+def _assert_states_equal(a, b, what):
+    assert a.keys() == b.keys()
+    for k in a:
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), f"{what}: {k} differs"
+
+
+def test_bssn_checkpoint_resume_is_bit_identical(am, cuda, tmp_path):
+    cfg = am.Config(16, 3, 100.0)
+    sim, _st, _ = _bssn_sim(am, cfg, "uneven", am.MODE_GRAPH)
+    sim.timestep()
+    sim.save_checkpoint(str(tmp_path))
+    sim.timestep()
+    sim.timestep()
+    sim.synchronize()
+    want = _full_state(am, sim, am.SIM_BSSN)
+    sim.close()
+    resumed = am.Sim(cfg, am.SIM_BSSN, slots=128, mode=am.MODE_BATCHED)
+    resumed.load_checkpoint(str(tmp_path))
+    resumed.timestep()
+    resumed.set_mode(am.MODE_GRAPH)
+    resumed.timestep()
+    resumed.synchronize()
+    _assert_states_equal(_full_state(am, resumed, am.SIM_BSSN), want, "resumed BSSN")
+    resumed.close()
+    # a checkpoint of another size is refused
+    other = am.Sim(am.Config(28, 2, 100.0), am.SIM_BSSN, slots=128, mode=am.MODE_BATCHED)
+    with pytest.raises(am.AmrError):
+        other.load_checkpoint(str(tmp_path))
+    other.close()
+
+
+def test_wave_checkpoint_resume_with_regridding(am, cuda, tmp_path):
+    """The wave plugin adds and removes nodes as it runs: the resumed run regrids identically."""
+    import torch
+    cfg = am.Config(28, 2, 100.0)
+    t = cfg.total
+
+    def fresh():
+        sim = am.Sim(cfg, am.SIM_WAVE, slots=128, mode=am.MODE_BATCHED)
+        xyz = cases.cell_coordinates(sim.state()["positions"], 1, 28, 2, 100.0)
+        f0 = cases.smooth_field(xyz, 100.0, 0, 77, noise=0.0) * np.float32(0.5)
+        for which in (am.Sim.OLD, am.Sim.NEW):
+            sim.tensor(which)[: t ** 3].copy_(torch.from_numpy(f0).cuda())
+        torch.cuda.synchronize()
+        return sim
+    sim = fresh()
+    for c in range(8):
+        sim.add_node(0, c)
+    sim.copy_bounds()
+    sim.timestep()
+    sim.save_checkpoint(str(tmp_path))
+    before = sim.state()["used_slots"]
+    for _ in range(3):
+        sim.timestep()
+    sim.synchronize()
+    want = _full_state(am, sim, am.SIM_WAVE)
+    sim.close()
+    resumed = fresh()
+    resumed.load_checkpoint(str(tmp_path))
+    assert resumed.state()["used_slots"] == before
+    for _ in range(3):
+        resumed.timestep()
+    resumed.synchronize()
+    _assert_states_equal(_full_state(am, resumed, am.SIM_WAVE), want, "resumed wave plugin")
+    resumed.close()
