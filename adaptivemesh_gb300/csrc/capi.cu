@@ -260,12 +260,13 @@ AMR_API int amr_criterion(const amr_config* cfg, const uint32_t* derivs, const u
 }
 
 AMR_API int amr_rasterise(const amr_config* cfg, const float* field, const int32_t* children, uint32_t used,
-                          uint32_t width, uint32_t height, float z_slice, float* raster_rgba, void* stream) {
+                          uint32_t width, uint32_t height, float z_slice, int bounding_boxes, float* raster_rgba,
+                          void* stream) {
     AMR_REQUIRE_CFG(cfg);
     AMR_REQUIRE(field && children && raster_rgba && used >= 1u && width <= 65536u && height <= 65536u);
     AMR_REQUIRE(reinterpret_cast<uintptr_t>(raster_rgba) % 16u == 0u);
-    return cuda_status(launch_rasterise(make_dims(*cfg), field, children, used, width, height, z_slice, raster_rgba,
-                                        S(stream)));
+    return cuda_status(launch_rasterise(make_dims(*cfg), field, children, used, width, height, z_slice,
+                                        bounding_boxes ? 1 : 0, raster_rgba, S(stream)));
 }
 
 // ---------------------------------------------------------------- octree

@@ -61,7 +61,7 @@ cudaError_t launch_wave_step(Dims d, const Geo& g, int corrector, const float* o
                              const uint32_t* hess, float* new_f, const uint32_t* positions, uint32_t used,
                              uint32_t substep, uint32_t max_depth, cudaStream_t st);
 cudaError_t launch_rasterise(Dims d, const float* data, const int32_t* children, uint32_t used, uint32_t width,
-                             uint32_t height, float z_slice, float* raster, cudaStream_t st);
+                             uint32_t height, float z_slice, int boxes, float* raster, cudaStream_t st);
 cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const uint32_t* hess, float* crit,
                              const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
                              cudaStream_t st);

@@ -172,24 +172,22 @@ __global__ void k_criterion_octants(Dims d, float* __restrict__ crit, uint32_t u
 
 // ---------------------------------------------------------------- slice rasteriser, AMR.h:1313-1352
 // One thread per pixel of a z-slice through the unit cube: descend the octree to the leaf holding
-// the point, interpolate the padded field there (10-point, AMR.h:672-699) and write grey RGBA.
-// The division is the approximate one of the reference's fast-math build; the descent stops at
+// the point, interpolate the padded field there (10-point, AMR.h:672-699) and write grey RGBA, or
+// red near the leaf's border when bounding boxes are drawn (the reference's build draws them).
+// As the reference's fast-math build computes them, px / width - 0.5 is a fused multiply-add with
+// the approximate reciprocal of width, and so is the border threshold.  The descent stops at
 // kDepthLimit levels or at a child index outside the used slots.
-__device__ __forceinline__ float div_fast(float a, float b) {
-    float r;
-    asm("div.full.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
-    return r;
-}
 __global__ void k_rasterise(Dims d, const float* __restrict__ data, const int32_t* __restrict__ children,
-                            uint32_t used, uint32_t width, uint32_t height, float z_slice, float4* __restrict__ raster) {
+                            uint32_t used, uint32_t width, uint32_t height, float z_slice, int boxes,
+                            float4* __restrict__ raster) {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
     if (px >= width || py >= height) return;
-    float tp[3] = {__fsub_rn(div_fast((float)px, (float)width), .5f), __fsub_rn(div_fast((float)py, (float)height), .5f),
-                   z_slice};
+    const float rw = rcp_approx((float)width), rh = rcp_approx((float)height);
+    float tp[3] = {__fmaf_rn((float)px, rw, -.5f), __fmaf_rn((float)py, rh, -.5f), z_slice};
     auto octant = [&]() { return (uint32_t)(tp[0] > 0.f) | ((uint32_t)(tp[1] > 0.f) << 1) | ((uint32_t)(tp[2] > 0.f) << 2); };
-    uint32_t curr = 0;
+    uint32_t curr = 0, depth = 0;
     int32_t child = children[octant()];
-    for (uint32_t level = 0; child != -1 && (uint32_t)child < used && level < kDepthLimit; level++) {
+    for (; child != -1 && (uint32_t)child < used && depth < kDepthLimit; depth++) {
         curr = (uint32_t)child;
 #pragma unroll
         for (int a = 0; a < 3; a++) {   // fracf(2 t) - 0.5, helper_math.h:1475-1478
@@ -197,6 +195,13 @@ __global__ void k_rasterise(Dims d, const float* __restrict__ data, const int32_
             tp[a] = __fsub_rn(__fsub_rn(v, floorf(v)), .5f);
         }
         child = children[curr * 8u + octant()];
+    }
+    if (boxes) {   // DISPLAY_BOUNDING_BOXES (AMR.h:1312, 1329-1337): red where the leaf's border is near
+        const float threshold = __fmaf_rn(-__fmul_rn(2.f, (float)(1u << depth)), rw, .5f);
+        if (fmaxf(fabsf(tp[0]), fabsf(tp[1])) >= threshold) {
+            raster[(size_t)py * width + px] = make_float4(1.f, 0.f, 0.f, 1.f);
+            return;
+        }
     }
     uint32_t ri[3];
     float r[3];
@@ -266,10 +271,11 @@ cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const ui
 }
 
 cudaError_t launch_rasterise(Dims d, const float* data, const int32_t* children, uint32_t used, uint32_t width,
-                             uint32_t height, float z_slice, float* raster, cudaStream_t st) {
+                             uint32_t height, float z_slice, int boxes, float* raster, cudaStream_t st) {
     if (width == 0 || height == 0) return cudaSuccess;
     const dim3 threads(32, 8), grid((width + 31) / 32, (height + 7) / 8);
-    k_rasterise<<<grid, threads, 0, st>>>(d, data, children, used, width, height, z_slice, reinterpret_cast<float4*>(raster));
+    k_rasterise<<<grid, threads, 0, st>>>(d, data, children, used, width, height, z_slice, boxes,
+                                          reinterpret_cast<float4*>(raster));
     return cudaGetLastError();
 }
 

@@ -395,7 +395,8 @@ private:
             return SimBase::timestep();
         }
         const uint32_t nsub = 1u << tree.read_max_depth();
-        if (!graph_valid) {
+        const bool capture = !graph_valid;   // capturing runs the host loop, counter and lifetimes included
+        if (capture) {
             if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
             cudaGraph_t graph;
             cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
@@ -427,6 +428,10 @@ private:
         if (e == cudaSuccess) e = cudaGraphLaunch(graph_exec, stream);
         if (e != cudaSuccess) return cuda_status(e);
         launches += graph_launches;
+        // a replay does the device work only: advance the octree's counter and lifetimes as the
+        // timestep loop would (AMR.h:180-188, once per substep; the counter returns to 0)
+        if (!capture)
+            for (uint32_t s = 0; s < nsub; s++) tree.increment_timer();
         return AMR_OK;
     }
 

@@ -92,9 +92,10 @@ def criterion(cfg: Config, derivs, hess, crit, positions, used: int, substep: in
 
 
 def rasterise(cfg: Config, field, children, used: int, width: int, height: int, raster, z_slice: float = 1e-9,
-              stream=None) -> None:
+              bounding_boxes: bool = True, stream=None) -> None:
     """Slice image of a padded field (rasterise_to_image, AdaptiveMesh/AMR.h:1313-1365): `raster`
-    holds width * height RGBA floats; the reference's default slice is z = 1e-9."""
-    check(load().amr_rasterise(ctypes.byref(cfg), _p(field), _p(children), used, width, height, z_slice, _p(raster),
-                               _s(stream)))
+    holds width * height RGBA floats; the reference's default slice is z = 1e-9 and its build draws
+    the leaves' bounding boxes (AMR.h:1312)."""
+    check(load().amr_rasterise(ctypes.byref(cfg), _p(field), _p(children), used, width, height, z_slice,
+                               1 if bounding_boxes else 0, _p(raster), _s(stream)))
 

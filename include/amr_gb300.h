@@ -110,10 +110,13 @@ int amr_copy_boundaries_noalloc(const amr_config* cfg, float* old_f, float* new_
 /* Rasterise the z = z_slice plane of the unit cube ([-0.5, 0.5]^3, the root's extent) into a
  * width x height RGBA float image (16-byte aligned, row-major, y rows): per pixel, descend the
  * octree (children, used_slots) to the leaf containing the point and interpolate `field` (a padded
- * field) there; the grey value is the interpolated value + 0.5, alpha 1.  Replaces
- * rasterise_to_image (AMR.h:1313-1365), bit for bit; width, height <= 65536. */
+ * field) there; the grey value is the interpolated value + 0.5, alpha 1.  With bounding_boxes != 0,
+ * pixels within 2^(depth+1) / width of a leaf's x or y border are red (1, 0, 0, 1), as the
+ * reference's build draws them (DISPLAY_BOUNDING_BOXES, AMR.h:1312).  Replaces rasterise_to_image
+ * (AMR.h:1313-1365), bit for bit; width, height <= 65536. */
 int amr_rasterise(const amr_config* cfg, const float* field, const int32_t* children, uint32_t used_slots,
-                  uint32_t width, uint32_t height, float z_slice, float* raster_rgba, void* stream);
+                  uint32_t width, uint32_t height, float z_slice, int bounding_boxes, float* raster_rgba,
+                  void* stream);
 /* ---- sharding by domain (no counterpart in the reference, which runs on one GPU) ----
  * Ranks own contiguous ranges of the live slots in the preorder (Morton) order of their positions
  * (octree_abs_pos, AMR.h:22-55), balanced by count; owner[s] = rank, or -1 for a free slot

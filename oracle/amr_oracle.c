@@ -542,20 +542,21 @@ void orc_copy_to_child(const orc_cfg* c, float* buf, uint32_t offset, int32_t ch
 }
 
 /* ------------------------------------------------------------------ slice rasteriser, AMR.h:1313-1352 */
-/* The device build divides px / width with its approximate division; this restatement divides
- * exactly, which is the same for power-of-two widths and heights. */
+/* The device build computes px / width - 0.5 (and the bounding-box threshold) as a fused
+ * multiply-add with the approximate reciprocal of width; this restatement divides exactly, which is
+ * the same for power-of-two widths and heights. */
 void orc_rasterise(const orc_cfg* c, const float* data, const int32_t* children, uint32_t width, uint32_t height,
-                   float z_slice, float* rgba) {
+                   float z_slice, int boxes, float* rgba) {
     const uint32_t n = c->n, p = c->p, t = n + 2 * p;
     #pragma omp parallel for schedule(static)
     for (int64_t yy = 0; yy < (int64_t)height; yy++) {
         const uint32_t py = (uint32_t)yy;
         for (uint32_t px = 0; px < width; px++) {
             float tp[3] = {(float)px / (float)width - .5f, (float)py / (float)height - .5f, z_slice};
-            uint32_t curr = 0;
+            uint32_t curr = 0, depth = 0;
             uint32_t off = (uint32_t)(tp[0] > 0.f) | ((uint32_t)(tp[1] > 0.f) << 1) | ((uint32_t)(tp[2] > 0.f) << 2);
             int32_t child = children[off];
-            while (child != -1) {
+            for (; child != -1; depth++) {
                 curr = (uint32_t)child;
                 for (int a = 0; a < 3; a++) {       /* fracf(2 t) - 0.5, helper_math.h:1475-1478 */
                     const float v = tp[a] * 2.f;
@@ -563,6 +564,14 @@ void orc_rasterise(const orc_cfg* c, const float* data, const int32_t* children,
                 }
                 off = (uint32_t)(tp[0] > 0.f) | ((uint32_t)(tp[1] > 0.f) << 1) | ((uint32_t)(tp[2] > 0.f) << 2);
                 child = children[curr * 8u + off];
+            }
+            float* o = rgba + 4 * ((uint64_t)py * width + px);
+            if (boxes) {                             /* DISPLAY_BOUNDING_BOXES, AMR.h:1312, 1329-1337 */
+                const float threshold = .5f - 2.f * (float)(1u << depth) / (float)width;
+                if (fmaxf(fabsf(tp[0]), fabsf(tp[1])) >= threshold) {
+                    o[0] = 1.f; o[1] = 0.f; o[2] = 0.f; o[3] = 1.f;
+                    continue;
+                }
             }
             uint32_t ri[3]; float r[3];
             for (int a = 0; a < 3; a++) {           /* nearest cell, USE_LAGRANGE_POLYNOMIAL (AMR.h:4, 1340-1344) */
@@ -572,7 +581,6 @@ void orc_rasterise(const orc_cfg* c, const float* data, const int32_t* children,
             }
             const int64_t rin = (((int64_t)curr * t + ri[2]) * t + ri[1]) * t + ri[0];
             const float v = interp10(data, rin, t, r) + .5f;
-            float* o = rgba + 4 * ((uint64_t)py * width + px);
             o[0] = v; o[1] = v; o[2] = v; o[3] = 1.f;
         }
     }

@@ -91,7 +91,7 @@ void orc_copy_to_child(const orc_cfg* c, float* buf, uint32_t offset, int32_t ch
 /* __predictor_step / __corrector_step, SimpleWave.h:7-46 */
 /* rasterise_to_image, AMR.h:1313-1365: width x height RGBA floats of the z = z_slice plane */
 void orc_rasterise(const orc_cfg* c, const float* data, const int32_t* children, uint32_t width, uint32_t height,
-                   float z_slice, float* rgba);
+                   float z_slice, int boxes, float* rgba);
 void orc_wave_step(const orc_cfg* c, int corrector, const float* old_f, const uint32_t* derivs, const uint32_t* hess,
                    float* new_f, const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth);
 /* __amr_criterion_1 and __amr_criterion_2, SimpleWave.h:91-139 */

@@ -59,7 +59,7 @@ _SIGS = {
     "orc_copy_to_child": (None, [VP, VP, U32, I32, I32]),
     "orc_wave_step": (None, [VP, ctypes.c_int, VP, VP, VP, VP, VP, U32, U32, U32]),
     "orc_criterion": (None, [VP, VP, VP, VP, VP, U32, U32, U32]),
-    "orc_rasterise": (None, [VP, VP, VP, U32, U32, ctypes.c_float, VP]),
+    "orc_rasterise": (None, [VP, VP, VP, U32, U32, ctypes.c_float, ctypes.c_int, VP]),
     "orc_differentiate_f64": (None, [VP, VP, VP, VP, VP, VP, U32]),
     "orc_bssn_timestep": (None, [VP, VP, VP, VP, VP, VP, VP, VP, VP, U32, U32, VP, VP, U32, U32]),
     "orc_num_threads": (ctypes.c_int, []),

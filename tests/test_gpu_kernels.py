@@ -408,6 +408,8 @@ def test_rasterise(am, cuda, orc, cfgname, tree, width, height, z_slice):
     torch.cuda.synchronize()
     mine = host(raster)
     assert np.isfinite(mine).all()
+    red = (mine.reshape(-1, 4) == np.array([1, 0, 0, 1], np.float32)).all(axis=1)
+    assert 0 < red.sum() < red.size // 2, "bounding boxes drawn on some, not most, pixels"
     ref = ref_lib(cfgname)
     if ref is not None:
         rr = torch.full_like(raster, float("nan"))
@@ -417,5 +419,5 @@ def test_rasterise(am, cuda, orc, cfgname, tree, width, height, z_slice):
     if width & (width - 1) == 0 and height & (height - 1) == 0:
         o = np.zeros(height * width * 4, np.float32)
         orc.lib().orc_rasterise(ctypes.byref(orc.cfg(c.n, c.p, OUTER)), orc.P(c.f_new), orc.P(c.st["children"]),
-                                width, height, z_slice, orc.P(o))
+                                width, height, z_slice, 1, orc.P(o))
         assert_same(mine, o, f"raster {width}x{height} vs oracle")
