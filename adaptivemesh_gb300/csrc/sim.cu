@@ -47,7 +47,12 @@ public:
     SimBase(const amr_config& c, uint32_t slots, int mode)
         : cfg(c), dims(make_dims(c)), geo(make_geo(c)), mode(mode), tree(slots, this) {}
     virtual ~SimBase() {
+        if (side_stream) cudaStreamSynchronize(side_stream);
         if (stream) cudaStreamSynchronize(stream);
+        if (side_stream) cudaStreamDestroy(side_stream);
+        if (main_mark) cudaEventDestroy(main_mark);
+        for (auto& row : side_done)
+            for (auto& ev : row) if (ev) cudaEventDestroy(ev);
         cudaFree(d_positions); cudaFree(d_children); cudaFree(d_boundaries); cudaFree(d_items);
         cudaFree(ghost_stage);
         for (auto& ev : events) cudaEventDestroy(ev);
@@ -212,6 +217,24 @@ public:
     std::vector<cudaEvent_t> events;
     size_t ev_used = 0;
     cudaEvent_t user_events[16] = {};
+    // Side stream for reads of results that overlap later work on `stream` (amr_sim_copy_to_host_side):
+    // side_done[which][comp] marks the last side copy of a buffer, side_pending that one is outstanding.
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t main_mark = nullptr;
+    cudaEvent_t side_done[6][6] = {};
+    bool side_pending[6][6] = {};
+
+    // Make `stream` wait for outstanding side copies: of one buffer, or (which < 0) of all.
+    int wait_side(int which, int comp) {
+        for (int w = 0; w < 6; w++)
+            for (int c = 0; c < 6; c++) {
+                if (!side_pending[w][c] || (which >= 0 && (w != which || c != comp))) continue;
+                cudaError_t e = cudaStreamWaitEvent(stream, side_done[w][c], 0);
+                if (e != cudaSuccess) return cuda_status(e);
+                side_pending[w][c] = false;
+            }
+        return AMR_OK;
+    }
     double timed_ms = 0.0;
     uint64_t timed_launches = 0;
 };
@@ -645,6 +668,8 @@ AMR_API int amr_sim_set_mode(amr_sim* s, int mode) {
 }
 AMR_API int amr_sim_add_node(amr_sim* s, int32_t parent, int32_t offset) {
     if (!s || parent < 0 || (uint32_t)parent >= s->impl->tree.max_slots() || offset < 0 || offset > 7) return AMR_ERR_INVALID;
+    const int st = s->impl->wait_side(-1, 0);   // node_ctor writes the new slot's fields
+    if (st) return st;
     s->impl->tree.add_node(parent, offset);
     return AMR_OK;
 }
@@ -666,12 +691,37 @@ static int sim_copy(amr_sim* s, int which, int comp, void* host, uint64_t count,
     if (!s || !host) return AMR_ERR_INVALID;
     void* dev = nullptr;
     uint64_t n = 0;
-    const int st = s->impl->buffer(which, comp, &dev, &n);
+    int st = s->impl->buffer(which, comp, &dev, &n);
     if (st) return st;
     if (count > n) return AMR_ERR_INVALID;
     if (count == 0) return AMR_OK;
+    if (to_device && (st = s->impl->wait_side(which, comp))) return st;   // a side read of this buffer first
     return cuda_status(to_device ? cudaMemcpyAsync(dev, host, count * 4u, cudaMemcpyHostToDevice, s->impl->stream)
                                  : cudaMemcpyAsync(host, dev, count * 4u, cudaMemcpyDeviceToHost, s->impl->stream));
+}
+AMR_API int amr_sim_copy_to_host_side(amr_sim* s, int which, int comp, void* host, uint64_t count) {
+    if (!s || !host || which < 0 || which >= 6 || comp < 0 || comp >= 6) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    void* dev = nullptr;
+    uint64_t n = 0;
+    int st = b->buffer(which, comp, &dev, &n);
+    if (st) return st;
+    if (count > n) return AMR_ERR_INVALID;
+    if (count == 0) return AMR_OK;
+    cudaError_t e = cudaSuccess;
+    if (!b->side_stream) e = cudaStreamCreateWithFlags(&b->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !b->main_mark) e = cudaEventCreateWithFlags(&b->main_mark, cudaEventDisableTiming);
+    if (e == cudaSuccess && !b->side_done[which][comp])
+        e = cudaEventCreateWithFlags(&b->side_done[which][comp], cudaEventDisableTiming);
+    // after everything already enqueued on the simulation's stream ...
+    if (e == cudaSuccess) e = cudaEventRecord(b->main_mark, b->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->side_stream, b->main_mark, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, dev, count * 4u, cudaMemcpyDeviceToHost, b->side_stream);
+    // ... and before the next timestep or write of this buffer there
+    if (e == cudaSuccess) e = cudaEventRecord(b->side_done[which][comp], b->side_stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    b->side_pending[which][comp] = true;
+    return AMR_OK;
 }
 AMR_API int amr_sim_copy_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count) {
     return sim_copy(s, which, comp, const_cast<void*>(host), count, true);
@@ -682,6 +732,8 @@ AMR_API int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, ui
 AMR_API int amr_sim_event_record(amr_sim* s, int slot) {
     if (!s || slot < 0 || slot >= 16) return AMR_ERR_INVALID;
     SimBase* b = s->impl;
+    const int st0 = b->wait_side(-1, 0);   // the event follows side copies too
+    if (st0) return st0;
     if (!b->user_events[slot]) {
         const int st = cuda_status(cudaEventCreate(&b->user_events[slot]));
         if (st) return st;
@@ -723,7 +775,8 @@ int sim_kind(const SimBase* b) { return dynamic_cast<const WaveSim*>(b) ? AMR_SI
 AMR_API int amr_sim_save(amr_sim* s, const char* dir) {
     if (!s || !dir) return AMR_ERR_INVALID;
     SimBase* b = s->impl;
-    int st = cuda_status(cudaStreamSynchronize(b->stream));
+    int st = b->side_stream ? cuda_status(cudaStreamSynchronize(b->side_stream)) : AMR_OK;
+    if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
     if (st) return st;
     const std::string d(dir);
     const Octree& t = b->tree;
@@ -759,7 +812,8 @@ AMR_API int amr_sim_save(amr_sim* s, const char* dir) {
 AMR_API int amr_sim_load(amr_sim* s, const char* dir) {
     if (!s || !dir) return AMR_ERR_INVALID;
     SimBase* b = s->impl;
-    int st = cuda_status(cudaStreamSynchronize(b->stream));
+    int st = b->side_stream ? cuda_status(cudaStreamSynchronize(b->side_stream)) : AMR_OK;
+    if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
     if (st) return st;
     const std::string d(dir);
     const uint32_t slots = b->tree.max_slots();
@@ -807,8 +861,16 @@ AMR_API int amr_sim_load(amr_sim* s, const char* dir) {
     return AMR_OK;
 }
 
-AMR_API int amr_sim_timestep(amr_sim* s) { return s ? s->impl->timestep() : AMR_ERR_INVALID; }
-AMR_API int amr_sim_copy_bounds(amr_sim* s) { return s ? s->impl->copy_bounds() : AMR_ERR_INVALID; }
+AMR_API int amr_sim_timestep(amr_sim* s) {
+    if (!s) return AMR_ERR_INVALID;
+    const int st = s->impl->wait_side(-1, 0);
+    return st ? st : s->impl->timestep();
+}
+AMR_API int amr_sim_copy_bounds(amr_sim* s) {
+    if (!s) return AMR_ERR_INVALID;
+    const int st = s->impl->wait_side(-1, 0);
+    return st ? st : s->impl->copy_bounds();
+}
 AMR_API int amr_sim_rng(const amr_sim* s, int32_t* seed) {
     if (!s || !seed) return AMR_ERR_INVALID;
     *seed = s->impl->rng;
@@ -826,7 +888,9 @@ AMR_API int amr_sim_stream(amr_sim* s, void** stream) {
 }
 AMR_API int amr_sim_synchronize(amr_sim* s) {
     if (!s) return AMR_ERR_INVALID;
-    int st = cuda_status(cudaStreamSynchronize(s->impl->stream));
+    int st = s->impl->side_stream ? cuda_status(cudaStreamSynchronize(s->impl->side_stream)) : AMR_OK;
+    if (st) return st;
+    st = cuda_status(cudaStreamSynchronize(s->impl->stream));
     if (st) return st;
     int h = 0;
     if (cudaMemcpy(&h, s->impl->err_flag, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return AMR_ERR_CUDA;

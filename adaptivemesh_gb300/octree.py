@@ -115,6 +115,13 @@ class Sim:
         addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
         check(load().amr_sim_copy_to_host(self.h, which, comp, addr, n), "amr_sim_copy_to_host")
 
+    def copy_to_host_side(self, which: int, comp: int, host, count: int | None = None) -> None:
+        """The same copy on the simulation's side stream (amr_sim_copy_to_host_side): overlaps later
+        uploads of other buffers; later work touching this buffer waits for it."""
+        n = host.numel() if count is None and hasattr(host, "numel") else (count if count is not None else host.size)
+        addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
+        check(load().amr_sim_copy_to_host_side(self.h, which, comp, addr, n), "amr_sim_copy_to_host_side")
+
     def event_record(self, slot: int) -> None:
         check(load().amr_sim_event_record(self.h, slot), "amr_sim_event_record")
 

@@ -209,6 +209,11 @@ int amr_sim_buffer(amr_sim* s, int which, int comp, void** dev_ptr, uint64_t* co
  * (CUDA_memory.h:177-184).  `count` elements (4 bytes each) from the start of the buffer. */
 int amr_sim_copy_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count);
 int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, uint64_t count);
+/* The same read, on the simulation's side stream: it runs after the work already enqueued on the
+ * simulation's stream and may overlap what is enqueued afterwards (uploads of other buffers); the
+ * next timestep, copy_bounds, add_node or upload into this buffer waits for it.  Completion:
+ * amr_sim_synchronize. */
+int amr_sim_copy_to_host_side(amr_sim* sim, int which, int comp, void* host, uint64_t count);
 /* Checkpoint of a simulation into the existing directory `dir`: the octree arrays
  * (positions.bin, parent.bin, children.bin, boundaries.bin, lifetime.bin), every field buffer
  * amr_sim_buffer names (field_<which>_<comp>.bin), each the raw little-endian bytes of the whole
@@ -220,8 +225,9 @@ int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, uint64_t c
  * reference has no checkpoint of its own. */
 int amr_sim_save(amr_sim* sim, const char* dir);
 int amr_sim_load(amr_sim* sim, const char* dir);
-/* Timing events on the simulation's stream: record event `slot` (0..15), and read the
- * milliseconds between two recorded events (waits for the later one). */
+/* Timing events on the simulation's stream: record event `slot` (0..15) after all work enqueued
+ * so far (side-stream copies included), and read the milliseconds between two recorded events
+ * (waits for the later one). */
 int amr_sim_event_record(amr_sim* s, int slot);
 int amr_sim_event_elapsed(amr_sim* s, int first, int second, float* ms);
 int amr_sim_timestep(amr_sim* s);                                      /* the plugin's timestep() */

@@ -297,3 +297,49 @@ def test_wave_checkpoint_resume_with_regridding(am, cuda, tmp_path):
     resumed.synchronize()
     _assert_states_equal(_full_state(am, resumed, am.SIM_WAVE), want, "resumed wave plugin")
     resumed.close()
+
+
+def test_timestep_does_not_read_old_on_entry(am, cuda):
+    """BSSN_AMR_data::timestep starts with copy_back at substep 0, when every depth is active: every
+    cell of every live domain's old field is rewritten from new before anything reads it, so a
+    timestep's input is the new field alone (the benchmark uploads only that)."""
+    import torch
+    cfg = am.Config(16, 3, 100.0)
+    outs = []
+    for poison in (False, True):
+        sim, st, _ = _bssn_sim(am, cfg, "uneven", am.MODE_BATCHED)
+        if poison:
+            for k in range(6):
+                sim.tensor(am.Sim.OLD, k).fill_(float("nan"))
+            torch.cuda.synchronize()
+        sim.timestep()
+        sim.synchronize()
+        outs.append(_dump(am, sim, st, cfg))
+        sim.close()
+    for k in outs[0]:
+        if k != "rng":
+            _same(outs[0][k], outs[1][k], f"{k}: poisoned old")
+
+
+def test_side_reads_match_plain_reads(am, cuda):
+    """Results read on the side stream equal those read on the simulation's stream, also when the
+    next upload and timestep are enqueued right behind them."""
+    import torch
+    cfg = am.Config(16, 3, 100.0)
+    sim, st, metric = _bssn_sim(am, cfg, "uneven", am.MODE_GRAPH)
+    used = st["used_slots"]
+    n_in = used * cfg.inner_cells
+    side = [torch.empty(n_in, dtype=torch.int32, pin_memory=True) for _ in range(6)]
+    plain = [torch.empty(n_in, dtype=torch.int32, pin_memory=True) for _ in range(6)]
+    host_new = [torch.from_numpy(m).pin_memory() for m in metric]
+    for step in range(3):
+        for k in range(6):
+            sim.copy_to_device(am.Sim.NEW, k, host_new[k])
+        sim.timestep()
+        for k in range(6):
+            sim.copy_to_host(am.Sim.CHR, k, plain[k])
+            sim.copy_to_host_side(am.Sim.CHR, k, side[k])
+    sim.synchronize()
+    for k in range(6):
+        _same(side[k].numpy(), plain[k].numpy(), f"chr{k} side vs plain read")
+    sim.close()
