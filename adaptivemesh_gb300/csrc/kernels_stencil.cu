@@ -37,6 +37,8 @@ struct StencilShape {
     // SK_BSSN: per thread, the 13 generator prefixes (d0, m0, d1, m1, ..., c) and the six gradient words
     static constexpr size_t TABLE_BYTES = KIND == SK_BSSN ? (size_t)(13 + 6) * N * N * 4u : 0u;
     static constexpr size_t SMEM = RING_BYTES + BAR_BYTES + TABLE_BYTES;
+    static constexpr uint32_t Q = N >= 16 ? 4u : 2u;              // z-ranges per split domain
+    static_assert(N % Q == 0, "split domains into whole planes");
     static_assert(PLANE_BYTES % 16u == 0u, "bulk copies move whole planes of 16-byte multiples");
 };
 
@@ -183,37 +185,84 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
         }
     }
 
-    uint32_t seq0 = 0;   // sequence number of plane 0 of the current domain (ring slot = seq % R)
-    for (uint32_t item = blockIdx.x; item < a.n_items; item += gridDim.x) {
-        const uint32_t node = a.items ? a.items[item] : item;
-        const int depth = pos_depth(a.positions[node]);
-        if (depth == -1 || !active_depth(a.substep, (uint32_t)depth, a.max_depth)) continue;   // uniform in the CTA
-
-        if (tid == 0) {
-#pragma unroll 1
-            for (int q = 0; q < R && q < T; q++) {
-                const uint32_t s = (seq0 + q) % R;
-                mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
-#pragma unroll
-                for (int k = 0; k < NC; k++)
-                    bulk_g2s(ring + ((size_t)k * R + s) * PLANE, a.field[k] + ((size_t)node * T + q) * PLANE,
-                             S::PLANE_BYTES, &bars[s]);
-            }
+    // Work units, assigned round-robin.  Items are processed whole, except that when the last
+    // round would leave a quarter or more of the CTAs idle (rem <= 3/4 of the grid), its items are
+    // cut into Q z-ranges of N/Q interior planes so that it spreads over every CTA.  A unit streams
+    // its nz + 2P padded planes through the ring; thread 0 keeps the ring R planes ahead of the
+    // plane being computed, across unit boundaries.
+    constexpr uint32_t Q = S::Q, NZQ = N / Q;
+    const uint32_t G = gridDim.x;
+    const uint32_t rem = a.n_items % G;
+    const bool split = rem != 0u && Q * rem <= (Q - 1u) * G;
+    const uint32_t n_whole = split ? a.n_items - rem : a.n_items;
+    const uint32_t n_units = n_whole + (split ? rem * Q : 0u);
+    auto unit_of = [&](uint32_t u, uint32_t& item, uint32_t& z0, uint32_t& nz) {
+        if (u < n_whole) { item = u; z0 = 0; nz = N; }
+        else { const uint32_t v = u - n_whole; item = n_whole + v / Q; z0 = (v % Q) * NZQ; nz = NZQ; }
+    };
+    auto active_node = [&](uint32_t item, uint32_t& node, int& depth) {
+        node = a.items ? a.items[item] : item;
+        depth = pos_depth(a.positions[node]);
+        return depth != -1 && active_depth(a.substep, (uint32_t)depth, a.max_depth);
+    };
+    auto next_unit = [&](uint32_t u) {   // this CTA's next unit at or after u with an active domain
+        for (; u < n_units; u += G) {
+            uint32_t item, z0, nz, node;
+            int depth;
+            unit_of(u, item, z0, nz);
+            if (active_node(item, node, depth)) break;
         }
-        const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
+        return u;
+    };
+    // thread 0's request state: unit p_unit (its domain's first plane p_src and its plane count
+    // p_np), the next of its planes p_j, and the planes requested so far
+    uint32_t p_unit = n_units, p_j = 0, p_np = 0, issued = 0;
+    size_t p_src = 0;
+    auto open_unit = [&](uint32_t u) {
+        p_unit = next_unit(u);
+        if (p_unit < n_units) {
+            uint32_t item, z0, nz, node;
+            int depth;
+            unit_of(p_unit, item, z0, nz);
+            active_node(item, node, depth);
+            p_src = ((size_t)node * T + z0) * PLANE;
+            p_np = nz + 2u * P;
+        }
+    };
+    if (tid == 0) open_unit(blockIdx.x);
+    auto issue_upto = [&](uint32_t limit) {
+        while (issued < limit && p_unit < n_units) {
+            const uint32_t s = issued % R;
+            mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
+#pragma unroll
+            for (int k = 0; k < NC; k++)
+                bulk_g2s(ring + ((size_t)k * R + s) * PLANE, a.field[k] + p_src + (size_t)p_j * PLANE,
+                         S::PLANE_BYTES, &bars[s]);
+            issued++;
+            if (++p_j == p_np) { p_j = 0; open_unit(p_unit + G); }
+        }
+    };
 
-        uint32_t base = seq0 % R;   // ring slot of plane z, advanced incrementally
+    uint32_t g_base = 0;   // stream index of the current unit's first padded plane
+    for (uint32_t cu = next_unit(blockIdx.x); cu < n_units; cu = next_unit(cu + G)) {
+        uint32_t item, z0, nz, node;
+        int depth;
+        unit_of(cu, item, z0, nz);
+        active_node(item, node, depth);
+        const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
 #pragma unroll 1
-        for (uint32_t z = 0; z < (uint32_t)N; z++) {
-            // planes z .. z+2P of the padded domain must have landed
+        for (uint32_t zl = 0; zl < nz; zl++) {
+            const uint32_t g = g_base + zl, z = z0 + zl;   // planes g .. g+2P hold padded z .. z+2P
+            if (tid == 0) issue_upto(g + R);               // every plane below g is finished
+            // a unit's first window needs all its planes, later windows one more
             bool ok = true;
-            const int j_first = z == 0 ? 0 : 2 * P;
-            for (int j = j_first; j <= 2 * P; j++) {
-                const uint32_t sq = seq0 + z + j;
+            for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {
+                const uint32_t sq = g + j;
                 ok &= mbar_wait(&bars[sq % R], (sq / R) & 1u);
             }
             if (!ok) s_abort = 1;
             if (ok) {
+                const uint32_t base = g % R;
                 uint32_t slot[2 * P + 1];
 #pragma unroll
                 for (int j = 0; j <= 2 * P; j++) slot[j] = base + j >= (uint32_t)R ? base + j - R : base + j;
@@ -268,23 +317,16 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                     for (int k = 0; k < 6; k++) a.chr[k][o] = out[k];
                 }
             }
-            __syncthreads();   // every thread is done with plane z: its slot may be refilled
-            if (s_abort) break;
-            base = base + 1 == (uint32_t)R ? 0u : base + 1;
-            if (tid == 0 && z + R < (uint32_t)T) {
-                const uint32_t q = z + R, sq = seq0 + q, s = sq % R;
-                mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
-#pragma unroll
-                for (int k = 0; k < NC; k++)
-                    bulk_g2s(ring + ((size_t)k * R + s) * PLANE, a.field[k] + ((size_t)node * T + q) * PLANE,
-                             S::PLANE_BYTES, &bars[s]);
+            __syncthreads();   // every thread is done with plane g: its slot may be refilled
+            if (s_abort) {
+                if (tid == 0) {
+                    atomicExch(a.err, 1);
+                    for (uint32_t sq = g; sq < issued; sq++) mbar_wait(&bars[sq % R], (sq / R) & 1u);   // drain (bounded)
+                }
+                return;
             }
         }
-        if (s_abort) {
-            if (tid == 0) atomicExch(a.err, 1);
-            return;
-        }
-        seq0 += T;
+        g_base += nz + 2u * P;
     }
 }
 
