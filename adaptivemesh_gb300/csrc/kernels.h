@@ -36,6 +36,11 @@ struct StencilArgs {
     uint32_t substep, max_depth;
     Geo geo;
     int* err;                     // set to 1 if a bounded wait gave up
+    // Restriction of leaves fused into the pass (SK_BSSN): with children set, a domain without
+    // children reads its planes from leaf_src[k] and writes them to field[k] (old <- new,
+    // AMR.h:961-996), while a domain with children reads field[k] (restricted beforehand).
+    const float* leaf_src[6];
+    const int32_t* children;
 };
 
 template <int N, int P, int KIND>

@@ -214,10 +214,20 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
         }
         return u;
     };
-    // thread 0's request state: unit p_unit (its domain's first plane p_src and its plane count
-    // p_np), the next of its planes p_j, and the planes requested so far
+    // A leaf domain when the restriction is fused: no children (its planes come from leaf_src).
+    auto fused_leaf = [&](uint32_t node) {
+        if (KIND != SK_BSSN || !a.children) return false;
+        bool leaf = true;
+#pragma unroll
+        for (int c = 0; c < 8; c++) leaf &= a.children[node * 8u + c] == -1;
+        return leaf;
+    };
+    // thread 0's request state: unit p_unit (its domain's first plane p_src, its plane count p_np,
+    // whether its planes come from leaf_src), the next of its planes p_j, and the planes requested
+    // so far; `storing` when bulk stores out of the ring may still be reading it
     uint32_t p_unit = n_units, p_j = 0, p_np = 0, issued = 0;
     size_t p_src = 0;
+    bool p_leaf = false, storing = false;
     auto open_unit = [&](uint32_t u) {
         p_unit = next_unit(u);
         if (p_unit < n_units) {
@@ -227,16 +237,18 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
             active_node(item, node, depth);
             p_src = ((size_t)node * T + z0) * PLANE;
             p_np = nz + 2u * P;
+            p_leaf = fused_leaf(node);
         }
     };
     if (tid == 0) open_unit(blockIdx.x);
     auto issue_upto = [&](uint32_t limit) {
+        if (storing && issued < limit && p_unit < n_units) { bulk_wait_read(); storing = false; }
         while (issued < limit && p_unit < n_units) {
             const uint32_t s = issued % R;
             mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
 #pragma unroll
             for (int k = 0; k < NC; k++)
-                bulk_g2s(ring + ((size_t)k * R + s) * PLANE, a.field[k] + p_src + (size_t)p_j * PLANE,
+                bulk_g2s(ring + ((size_t)k * R + s) * PLANE, (p_leaf ? a.leaf_src[k] : a.field[k]) + p_src + (size_t)p_j * PLANE,
                          S::PLANE_BYTES, &bars[s]);
             issued++;
             if (++p_j == p_np) { p_j = 0; open_unit(p_unit + G); }
@@ -250,6 +262,7 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
         unit_of(cu, item, z0, nz);
         active_node(item, node, depth);
         const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
+        const bool leaf = tid == 0 && fused_leaf(node);
 #pragma unroll 1
         for (uint32_t zl = 0; zl < nz; zl++) {
             const uint32_t g = g_base + zl, z = z0 + zl;   // planes g .. g+2P hold padded z .. z+2P
@@ -261,6 +274,23 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                 ok &= mbar_wait(&bars[sq % R], (sq / R) & 1u);
             }
             if (!ok) s_abort = 1;
+            if (ok && leaf) {
+                // fused restriction: each padded plane of the leaf goes to field[k] once -- by the
+                // unit whose interior it is, the end units also taking the ghost planes beyond
+                const uint32_t base_s = g % R;
+                for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {
+                    const uint32_t jj = zl + (uint32_t)j;   // plane index within the unit
+                    const bool own = (jj >= P && jj < nz + P) || (z0 == 0 && jj < P) || (z0 + nz == N && jj >= nz + P);
+                    if (!own) continue;
+                    const uint32_t sl = base_s + (uint32_t)j >= (uint32_t)R ? base_s + j - R : base_s + j;
+#pragma unroll
+                    for (int k = 0; k < NC; k++)
+                        bulk_s2g(const_cast<float*>(a.field[k]) + ((size_t)node * T + z0 + jj) * PLANE,
+                                 ring + ((size_t)k * R + sl) * PLANE, S::PLANE_BYTES);
+                    storing = true;
+                }
+                bulk_commit();
+            }
             if (ok) {
                 const uint32_t base = g % R;
                 uint32_t slot[2 * P + 1];
@@ -322,12 +352,14 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                 if (tid == 0) {
                     atomicExch(a.err, 1);
                     for (uint32_t sq = g; sq < issued; sq++) mbar_wait(&bars[sq % R], (sq / R) & 1u);   // drain (bounded)
+                    bulk_wait();
                 }
                 return;
             }
         }
         g_base += nz + 2u * P;
     }
+    if (tid == 0) bulk_wait();   // stores out of the ring done before the CTA's shared memory goes
 }
 
 // ---------------------------------------------------------------- launch

@@ -66,7 +66,7 @@ public:
         if (e == cudaSuccess) e = dev_alloc(&d_positions, s);
         if (e == cudaSuccess) e = dev_alloc(&d_children, (size_t)s * 8u);
         if (e == cudaSuccess) e = dev_alloc(&d_boundaries, (size_t)s * 6u);
-        if (e == cudaSuccess) e = dev_alloc(&d_items, (size_t)s << kDepthLimit);
+        if (e == cudaSuccess) e = dev_alloc(&d_items, (size_t)s << (kDepthLimit + 1));   // active and parent lists
         if (e == cudaSuccess) { err_flag = device_error_flag(); if (!err_flag) e = cudaErrorMemoryAllocation; }
         if (e == cudaSuccess) {
             // set the kernels' shared-memory limits now, outside any later stream capture
@@ -129,6 +129,8 @@ public:
         std::vector<uint32_t> all;
         item_offset.assign(nsub, 0);
         item_count.assign(nsub, 0);
+        parent_offset.assign(nsub, 0);
+        parent_count.assign(nsub, 0);
         for (uint32_t s = 0; s < nsub; s++) {
             item_offset[s] = (uint32_t)all.size();
             for (uint32_t i = 0; i < used; i++) {
@@ -136,6 +138,13 @@ public:
                 if (d != -1 && (s & ((1u << (md - (uint32_t)d)) - 1u)) == 0u) all.push_back(i);
             }
             item_count[s] = (uint32_t)all.size() - item_offset[s];
+            parent_offset[s] = (uint32_t)all.size();   // the active domains that have children
+            for (uint32_t k = item_offset[s]; k < item_offset[s] + item_count[s]; k++) {
+                bool parent = false;
+                for (int c = 0; c < 8; c++) parent |= tree.children()[(size_t)all[k] * 8u + c] != -1;
+                if (parent) all.push_back(all[k]);
+            }
+            parent_count[s] = (uint32_t)all.size() - parent_offset[s];
         }
         cudaError_t e = cudaMemcpyAsync(d_items, all.data(), all.size() * 4u, cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -204,7 +213,7 @@ public:
     int32_t* d_children = nullptr;
     uint64_t* d_boundaries = nullptr;
     uint32_t* d_items = nullptr;
-    std::vector<uint32_t> item_offset, item_count;
+    std::vector<uint32_t> item_offset, item_count, parent_offset, parent_count;
     bool items_valid = false;
     bool graph_valid = false;
     bool capturing = false;
@@ -302,11 +311,16 @@ public:
         if ((st = build_items())) return st;
         f.ncomp = 6;
         for (int k = 0; k < 6; k++) { f.old_f[k] = old6[k]; f.new_f[k] = new6[k]; }
-        return check(launch_copy_new_to_old(dims, f, d_positions, d_children, d_items + item_offset[s], item_count[s], s,
-                                            md, stream));
+        // With the fused predictor, leaves restrict themselves as the predictor streams their planes
+        // (old <- new plane by plane); only the domains with children are restricted here.
+        const bool fused = bssn_fused_supported(&cfg);
+        if ((fused ? parent_count[s] : item_count[s]) == 0u) return AMR_OK;   // nothing to launch
+        return check(launch_copy_new_to_old(dims, f, d_positions, d_children,
+                                            d_items + (fused ? parent_offset[s] : item_offset[s]),
+                                            fused ? parent_count[s] : item_count[s], s, md, stream));
     }
     int modify_nodes() override { return AMR_OK; }              // BSSN.h:139-142
-    int predictor() override { return derivatives(old6, seed_slot(0)); }
+    int predictor() override { return derivatives(old6, seed_slot(0), true); }
     int corrector() override { return derivatives(new6, seed_slot(1)); }
     int copy_bounds() override {                                 // BSSN.h:149-153
         int st = sync_octree();
@@ -361,7 +375,8 @@ private:
     }
 
     // metric_derivatives_noncovariant + compute_raised_christoffel_symbols (BSSN.h:38-102)
-    int derivatives(float* const* g, const int32_t* dev_seeds) {
+    // restrict_leaves: the predictor's pass also performs the leaves' part of copy_back.
+    int derivatives(float* const* g, const int32_t* dev_seeds, bool restrict_leaves = false) {
         int st = sync_octree();
         if (st) return st;
         const uint32_t s = tree.timer(), md = (uint32_t)tree.read_max_depth(), used = tree.curr_used_slots();
@@ -401,6 +416,10 @@ private:
         a.items = d_items + item_offset[s];
         a.n_items = item_count[s];
         for (int k = 0; k < 6; k++) { a.field[k] = g[k]; a.grad[k] = dmet6[k]; a.lap[k] = ricci6[k]; a.chr[k] = chr6[k]; }
+        if (restrict_leaves) {
+            a.children = d_children;
+            for (int k = 0; k < 6; k++) a.leaf_src[k] = new6[k];
+        }
         time_begin();
         st = check(launch_stencil(cfg, SK_BSSN, a, stencil_grid(cfg, SK_BSSN, a.n_items), stream));
         time_end();
