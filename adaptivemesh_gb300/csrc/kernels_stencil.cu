@@ -224,10 +224,10 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
     };
     // thread 0's request state: unit p_unit (its domain's first plane p_src, its plane count p_np,
     // whether its planes come from leaf_src), the next of its planes p_j, and the planes requested
-    // so far; `storing` when bulk stores out of the ring may still be reading it
+    // so far
     uint32_t p_unit = n_units, p_j = 0, p_np = 0, issued = 0;
     size_t p_src = 0;
-    bool p_leaf = false, storing = false;
+    bool p_leaf = false;
     auto open_unit = [&](uint32_t u) {
         p_unit = next_unit(u);
         if (p_unit < n_units) {
@@ -242,7 +242,6 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
     };
     if (tid == 0) open_unit(blockIdx.x);
     auto issue_upto = [&](uint32_t limit) {
-        if (storing && issued < limit && p_unit < n_units) { bulk_wait_read(); storing = false; }
         while (issued < limit && p_unit < n_units) {
             const uint32_t s = issued % R;
             mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
@@ -262,7 +261,7 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
         unit_of(cu, item, z0, nz);
         active_node(item, node, depth);
         const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
-        const bool leaf = tid == 0 && fused_leaf(node);
+        const bool leaf = fused_leaf(node);
 #pragma unroll 1
         for (uint32_t zl = 0; zl < nz; zl++) {
             const uint32_t g = g_base + zl, z = z0 + zl;   // planes g .. g+2P hold padded z .. z+2P
@@ -274,9 +273,12 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                 ok &= mbar_wait(&bars[sq % R], (sq / R) & 1u);
             }
             if (!ok) s_abort = 1;
-            if (ok && leaf) {
-                // fused restriction: each padded plane of the leaf goes to field[k] once -- by the
-                // unit whose interior it is, the end units also taking the ghost planes beyond
+            // fused restriction: each padded plane of a leaf goes to field[k] once -- by the unit
+            // whose interior it is, the end units also taking the ghost planes beyond -- stored out
+            // of the ring by lane 0 of one warp per plane (in turn), which waits for the stores to
+            // have read the ring before the plane's closing barrier
+            const bool storer = leaf && tid == 32u * (g % (NN / 32u));
+            if (ok && storer) {
                 const uint32_t base_s = g % R;
                 for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {
                     const uint32_t jj = zl + (uint32_t)j;   // plane index within the unit
@@ -287,7 +289,6 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                     for (int k = 0; k < NC; k++)
                         bulk_s2g(const_cast<float*>(a.field[k]) + ((size_t)node * T + z0 + jj) * PLANE,
                                  ring + ((size_t)k * R + sl) * PLANE, S::PLANE_BYTES);
-                    storing = true;
                 }
                 bulk_commit();
             }
@@ -347,19 +348,20 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                     for (int k = 0; k < 6; k++) a.chr[k][o] = out[k];
                 }
             }
+            if (storer) bulk_wait_read();
             __syncthreads();   // every thread is done with plane g: its slot may be refilled
             if (s_abort) {
                 if (tid == 0) {
                     atomicExch(a.err, 1);
                     for (uint32_t sq = g; sq < issued; sq++) mbar_wait(&bars[sq % R], (sq / R) & 1u);   // drain (bounded)
-                    bulk_wait();
                 }
+                bulk_wait();
                 return;
             }
         }
         g_base += nz + 2u * P;
     }
-    if (tid == 0) bulk_wait();   // stores out of the ring done before the CTA's shared memory goes
+    bulk_wait();   // this thread's stores out of the ring are complete
 }
 
 // ---------------------------------------------------------------- launch
