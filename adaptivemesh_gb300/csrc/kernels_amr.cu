@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(kBlock) k_copy_new_to_old(const __grid_constan
         return;
     }
     const uint32_t end = (blockIdx.z + 1u) * CELLS / kSlabs;
+#pragma unroll 4   // independent cells: several gathers in flight per thread
     for (uint32_t cell = blockIdx.z * CELLS / kSlabs + threadIdx.x; cell < end; cell += kBlock) {
         const uint32_t x = cell % T, y = (cell / T) % T, z = cell / (T * T);
         const uint32_t tx = (x - P) / H, ty = (y - P) / H, tz = (z - P) / H;   // ghosts wrap to >= 2

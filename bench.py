@@ -119,6 +119,12 @@ def fused_kernel_bytes_per_domain() -> int:
     return 6 * 4 * (N ** 3 + 6 * P * N ** 2) + 18 * 4 * N ** 3
 
 
+def fused_restriction_bytes_per_leaf() -> int:
+    """Added to a leaf domain in the predictor pass, which also performs its restriction: the six
+    old fields' padded cubes written (the padded planes it reads anyway come from new)."""
+    return 6 * 4 * (N + 2 * P) ** 3
+
+
 class CpuPort:
     """The oracle's restatement of BSSN_AMR_data::timestep on the host cores (OpenMP over
     domains), run on a bounded sample of the workload's leaf domains."""
@@ -321,9 +327,14 @@ def main() -> None:
     k_ms, k_n = sim.kernel_timing()
     sim.enable_kernel_timing(False)
     # domains processed per timestep by the fused kernel: active domains of each substep, twice
+    # (predictor and corrector); the predictor's leaves also write their restriction
     depths = [int(p) >> 27 for p in st["positions"][:used]]
-    per_step = sum(2 * sum(1 for d in depths if (s & ((1 << (md - d)) - 1)) == 0) for s in range(1 << md))
-    bytes_per_launch = fused_kernel_bytes_per_domain() * per_step / (2 << md)
+    leaf = [all(c == -1 for c in st["children"][8 * i:8 * i + 8]) for i in range(used)]
+    active = [[i for i, d in enumerate(depths) if (s & ((1 << (md - d)) - 1)) == 0] for s in range(1 << md)]
+    per_step = sum(2 * len(a) for a in active)
+    leaves_per_step = sum(sum(1 for i in a if leaf[i]) for a in active)
+    bytes_per_launch = (fused_kernel_bytes_per_domain() * per_step +
+                        fused_restriction_bytes_per_leaf() * leaves_per_step) / (2 << md)
     achieved = bytes_per_launch / (k_ms / k_n / 1e3) / 1e9 if k_n else None
     pk = peaks()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -332,8 +343,9 @@ def main() -> None:
                 "avg_launch_ms": k_ms / k_n if k_n else None, "launches_timed": k_n}
     try:   # DRAM bytes per domain from an ncu capture of the same kernel and workload, scaled per launch
         with open(os.path.join(ROOT, "profiles", "k_stencil_bssn_16p3.traffic.json")) as f:
-            per_domain = json.load(f)["dram_bytes_per_domain"]
-        roofline["traffic"] = per_domain * per_step / (2 << md)
+            tr = json.load(f)
+        roofline["traffic"] = (tr["corrector_dram_bytes_per_domain"] * per_step / 2 +
+                               tr["predictor_dram_bytes_per_domain"] * per_step / 2) / (2 << md)
     except (OSError, KeyError, ValueError):
         pass
 
