@@ -12,8 +12,8 @@ Metric: zone-cycles/s = 512 * 16^3 leaf zones x steps / seconds (covered parents
   e2e    the same metric through the C ABI with host buffers: every step uploads its input (the
          new metric; the old one is rewritten from it by the step's first phase) from pinned host
          memory and downloads new metric, gradients, Christoffel symbols and traces to pinned host
-         memory, inside the timed region (the derived outputs on the simulation's side stream,
-         overlapping the next upload)
+         memory, inside the timed region (downloads on the simulation's side stream, the derived
+         outputs overlapping the next upload)
 
 `--impl reference` times the reference path on the CPU: the reference has no CPU solver, so
 this is the oracle's restatement of BSSN_AMR_data::timestep (OpenMP over domains), on a bounded
@@ -260,13 +260,11 @@ def main() -> None:
             sim.copy_to_device(w, k, h)
 
     def download():
-        # `new` on the simulation's stream (the next upload overwrites it); the derived outputs on
-        # its side stream, overlapping the next step's upload (the next timestep waits for them)
+        # on the simulation's side stream: the next step's upload of `new` waits only for the
+        # download of `new`, and overlaps the derived outputs' download (the next timestep waits
+        # for all of them)
         for (w, k, n), h in zip(outs, h_out):
-            if w == am.Sim.NEW:
-                sim.copy_to_host(w, k, h)
-            else:
-                sim.copy_to_host_side(w, k, h)
+            sim.copy_to_host_side(w, k, h)
 
     upload()
     sim.synchronize()
