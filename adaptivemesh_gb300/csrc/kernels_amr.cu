@@ -303,19 +303,45 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
     const uint64_t stage_base = ((uint64_t)slot * 3u + (face - 3u)) * (N * N);   // used for lower faces only
     const uint64_t slot_base = (uint64_t)slot * G::CELLS;
 
+    // The source offsets of this thread's box elements are the same for every component: at
+    // small sizes they are computed once and kept in registers.
+    constexpr uint32_t EPT = (BOX + kBlock - 1) / kBlock;   // box elements per thread, at most
+    constexpr bool kCached = EPT <= 8;
+    uint32_t e_gi[kCached ? EPT : 1];
+    if (kCached) {
+        uint32_t bx = bx0, by = by0, bz = bz0;
+#pragma unroll
+        for (uint32_t e = 0; e < EPT; e++) {
+            e_gi[e] = bx + (by + bz * T) * T;
+            bx += A; by += B; bz += C;
+            if (bx >= sy) { bx -= sy; by++; }
+            if (by >= ext[1]) { by -= ext[1]; bz++; }
+        }
+    }
     // Component k's box goes to buffer k & 1 by asynchronous copies, issued one component ahead.
     auto issue = [&](int k) {
         float* buf = sbox + (k & 1) * 2u * BOX;
         const float* go = f.old_f[k] + src0;
         const float* gn = f.new_f[k] + src0;
-        uint32_t bx = bx0, by = by0, bz = bz0;
-        for (uint32_t i = threadIdx.x; i < box; i += kBlock) {
-            const uint32_t gi = bx + (by + bz * T) * T;
-            cp_async4(buf + i, go + gi);
-            cp_async4(buf + BOX + i, gn + gi);
-            bx += A; by += B; bz += C;
-            if (bx >= sy) { bx -= sy; by++; }
-            if (by >= ext[1]) { by -= ext[1]; bz++; }
+        if (kCached) {
+#pragma unroll
+            for (uint32_t e = 0; e < EPT; e++) {
+                const uint32_t i = threadIdx.x + e * kBlock;
+                if (i < box) {
+                    cp_async4(buf + i, go + e_gi[kCached ? e : 0]);
+                    cp_async4(buf + BOX + i, gn + e_gi[kCached ? e : 0]);
+                }
+            }
+        } else {
+            uint32_t bx = bx0, by = by0, bz = bz0;
+            for (uint32_t i = threadIdx.x; i < box; i += kBlock) {
+                const uint32_t gi = bx + (by + bz * T) * T;
+                cp_async4(buf + i, go + gi);
+                cp_async4(buf + BOX + i, gn + gi);
+                bx += A; by += B; bz += C;
+                if (bx >= sy) { bx -= sy; by++; }
+                if (by >= ext[1]) { by -= ext[1]; bz++; }
+            }
         }
         cp_async_commit();
     };
