@@ -80,7 +80,7 @@ struct FieldSet {
 };
 cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* positions, const int32_t* children,
                                    const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
-                                   cudaStream_t st);
+                                   cudaStream_t st, bool parents_only = false);
 cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t child, int32_t parent, cudaStream_t st);
 // Staging for the ghost fill (the innermost layer of the three lower faces, old and new):
 // 2 * ncomp * 3 * n^2 floats per slot.

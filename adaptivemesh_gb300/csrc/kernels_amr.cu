@@ -16,12 +16,13 @@ constexpr int kBlock = 256;
 inline uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kBlock - 1) / kBlock); }
 
 // ---------------------------------------------------------------- restriction, AMR.h:961-996
-// One CTA per (domain, component, slab): the padded cube is cut into kSlabs contiguous ranges so a
+// One CTA per (domain, component, slab): the padded cube is cut into gridDim.z contiguous ranges so a
 // domain with children (8 gathers per covered cell) spreads over as many CTAs as a leaf.  A domain
 // without children is a straight copy of its range (16-byte aligned: 128-bit loads and stores,
 // several in flight per thread); otherwise every cell covered by a child becomes the mean of the
 // child's 2x2x2 cells and the rest is copied.
-constexpr uint32_t kSlabs = 4;
+constexpr uint32_t kSlabs = 4;          // slabs per domain of a launch over all active domains
+constexpr uint32_t kParentSlabs = 16;   // ... of a launch over domains with children only (gathers)
 template <int N, int P>
 __global__ void __launch_bounds__(kBlock) k_copy_new_to_old(const __grid_constant__ FieldSet f, const uint32_t* __restrict__ positions,
                                                         const int32_t* __restrict__ children,
@@ -41,10 +42,10 @@ __global__ void __launch_bounds__(kBlock) k_copy_new_to_old(const __grid_constan
     for (int i = 0; i < 8; i++) { ch[i] = children[slot * 8u + i]; any_child |= ch[i] != -1; }
     if (!any_child) {   // kU vectors per thread in flight before the first store
         constexpr uint32_t V = CELLS / 4, kU = 8;
-        const uint32_t end = (blockIdx.z + 1u) * V / kSlabs;
+        const uint32_t end = (blockIdx.z + 1u) * V / gridDim.z;
         const float4* s4 = reinterpret_cast<const float4*>(own);
         float4* d4 = reinterpret_cast<float4*>(dst);
-        for (uint32_t base = blockIdx.z * V / kSlabs + threadIdx.x; base < end; base += kU * kBlock) {
+        for (uint32_t base = blockIdx.z * V / gridDim.z + threadIdx.x; base < end; base += kU * kBlock) {
             float4 b[kU];
 #pragma unroll
             for (uint32_t i = 0; i < kU; i++)
@@ -55,24 +56,29 @@ __global__ void __launch_bounds__(kBlock) k_copy_new_to_old(const __grid_constan
         }
         return;
     }
-    const uint32_t end = (blockIdx.z + 1u) * CELLS / kSlabs;
+    const uint32_t end = (blockIdx.z + 1u) * CELLS / gridDim.z;
 #pragma unroll 4   // independent cells: several gathers in flight per thread
-    for (uint32_t cell = blockIdx.z * CELLS / kSlabs + threadIdx.x; cell < end; cell += kBlock) {
+    for (uint32_t cell = blockIdx.z * CELLS / gridDim.z + threadIdx.x; cell < end; cell += kBlock) {
         const uint32_t x = cell % T, y = (cell / T) % T, z = cell / (T * T);
         const uint32_t tx = (x - P) / H, ty = (y - P) / H, tz = (z - P) / H;   // ghosts wrap to >= 2
         const int32_t child = (tx < 2u && ty < 2u && tz < 2u) ? ch[tx + ty * 2u + tz * 4u] : -1;
-        if (child == -1) { dst[cell] = own[cell]; continue; }
-        const uint32_t cx = ((x - P) * 2u) % N + P, cy = ((y - P) * 2u) % N + P, cz = ((z - P) * 2u) % N + P;
-        const float* c = src + (size_t)child * CELLS + (cz * T + cy) * T + cx;
-        constexpr uint32_t T2 = T * T;
-        float s = __fadd_rn(c[0], c[1]);
-        s = __fadd_rn(s, c[T]);
-        s = __fadd_rn(s, c[T + 1]);
-        s = __fadd_rn(s, c[T2]);
-        s = __fadd_rn(s, c[T2 + 1]);
-        s = __fadd_rn(s, c[T2 + T]);
-        s = __fadd_rn(s, c[T2 + T + 1]);
-        dst[cell] = __fmul_rn(s, .125f);
+        float v;
+        if (child == -1) {
+            v = own[cell];
+        } else {
+            const uint32_t cx = ((x - P) * 2u) % N + P, cy = ((y - P) * 2u) % N + P, cz = ((z - P) * 2u) % N + P;
+            const float* c = src + (size_t)child * CELLS + (cz * T + cy) * T + cx;
+            constexpr uint32_t T2 = T * T;
+            float s = __fadd_rn(c[0], c[1]);
+            s = __fadd_rn(s, c[T]);
+            s = __fadd_rn(s, c[T + 1]);
+            s = __fadd_rn(s, c[T2]);
+            s = __fadd_rn(s, c[T2 + 1]);
+            s = __fadd_rn(s, c[T2 + T]);
+            s = __fadd_rn(s, c[T2 + T + 1]);
+            v = __fmul_rn(s, .125f);
+        }
+        dst[cell] = v;
     }
 }
 
@@ -411,9 +417,9 @@ __global__ void __launch_bounds__(256) k_ghost_commit(const __grid_constant__ Fi
 // ---------------------------------------------------------------- launchers
 cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* positions, const int32_t* children,
                                    const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
-                                   cudaStream_t st) {
+                                   cudaStream_t st, bool parents_only) {
     if (n_items == 0 || f.ncomp == 0) return cudaSuccess;
-    const dim3 grid(n_items, (uint32_t)f.ncomp, kSlabs);
+    const dim3 grid(n_items, (uint32_t)f.ncomp, parents_only ? kParentSlabs : kSlabs);
 #define AMR_RESTRICT(N, P) \
     if (d.n == N && d.p == P) { k_copy_new_to_old<N, P><<<grid, kBlock, 0, st>>>(f, positions, children, items, substep, max_depth); return cudaGetLastError(); }
     AMR_FOR_EACH_CONFIG(AMR_RESTRICT)

@@ -317,7 +317,7 @@ public:
         if ((fused ? parent_count[s] : item_count[s]) == 0u) return AMR_OK;   // nothing to launch
         return check(launch_copy_new_to_old(dims, f, d_positions, d_children,
                                             d_items + (fused ? parent_offset[s] : item_offset[s]),
-                                            fused ? parent_count[s] : item_count[s], s, md, stream));
+                                            fused ? parent_count[s] : item_count[s], s, md, stream, fused));
     }
     int modify_nodes() override { return AMR_OK; }              // BSSN.h:139-142
     int predictor() override { return derivatives(old6, seed_slot(0), true); }
