@@ -318,9 +318,9 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                     const Sym g{ring[0 * R * PLANE + cz], ring[1 * (size_t)R * PLANE + cz], ring[2 * (size_t)R * PLANE + cz],
                                 ring[3 * (size_t)R * PLANE + cz], ring[4 * (size_t)R * PLANE + cz], ring[5 * (size_t)R * PLANE + cz]};
                     const Sym ginv = sym_inverse(g);
-                    // two components per pass: six unrolled copies of the body overflow the
+                    // three components per pass: six unrolled copies of the body overflow the
                     // instruction cache, a rolled loop spends instructions on addressing
-#pragma unroll 2
+#pragma unroll 3
                     for (int k = 0; k < 6; k++) {
                         const float* base = ring + (size_t)k * R * PLANE;
                         auto pl = [&](int j) { return base + (size_t)slot[j] * PLANE; };
