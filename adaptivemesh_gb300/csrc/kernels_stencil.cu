@@ -33,7 +33,11 @@ struct StencilShape {
     static constexpr uint32_t PLANE = (uint32_t)(T * T);         // floats per plane
     static constexpr uint32_t PLANE_BYTES = PLANE * 4u;
     static constexpr size_t RING_BYTES = (size_t)NC * R * PLANE_BYTES;
-    static constexpr size_t BAR_BYTES = (size_t)R * 8u;
+    static constexpr size_t BAR_BYTES = (size_t)R * 8u * (KIND == SK_BSSN ? 2u : 1u);   // full (+ empty) per slot
+    // SK_BSSN runs warp-specialised: ceil(N^2 / 32) compute warps (thread (x, y) per column) and one
+    // producer warp that streams the planes
+    static constexpr uint32_t CW = (uint32_t)(N * N + 31) / 32u;
+    static constexpr uint32_t THREADS = KIND == SK_BSSN ? 32u * (CW + 1u) : (uint32_t)(N * N);
     // SK_BSSN: per thread, the 13 generator prefixes (d0, m0, d1, m1, ..., c) and the six gradient words
     static constexpr size_t TABLE_BYTES = KIND == SK_BSSN ? (size_t)(13 + 6) * N * N * 4u : 0u;
     static constexpr size_t SMEM = RING_BYTES + BAR_BYTES + TABLE_BYTES;
@@ -364,18 +368,227 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
     bulk_wait();   // this thread's stores out of the ring are complete
 }
 
+// ---------------------------------------------------------------- the fused BSSN pass, warp-specialised
+// Work units and plane stream as in k_stencil, but the planes are requested by a producer warp:
+// ring slot s has a `full` barrier (the producer's expected bytes, completed by the copies) and an
+// `empty` barrier (one arrival per compute warp when it is done with the plane in it).  Compute
+// warps never wait for each other, only for data; the producer waits only for the slot it refills.
+template <int N, int P>
+__device__ __forceinline__ void bssn_cell(const StencilArgs& a, const float* ring, const uint32_t* slot, int c0,
+                                          uint32_t x, uint32_t y, uint32_t z, uint32_t zg, size_t o, float dx1,
+                                          float dx2, uint32_t tid, const int32_t* s_pre, uint32_t* s_grad) {
+    using S = StencilShape<N, P, SK_BSSN>;
+    constexpr int T = S::T, R = S::R;
+    constexpr uint32_t PLANE = S::PLANE, NN = N * N;
+    const size_t cz = (size_t)slot[P] * PLANE + c0;
+    const Sym g{ring[0 * R * PLANE + cz], ring[1 * (size_t)R * PLANE + cz], ring[2 * (size_t)R * PLANE + cz],
+                ring[3 * (size_t)R * PLANE + cz], ring[4 * (size_t)R * PLANE + cz], ring[5 * (size_t)R * PLANE + cz]};
+    const Sym ginv = sym_inverse(g);
+    // three components per pass: six unrolled copies of the body overflow the instruction cache,
+    // a rolled loop spends instructions on addressing
+#pragma unroll 3
+    for (int k = 0; k < 6; k++) {
+        const float* base = ring + (size_t)k * R * PLANE;
+        auto pl = [&](int j) { return base + (size_t)slot[j] * PLANE; };
+        float gx, gy, gz, hx, hy, hz;
+        fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
+        int32_t rd = cell_rng_at(s_pre[(2 * k) * NN + tid], zg);
+        // the Hessians are quantised exactly as the reference writes and re-reads them
+        const Cf3Quantised hq = cf3_encode_quantised(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
+        const uint32_t gk = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
+        a.grad[k][o] = gk;
+        s_grad[k * NN + tid] = gk;
+        const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
+        int32_t rm = cell_rng_at(s_pre[(2 * k + 1) * NN + tid], zg);
+        const Cf3Quantised oq = cf3_encode_quantised(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
+        const Sym H{hq.value.x, oq.value.x, oq.value.y, hq.value.y, oq.value.z, hq.value.z};   // tensors.h:430-435
+        a.lap[k][o] = trace_contra(H, ginv);
+    }
+    uint32_t G[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) G[k] = s_grad[k * NN + tid];
+    int32_t rc = cell_rng_at(s_pre[12 * NN + tid], zg);
+    uint32_t out[6];
+    christoffel_cell(G, a.christoffel_mode == AMR_CHRISTOFFEL_RAISED ? ginv : g, rc, out);
+#pragma unroll
+    for (int k = 0; k < 6; k++) a.chr[k][o] = out[k];
+}
+
+template <int N, int P>
+__global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <= 256 ? 2 : 1)
+    k_stencil_bssn(const __grid_constant__ StencilArgs a) {
+    using S = StencilShape<N, P, SK_BSSN>;
+    constexpr int T = S::T, NC = 6, R = S::R;
+    constexpr uint32_t PLANE = S::PLANE, NN = N * N, CW = S::CW;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* ring = reinterpret_cast<float*>(smem_raw);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + S::RING_BYTES);
+    uint64_t* empty = full + R;
+    int32_t* s_pre = reinterpret_cast<int32_t*>(smem_raw + S::RING_BYTES + S::BAR_BYTES);   // [13][NN]
+    uint32_t* s_grad = reinterpret_cast<uint32_t*>(s_pre + 13 * NN);                       // [6][NN]
+    __shared__ volatile int s_abort;
+
+    const uint32_t tid = threadIdx.x, warp = tid / 32u, lane = tid % 32u;
+    if (tid == 0) {
+        for (int r = 0; r < R; r++) { mbar_init(&full[r], 1); mbar_init(&empty[r], CW); }
+        mbar_fence_init();
+        s_abort = 0;
+    }
+    __syncthreads();   // the only CTA-wide barrier: the producer warp leaves the compute loop
+
+    // Work units, assigned round-robin; a last round that would leave a quarter or more of the
+    // CTAs idle is cut into z-quarters (see k_stencil).
+    constexpr uint32_t Q = S::Q, NZQ = N / Q;
+    const uint32_t G = gridDim.x;
+    const uint32_t rem = a.n_items % G;
+    const bool split = rem != 0u && Q * rem <= (Q - 1u) * G;
+    const uint32_t n_whole = split ? a.n_items - rem : a.n_items;
+    const uint32_t n_units = n_whole + (split ? rem * Q : 0u);
+    auto unit_of = [&](uint32_t u, uint32_t& item, uint32_t& z0, uint32_t& nz) {
+        if (u < n_whole) { item = u; z0 = 0; nz = N; }
+        else { const uint32_t v = u - n_whole; item = n_whole + v / Q; z0 = (v % Q) * NZQ; nz = NZQ; }
+    };
+    auto active_node = [&](uint32_t item, uint32_t& node, int& depth) {
+        node = a.items ? a.items[item] : item;
+        depth = pos_depth(a.positions[node]);
+        return depth != -1 && active_depth(a.substep, (uint32_t)depth, a.max_depth);
+    };
+    auto next_unit = [&](uint32_t u) {
+        for (; u < n_units; u += G) {
+            uint32_t item, z0, nz, node;
+            int depth;
+            unit_of(u, item, z0, nz);
+            if (active_node(item, node, depth)) break;
+        }
+        return u;
+    };
+    auto fused_leaf = [&](uint32_t node) {   // restriction fused: a domain without children
+        if (!a.children) return false;
+        bool leaf = true;
+#pragma unroll
+        for (int c = 0; c < 8; c++) leaf &= a.children[node * 8u + c] == -1;
+        return leaf;
+    };
+
+    if (warp == CW) {   // ---------------- producer warp: one thread requests every plane
+        if (lane != 0) return;
+        uint32_t q = 0;   // planes requested
+        bool ok = true;
+        for (uint32_t u = next_unit(blockIdx.x); ok && u < n_units; u = next_unit(u + G)) {
+            uint32_t item, z0, nz, node;
+            int depth;
+            unit_of(u, item, z0, nz);
+            active_node(item, node, depth);
+            const bool leaf = fused_leaf(node);
+            const size_t src = ((size_t)node * T + z0) * PLANE;
+            for (uint32_t j = 0; j < nz + 2u * P; j++, q++) {
+                const uint32_t s = q % R;
+                // the slot's previous plane (q - R) must have been released by every compute warp
+                if (q >= (uint32_t)R && !mbar_wait(&empty[s], ((q / R) - 1u) & 1u)) { ok = false; break; }
+                if (s_abort) { ok = false; break; }
+                mbar_arrive_expect_tx(&full[s], NC * S::PLANE_BYTES);
+#pragma unroll
+                for (int k = 0; k < NC; k++)
+                    bulk_g2s(ring + ((size_t)k * R + s) * PLANE, (leaf ? a.leaf_src[k] : a.field[k]) + src + (size_t)j * PLANE,
+                             S::PLANE_BYTES, &full[s]);
+            }
+        }
+        if (!ok) {   // abort: let the copies in flight land before the CTA's shared memory goes
+            s_abort = 1;
+            atomicExch(a.err, 1);
+            for (uint32_t p = q > (uint32_t)R ? q - R : 0u; p < q; p++) mbar_wait(&full[p % R], (p / R) & 1u);
+        }
+        return;
+    }
+
+    // ---------------- compute warps: thread (x, y) per column; the last warp may be partial
+    const bool lane_active = tid < NN;
+    const uint32_t t = lane_active ? tid : 0u;
+    const uint32_t x = t % N;
+    const uint32_t y = N == 16 ? ((t / N) >> 1) | (((t / N) & 1u) << 3) : t / N;
+    const int c0 = (int)((y + P) * T + (x + P));
+    if (lane_active) {   // per-cell generators: the part that depends on (seed, x, y) only
+        const int32_t* sp = a.seed_ptr;
+#pragma unroll
+        for (int k = 0; k < NC; k++) {
+            s_pre[(2 * k) * NN + tid] = cell_rng_prefix(sp ? sp[2 * k] : a.seed_d[k], x, y);
+            s_pre[(2 * k + 1) * NN + tid] = cell_rng_prefix(sp ? sp[2 * k + 1] : a.seed_m[k], x, y);
+        }
+        s_pre[12 * NN + tid] = cell_rng_prefix(sp ? sp[12] : a.seed_c, x, y);
+    }
+    uint32_t g_base = 0;   // stream index of the current unit's first padded plane
+    for (uint32_t cu = next_unit(blockIdx.x); cu < n_units; cu = next_unit(cu + G)) {
+        uint32_t item, z0, nz, node;
+        int depth;
+        unit_of(cu, item, z0, nz);
+        active_node(item, node, depth);
+        const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
+        const bool leaf = fused_leaf(node);
+#pragma unroll 1
+        for (uint32_t zl = 0; zl < nz; zl++) {
+            const uint32_t g = g_base + zl, z = z0 + zl;   // planes g .. g+2P hold padded z .. z+2P
+            bool ok = true;
+            for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {   // a unit's first window needs all
+                const uint32_t sq = g + j;
+                ok &= mbar_wait(&full[sq % R], (sq / R) & 1u);
+            }
+            if (!ok) s_abort = 1;
+            if (s_abort) { bulk_wait(); return; }
+            const uint32_t base_s = g % R;
+            uint32_t slot[2 * P + 1];
+#pragma unroll
+            for (int j = 0; j <= 2 * P; j++) slot[j] = base_s + j >= (uint32_t)R ? base_s + j - R : base_s + j;
+            // fused restriction: each padded plane of a leaf goes to field[k] once -- by the unit
+            // whose interior it is, the end units also taking the ghost planes beyond -- stored out
+            // of the ring by lane 0 of one compute warp per plane, in turn
+            const bool storer = leaf && tid == 32u * (g % CW);
+            if (storer) {
+                for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {
+                    const uint32_t jj = zl + (uint32_t)j;   // plane index within the unit
+                    const bool own = (jj >= P && jj < nz + P) || (z0 == 0 && jj < P) || (z0 + nz == N && jj >= nz + P);
+                    if (!own) continue;
+                    const uint32_t sl = base_s + (uint32_t)j >= (uint32_t)R ? base_s + j - R : base_s + j;
+#pragma unroll
+                    for (int k = 0; k < NC; k++)
+                        bulk_s2g(const_cast<float*>(a.field[k]) + ((size_t)node * T + z0 + jj) * PLANE,
+                                 ring + ((size_t)k * R + sl) * PLANE, S::PLANE_BYTES);
+                }
+                bulk_commit();
+            }
+            if (lane_active) {
+                const uint32_t zg = node * N + z;
+                bssn_cell<N, P>(a, ring, slot, c0, x, y, z, zg, ((size_t)zg * N + y) * N + x, dx1, dx2, tid, s_pre,
+                                s_grad);
+            }
+            // this warp is done with plane g (a storer first waits for its stores to read the ring)
+            if (storer) bulk_wait_read();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[base_s]);
+        }
+        // the unit's trailing 2P planes start no window: release them too
+        __syncwarp();
+        if (lane == 0)
+            for (uint32_t p = g_base + nz; p < g_base + nz + 2u * P; p++) mbar_arrive(&empty[p % R]);
+        g_base += nz + 2u * P;
+    }
+    bulk_wait();   // this thread's stores out of the ring are complete
+}
+
 // ---------------------------------------------------------------- launch
 template <int N, int P, int KIND>
 cudaError_t launch_stencil_t(const StencilArgs& a, uint32_t grid, cudaStream_t st) {
     using S = StencilShape<N, P, KIND>;
     static bool configured = false;
+    void (*kernel)(const StencilArgs);
+    if constexpr (KIND == SK_BSSN) kernel = k_stencil_bssn<N, P>;
+    else kernel = k_stencil<N, P, KIND>;
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_stencil<N, P, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
         if (e != cudaSuccess) return e;
         configured = true;
     }
     if (grid == 0) return cudaSuccess;
-    k_stencil<N, P, KIND><<<grid, N * N, S::SMEM, st>>>(a);
+    kernel<<<grid, S::THREADS, S::SMEM, st>>>(a);
     return cudaGetLastError();
 }
 
