@@ -1,10 +1,12 @@
 // kernels_stencil.cu -- finite-difference stencils on padded domains (sm_103a).
 //
-// One CTA processes one domain at a time (a persistent loop over a work list).  The domain's
-// padded z-planes are streamed through a shared-memory ring with 1-D TMA bulk copies
-// (cp.async.bulk, one copy per plane and component, completion on an mbarrier per ring slot);
-// thread (x, y) computes the interior cell (x, y, z) of every plane, so each plane is read from
-// HBM exactly once and every stencil tap comes from shared memory.
+// A persistent grid works through units of domains (whole domains, or z-ranges of them to fill a
+// last round).  A unit's padded z-planes are streamed through a shared-memory ring with 1-D TMA
+// bulk copies (cp.async.bulk, one copy per plane and component, completion on an mbarrier per ring
+// slot); thread (x, y) computes the interior cell (x, y, z) of every plane, so each plane is read
+// from HBM once per unit and every stencil tap comes from shared memory.  k_stencil (one operator)
+// refills the ring from thread 0 behind a CTA barrier per plane; k_stencil_bssn (the fused pass)
+// is warp-specialised, with a producer warp and per-slot full/empty barriers.
 //
 // Kinds:
 //   SK_GRAD       gradient                                   __differentiate  (AMR.h:1152-1179)
@@ -143,14 +145,13 @@ __device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M
 // ---------------------------------------------------------------- the streaming kernel
 template <int N, int P, int KIND>
 __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const __grid_constant__ StencilArgs a) {
+    static_assert(KIND != SK_BSSN, "the fused kind is k_stencil_bssn");
     using S = StencilShape<N, P, KIND>;
     constexpr int T = S::T, NC = S::NC, R = S::R;
-    constexpr uint32_t PLANE = S::PLANE, NN = N * N;
+    constexpr uint32_t PLANE = S::PLANE;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* ring = reinterpret_cast<float*>(smem_raw);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + S::RING_BYTES);
-    int32_t* s_pre = reinterpret_cast<int32_t*>(smem_raw + S::RING_BYTES + S::BAR_BYTES);   // [13][NN]
-    uint32_t* s_grad = reinterpret_cast<uint32_t*>(s_pre + 13 * NN);                       // [6][NN]
     __shared__ int s_abort;
 
     const uint32_t tid = threadIdx.x;
@@ -182,12 +183,8 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
 #pragma unroll
         for (int k = 0; k < NC; k++) { pre_d[k] = cell_rng_prefix(seed_d[k], x, y); pre_m[k] = cell_rng_prefix(seed_m[k], x, y); }
         pre_c = cell_rng_prefix(seed_c, x, y);
-        if (KIND == SK_BSSN) {   // the fused kind's component loop is not unrolled: it reads them here
-#pragma unroll
-            for (int k = 0; k < NC; k++) { s_pre[(2 * k) * NN + tid] = pre_d[k]; s_pre[(2 * k + 1) * NN + tid] = pre_m[k]; }
-            s_pre[12 * NN + tid] = pre_c;
-        }
     }
+    (void)pre_c;
 
     // Work units, assigned round-robin.  Items are processed whole, except that when the last
     // round would leave a quarter or more of the CTAs idle (rem <= 3/4 of the grid), its items are
@@ -218,20 +215,10 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
         }
         return u;
     };
-    // A leaf domain when the restriction is fused: no children (its planes come from leaf_src).
-    auto fused_leaf = [&](uint32_t node) {
-        if (KIND != SK_BSSN || !a.children) return false;
-        bool leaf = true;
-#pragma unroll
-        for (int c = 0; c < 8; c++) leaf &= a.children[node * 8u + c] == -1;
-        return leaf;
-    };
-    // thread 0's request state: unit p_unit (its domain's first plane p_src, its plane count p_np,
-    // whether its planes come from leaf_src), the next of its planes p_j, and the planes requested
-    // so far
+    // thread 0's request state: unit p_unit (its domain's first plane p_src and its plane count
+    // p_np), the next of its planes p_j, and the planes requested so far
     uint32_t p_unit = n_units, p_j = 0, p_np = 0, issued = 0;
     size_t p_src = 0;
-    bool p_leaf = false;
     auto open_unit = [&](uint32_t u) {
         p_unit = next_unit(u);
         if (p_unit < n_units) {
@@ -241,7 +228,6 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
             active_node(item, node, depth);
             p_src = ((size_t)node * T + z0) * PLANE;
             p_np = nz + 2u * P;
-            p_leaf = fused_leaf(node);
         }
     };
     if (tid == 0) open_unit(blockIdx.x);
@@ -251,8 +237,8 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
             mbar_arrive_expect_tx(&bars[s], NC * S::PLANE_BYTES);
 #pragma unroll
             for (int k = 0; k < NC; k++)
-                bulk_g2s(ring + ((size_t)k * R + s) * PLANE, (p_leaf ? a.leaf_src[k] : a.field[k]) + p_src + (size_t)p_j * PLANE,
-                         S::PLANE_BYTES, &bars[s]);
+                bulk_g2s(ring + ((size_t)k * R + s) * PLANE, a.field[k] + p_src + (size_t)p_j * PLANE, S::PLANE_BYTES,
+                         &bars[s]);
             issued++;
             if (++p_j == p_np) { p_j = 0; open_unit(p_unit + G); }
         }
@@ -265,7 +251,6 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
         unit_of(cu, item, z0, nz);
         active_node(item, node, depth);
         const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
-        const bool leaf = fused_leaf(node);
 #pragma unroll 1
         for (uint32_t zl = 0; zl < nz; zl++) {
             const uint32_t g = g_base + zl, z = z0 + zl;   // planes g .. g+2P hold padded z .. z+2P
@@ -277,25 +262,6 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                 ok &= mbar_wait(&bars[sq % R], (sq / R) & 1u);
             }
             if (!ok) s_abort = 1;
-            // fused restriction: each padded plane of a leaf goes to field[k] once -- by the unit
-            // whose interior it is, the end units also taking the ghost planes beyond -- stored out
-            // of the ring by lane 0 of one warp per plane (in turn), which waits for the stores to
-            // have read the ring before the plane's closing barrier
-            const bool storer = leaf && tid == 32u * (g % (NN / 32u));
-            if (ok && storer) {
-                const uint32_t base_s = g % R;
-                for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {
-                    const uint32_t jj = zl + (uint32_t)j;   // plane index within the unit
-                    const bool own = (jj >= P && jj < nz + P) || (z0 == 0 && jj < P) || (z0 + nz == N && jj >= nz + P);
-                    if (!own) continue;
-                    const uint32_t sl = base_s + (uint32_t)j >= (uint32_t)R ? base_s + j - R : base_s + j;
-#pragma unroll
-                    for (int k = 0; k < NC; k++)
-                        bulk_s2g(const_cast<float*>(a.field[k]) + ((size_t)node * T + z0 + jj) * PLANE,
-                                 ring + ((size_t)k * R + sl) * PLANE, S::PLANE_BYTES);
-                }
-                bulk_commit();
-            }
             if (ok) {
                 const uint32_t base = g % R;
                 uint32_t slot[2 * P + 1];
@@ -317,55 +283,19 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
                     const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
                     int32_t rng = cell_rng_at(pre_m[0], zg);
                     a.hoff[o] = cf3_encode(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rng);
-                } else {   // SK_BSSN
-                    const size_t cz = (size_t)slot[P] * PLANE + c0;
-                    const Sym g{ring[0 * R * PLANE + cz], ring[1 * (size_t)R * PLANE + cz], ring[2 * (size_t)R * PLANE + cz],
-                                ring[3 * (size_t)R * PLANE + cz], ring[4 * (size_t)R * PLANE + cz], ring[5 * (size_t)R * PLANE + cz]};
-                    const Sym ginv = sym_inverse(g);
-                    // three components per pass: six unrolled copies of the body overflow the
-                    // instruction cache, a rolled loop spends instructions on addressing
-#pragma unroll 3
-                    for (int k = 0; k < 6; k++) {
-                        const float* base = ring + (size_t)k * R * PLANE;
-                        auto pl = [&](int j) { return base + (size_t)slot[j] * PLANE; };
-                        float gx, gy, gz, hx, hy, hz;
-                        fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
-                        int32_t rd = cell_rng_at(s_pre[(2 * k) * NN + tid], zg);
-                        // the Hessians are quantised exactly as the reference writes and re-reads them
-                        const Cf3Quantised hq = cf3_encode_quantised(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
-                        const uint32_t gk = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
-                        a.grad[k][o] = gk;
-                        s_grad[k * NN + tid] = gk;
-                        const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
-                        int32_t rm = cell_rng_at(s_pre[(2 * k + 1) * NN + tid], zg);
-                        const Cf3Quantised oq = cf3_encode_quantised(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
-                        const Sym H{hq.value.x, oq.value.x, oq.value.y, hq.value.y, oq.value.z, hq.value.z};   // tensors.h:430-435
-                        a.lap[k][o] = trace_contra(H, ginv);
-                    }
-                    uint32_t G[6];
-#pragma unroll
-                    for (int k = 0; k < 6; k++) G[k] = s_grad[k * NN + tid];
-                    int32_t rc = cell_rng_at(s_pre[12 * NN + tid], zg);
-                    uint32_t out[6];
-                    christoffel_cell(G, a.christoffel_mode == AMR_CHRISTOFFEL_RAISED ? ginv : g, rc, out);
-#pragma unroll
-                    for (int k = 0; k < 6; k++) a.chr[k][o] = out[k];
                 }
             }
-            if (storer) bulk_wait_read();
             __syncthreads();   // every thread is done with plane g: its slot may be refilled
             if (s_abort) {
                 if (tid == 0) {
                     atomicExch(a.err, 1);
                     for (uint32_t sq = g; sq < issued; sq++) mbar_wait(&bars[sq % R], (sq / R) & 1u);   // drain (bounded)
                 }
-                bulk_wait();
                 return;
             }
         }
         g_base += nz + 2u * P;
     }
-    bulk_wait();   // this thread's stores out of the ring are complete
 }
 
 // ---------------------------------------------------------------- the fused BSSN pass, warp-specialised
