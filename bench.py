@@ -337,7 +337,7 @@ def main() -> None:
     pk = peaks()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"] if achieved else None, "traffic": None,
-                "kernel": "k_stencil<16,3,SK_BSSN> (fused BSSN derivatives)", "peak_source": pk["source"],
+                "kernel": "k_stencil_bssn<16,3> (fused BSSN derivatives)", "peak_source": pk["source"],
                 "avg_launch_ms": k_ms / k_n if k_n else None, "launches_timed": k_n}
     try:   # DRAM bytes per domain from an ncu capture of the same kernel and workload, scaled per launch
         with open(os.path.join(ROOT, "profiles", "k_stencil_bssn_16p3.traffic.json")) as f:
