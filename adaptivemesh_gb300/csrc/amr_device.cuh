@@ -13,6 +13,21 @@
 
 namespace amr {
 
+// ------------------------------------------------------------------ packed pairs (f32x2, sm_100+)
+// One instruction performs the same operation on two independent floats.  Each lane rounds as the
+// scalar operation does and flushes subnormals as the -ftz=true scalar code.  One difference: the
+// code generator fuses a packed product that feeds a packed add or subtract into one packed
+// fused multiply-add (it never does so with the scalar __fmul_rn), so a packed product must only
+// feed a multiply or a fused multiply-add, or be exact; where a rounded product is added, the
+// product and the sum are done as scalars.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 add2_rz(float2 a, float2 b) { return __fadd2_rz(a, b); }
+// a - b = a + (-b) exactly, signed zeros included
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
+
 // ------------------------------------------------------------------ fast_prng (tensors.h:276-304)
 __device__ __forceinline__ int32_t prng_next(int32_t& s) {
     uint32_t v = (uint32_t)s + 1124781675u;
@@ -126,6 +141,68 @@ __device__ __forceinline__ uint32_t cf3_encode_det(float x, float y, float z) {
     int32_t unused = 0;
     return cf3_encode_impl<false, false>(x, y, z, unused).word;
 }
+// ------------------------------------------------------------------ the encoder on pairs
+// Two independent stochastic encodes (lanes x and y) with their floating-point steps done as
+// packed pairs; each lane is cf3_encode_impl<true, WANT_VALUE> bit for bit.  The noise pairs
+// (nx, ny, nz) are the lanes' three draws in the order the scalar encoder takes them (x, y, z).
+struct Cf3Pair {
+    uint32_t w0, w1;        // the words of lanes x and y
+    float2 vx, vy, vz;      // WANT_VALUE: the decoded components (lane x of each: the first word)
+};
+__device__ __forceinline__ float2 noise_pair(int32_t s0, int32_t s1) {
+    constexpr float kScale = 0.95f * 0x1p-32f;   // as prng_noise
+    return mul2(make_float2(__int2float_rn(s0), __int2float_rn(s1)), splat2(kScale));
+}
+// Noise pairs of two generators, one per lane.
+__device__ __forceinline__ void noise_pairs2(int32_t& r0, int32_t& r1, float2& nx, float2& ny, float2& nz) {
+    nx = noise_pair(prng_next(r0), prng_next(r1));
+    ny = noise_pair(prng_next(r0), prng_next(r1));
+    nz = noise_pair(prng_next(r0), prng_next(r1));
+}
+// Noise pairs of one generator: lane x takes its next three draws, lane y the three after.
+__device__ __forceinline__ void noise_pairs1(int32_t& r, float2& nx, float2& ny, float2& nz) {
+    const int32_t a0 = prng_next(r), a1 = prng_next(r), a2 = prng_next(r);
+    const int32_t b0 = prng_next(r), b1 = prng_next(r), b2 = prng_next(r);
+    nx = noise_pair(a0, b0);
+    ny = noise_pair(a1, b1);
+    nz = noise_pair(a2, b2);
+}
+struct Cf3Field2 {
+    float2 bits, k, sign;   // per lane as Cf3Field (bits as a float)
+};
+__device__ __forceinline__ Cf3Field2 cf3_field2(float2 v) {
+    Cf3Field2 c;
+    const float2 q = add2(make_float2(fminf(fabsf(v.x), 255.f), fminf(fabsf(v.y), 255.f)), splat2(.5f));
+    asm("set.lt.f32.f32 %0, %1, 0f00000000;" : "=f"(c.sign.x) : "f"(v.x));
+    asm("set.lt.f32.f32 %0, %1, 0f00000000;" : "=f"(c.sign.y) : "f"(v.y));
+    c.k = fma2(c.sign, splat2(256.f), splat2(8388608.f));
+    c.bits = add2_rz(q, c.k);
+    return c;
+}
+template <bool WANT_VALUE>
+__device__ __forceinline__ Cf3Pair cf3_encode2(float2 x, float2 y, float2 z, float2 nx, float2 ny, float2 nz) {
+    const uint32_t E0 = min(max(max_exponent3(x.x, y.x, z.x), 112u) - 112u, 31u);
+    const uint32_t E1 = min(max(max_exponent3(x.y, y.y, z.y), 112u) - 112u, 31u);
+    const float2 scale = make_float2(__uint_as_float((149u - E0) << 23), __uint_as_float((149u - E1) << 23));
+    x = fma2(x, scale, nx);
+    y = fma2(y, scale, ny);
+    z = fma2(z, scale, nz);
+    const Cf3Field2 fx = cf3_field2(x), fy = cf3_field2(y), fz = cf3_field2(z);
+    Cf3Pair r;
+    r.w0 = (E0 << 27) + (__float_as_uint(fx.bits.x) & 511u) + __float_as_uint(fy.bits.x) * 512u +
+           __float_as_uint(fz.bits.x) * 262144u;
+    r.w1 = (E1 << 27) + (__float_as_uint(fx.bits.y) & 511u) + __float_as_uint(fy.bits.y) * 512u +
+           __float_as_uint(fz.bits.y) * 262144u;
+    if (WANT_VALUE) {
+        const float2 back = make_float2(__uint_as_float((105u + E0) << 23), __uint_as_float((105u + E1) << 23));
+        const float2 back2 = mul2(back, splat2(-2.f));
+        r.vx = mul2(sub2(fx.bits, fx.k), fma2(fx.sign, back2, back));
+        r.vy = mul2(sub2(fy.bits, fy.k), fma2(fy.sign, back2, back));
+        r.vz = mul2(sub2(fz.bits, fz.k), fma2(fz.sign, back2, back));
+    }
+    return r;
+}
+
 // Exact: m * 2^(E-22) is representable, the sign bit is applied last (so m = 0 keeps its sign).
 __device__ __forceinline__ float cf3_component(uint32_t w, uint32_t mpos, uint32_t spos) {
     const float scale = __uint_as_float((105u + (w >> 27)) << 23);  // 2^(E-22)
@@ -260,6 +337,38 @@ __device__ __forceinline__ float interp10_strided(const float* __restrict__ d, S
     acc = __fmaf_rn(__fmul_rn(fxy, rx), ry, acc);
     acc = __fmaf_rn(__fmul_rn(fxz, rx), rz, acc);
     acc = __fmaf_rn(__fmul_rn(fyz, ry), rz, acc);
+    return acc;
+}
+// interp10_strided on two fields at once: d holds (a, b) pairs, the result is
+// (interp10_strided(a), interp10_strided(b)), each lane the same operation sequence.
+template <class S>
+__device__ __forceinline__ float2 interp10_pair(const float2* __restrict__ d, S sy, S sz, float rx, float ry, float rz) {
+    const float2 f = d[0];
+    float2 fx = d[1], fy = d[sy], fz = d[sz];
+    float2 fxx = d[-1], fyy = d[-sy], fzz = d[-sz];
+    float2 fxy = d[sy + 1], fxz = d[sz + 1], fyz = d[sz + sy];
+    fxy = add2(fxy, sub2(sub2(f, fx), fy));
+    fxz = add2(fxz, sub2(sub2(f, fx), fz));
+    fyz = add2(fyz, sub2(sub2(f, fy), fz));
+    // the halving is exact (bar a subnormal product), fused into the next add or not
+    const float2 half = splat2(.5f);
+    fx = mul2(sub2(fx, fxx), half);
+    fy = mul2(sub2(fy, fyy), half);
+    fz = mul2(sub2(fz, fzz), half);
+    fxx = sub2(add2(fx, fxx), f);
+    fyy = sub2(add2(fy, fyy), f);
+    fzz = sub2(add2(fz, fzz), f);
+    const float2 Rx = splat2(rx), Ry = splat2(ry), Rz = splat2(rz);
+    // fx + fxx * rx with the product rounded: scalar (a packed product would be fused into the add)
+    auto axis = [](float2 g, float2 h, float r) {
+        return make_float2(__fadd_rn(g.x, __fmul_rn(h.x, r)), __fadd_rn(g.y, __fmul_rn(h.y, r)));
+    };
+    float2 acc = fma2(axis(fx, fxx, rx), Rx, f);
+    acc = fma2(axis(fy, fyy, ry), Ry, acc);
+    acc = fma2(axis(fz, fzz, rz), Rz, acc);
+    acc = fma2(mul2(fxy, Rx), Ry, acc);
+    acc = fma2(mul2(fxz, Rx), Rz, acc);
+    acc = fma2(mul2(fyz, Ry), Rz, acc);
     return acc;
 }
 // The same on a padded domain (strides T, T^2).

@@ -325,8 +325,10 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
         }
     }
     // Component k's box goes to buffer k & 1 by asynchronous copies, issued one component ahead.
+    // A box element is the pair (old, new), so that one interpolation serves both.
+    float2* const sbox2 = reinterpret_cast<float2*>(sbox);
     auto issue = [&](int k) {
-        float* buf = sbox + (k & 1) * 2u * BOX;
+        float* buf = reinterpret_cast<float*>(sbox2 + (k & 1) * BOX);
         const float* go = f.old_f[k] + src0;
         const float* gn = f.new_f[k] + src0;
         if (kCached) {
@@ -334,16 +336,16 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
             for (uint32_t e = 0; e < EPT; e++) {
                 const uint32_t i = threadIdx.x + e * kBlock;
                 if (i < box) {
-                    cp_async4(buf + i, go + e_gi[kCached ? e : 0]);
-                    cp_async4(buf + BOX + i, gn + e_gi[kCached ? e : 0]);
+                    cp_async4(buf + 2u * i, go + e_gi[kCached ? e : 0]);
+                    cp_async4(buf + 2u * i + 1u, gn + e_gi[kCached ? e : 0]);
                 }
             }
         } else {
             uint32_t bx = bx0, by = by0, bz = bz0;
             for (uint32_t i = threadIdx.x; i < box; i += kBlock) {
                 const uint32_t gi = bx + (by + bz * T) * T;
-                cp_async4(buf + i, go + gi);
-                cp_async4(buf + BOX + i, gn + gi);
+                cp_async4(buf + 2u * i, go + gi);
+                cp_async4(buf + 2u * i + 1u, gn + gi);
                 bx += A; by += B; bz += C;
                 if (bx >= sy) { bx -= sy; by++; }
                 if (by >= ext[1]) { by -= ext[1]; bz++; }
@@ -353,7 +355,7 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
     };
     issue(0);
     for (int k = 0; k < f.ncomp; k++) {
-        const float* buf = sbox + (k & 1) * 2u * BOX;
+        const float2* buf = sbox2 + (k & 1) * BOX;
         if (k + 1 < f.ncomp) { issue(k + 1); cp_async_wait<1>(); }
         else cp_async_wait<0>();
         __syncthreads();   // component k's box is complete in every thread's view
@@ -379,8 +381,8 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
 #pragma unroll
         for (uint32_t c = 0; c < CPT; c++) {
             if (threadIdx.x + c * kBlock >= G::FACE) break;
-            const float od = interp10_strided(buf + c_o[c], (int)sy, (int)sz, c_rx[c], c_ry[c], c_rz[c]);
-            const float nw = interp10_strided(buf + BOX + c_o[c], (int)sy, (int)sz, c_rx[c], c_ry[c], c_rz[c]);
+            const float2 on = interp10_pair(buf + c_o[c], (int)sy, (int)sz, c_rx[c], c_ry[c], c_rz[c]);
+            const float od = on.x, nw = on.y;
             const bool staged = (c_dst[c] & 0x80000000u) != 0u;
             const uint32_t off = c_dst[c] & 0x7FFFFFFFu;
             if (!copy_only_new) (staged ? stage_old : field_old)[off] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));

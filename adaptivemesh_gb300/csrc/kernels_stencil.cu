@@ -117,6 +117,69 @@ __device__ __forceinline__ float3 mixed_partials(const PL& pl, int c0, uint32_t 
     return make_float3(vxy, vxz, vyz);
 }
 
+// fd_axes on two components at once: lane x reads the planes at p, lane y the planes OFF floats
+// further (the next component's ring).
+template <int P, int T, int OFF, class PL>
+__device__ __forceinline__ void fd_axes2(const PL& pl, int c0, float2& gx, float2& gy, float2& gz, float2& hx,
+                                         float2& hy, float2& hz) {
+    gx = gy = gz = hx = hy = hz = splat2(0.f);
+    const float* m = pl(P);
+#pragma unroll
+    for (int i = -P; i <= P; i++) {
+        const float2 c1 = splat2(FD<P>::d1(i)), c2 = splat2(FD<P>::d2(i));
+        float2 a = make_float2(m[c0 + i], m[c0 + i + OFF]);
+        gx = fma2(a, c1, gx); hx = fma2(a, c2, hx);
+        a = make_float2(m[c0 + i * T], m[c0 + i * T + OFF]);
+        gy = fma2(a, c1, gy); hy = fma2(a, c2, hy);
+        const float* q = pl(P + i);
+        a = make_float2(q[c0], q[c0 + OFF]);
+        gz = fma2(a, c1, gz); hz = fma2(a, c2, hz);
+    }
+}
+__device__ __forceinline__ float2 mixed_centre2(float2 a, float2 b, float2 c, float2 d) {
+    return mul2(splat2(.25f), sub2(sub2(add2(a, b), c), d));
+}
+__device__ __forceinline__ float2 mixed_edge2(float2 f, float2 a, float2 b, float2 c, float2 d, float2 e, float2 g) {
+    float2 s = add2(a, b);
+    s = sub2(s, c); s = sub2(s, d); s = sub2(s, e); s = sub2(s, g);
+    return fma2(splat2(.5f), s, f);
+}
+// mixed_partials on two components at once (lanes as in fd_axes2); the edge cases depend on the
+// cell only, so both lanes take the same branch.
+template <int N, int P, int T, int OFF, class PL>
+__device__ __forceinline__ void mixed_partials2(const PL& pl, int c0, uint32_t x, uint32_t y, uint32_t z, float2& vxy,
+                                                float2& vxz, float2& vyz) {
+    const float* zm = pl(P - 1);
+    const float* z0 = pl(P);
+    const float* zp = pl(P + 1);
+    auto ld = [&](const float* q, int i) { return make_float2(q[i], q[i + OFF]); };
+    const int ex = (int)x - (int)min(max(x, 1u), (uint32_t)N - 2u);
+    const int ey = (int)y - (int)min(max(y, 1u), (uint32_t)N - 2u);
+    const int ez = (int)z - (int)min(max(z, 1u), (uint32_t)N - 2u);
+    const int cxy = ex * ey, cxz = ex * ez, cyz = ey * ez;
+    if (cxy == 0) {
+        vxy = mixed_centre2(ld(z0, c0 + 1 + T), ld(z0, c0 - 1 - T), ld(z0, c0 + 1 - T), ld(z0, c0 - 1 + T));
+    } else {
+        const int dx = -cxy;
+        vxy = mul2(splat2((float)(-cxy)), mixed_edge2(ld(z0, c0), ld(z0, c0 + dx + T), ld(z0, c0 - dx - T),
+                                                      ld(z0, c0 - dx), ld(z0, c0 + dx), ld(z0, c0 - T), ld(z0, c0 + T)));
+    }
+    if (cxz == 0) {
+        vxz = mixed_centre2(ld(zp, c0 + 1), ld(zm, c0 - 1), ld(zm, c0 + 1), ld(zp, c0 - 1));
+    } else {
+        const int dx = -cxz;
+        vxz = mul2(splat2((float)(-cxz)), mixed_edge2(ld(z0, c0), ld(zp, c0 + dx), ld(zm, c0 - dx), ld(z0, c0 - dx),
+                                                      ld(z0, c0 + dx), ld(zm, c0), ld(zp, c0)));
+    }
+    if (cyz == 0) {
+        vyz = mixed_centre2(ld(zp, c0 + T), ld(zm, c0 - T), ld(zm, c0 + T), ld(zp, c0 - T));
+    } else {
+        const int dx = -cyz * T;
+        vyz = mul2(splat2((float)(-cyz)), mixed_edge2(ld(z0, c0), ld(zp, c0 + dx), ld(zm, c0 - dx), ld(z0, c0 - dx),
+                                                      ld(z0, c0 + dx), ld(zm, c0), ld(zp, c0)));
+    }
+}
+
 // Christoffel symbols of one cell from the six compressed metric gradients (BSSN.h:72-90).
 // `M` multiplies the lowered symbols: the metric itself (reference) or its inverse.
 __device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M, int32_t& rng, uint32_t* out) {
@@ -133,12 +196,21 @@ __device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M
     const float sx[6] = {Sx.xx, Sx.xy, Sx.xz, Sx.yy, Sx.yz, Sx.zz};
     const float sy[6] = {Sy.xx, Sy.xy, Sy.xz, Sy.yy, Sy.yz, Sy.zz};
     const float sz[6] = {Sz.xx, Sz.xy, Sz.xz, Sz.yy, Sz.yz, Sz.zz};
+    // symbols jk and jk+1 as the two lanes of a pair; fma(-d, .5, s) = fma(d, -.5, s) exactly
 #pragma unroll
-    for (int jk = 0; jk < 6; jk++) {
-        const float3 v = make_float3(__fmaf_rn(-d[jk].x, .5f, sx[jk]), __fmaf_rn(-d[jk].y, .5f, sy[jk]),
-                                     __fmaf_rn(-d[jk].z, .5f, sz[jk]));
-        const float3 r = sym_times(M, v);
-        out[jk] = cf3_encode(r.x, r.y, r.z, rng);
+    for (int jk = 0; jk < 6; jk += 2) {
+        const float2 vx = fma2(make_float2(d[jk].x, d[jk + 1].x), splat2(-.5f), make_float2(sx[jk], sx[jk + 1]));
+        const float2 vy = fma2(make_float2(d[jk].y, d[jk + 1].y), splat2(-.5f), make_float2(sy[jk], sy[jk + 1]));
+        const float2 vz = fma2(make_float2(d[jk].z, d[jk + 1].z), splat2(-.5f), make_float2(sz[jk], sz[jk + 1]));
+        // M * v (sym_times)
+        const float2 rx = fma2(vz, splat2(M.xz), fma2(vx, splat2(M.xx), mul2(vy, splat2(M.xy))));
+        const float2 ry = fma2(vz, splat2(M.yz), fma2(vx, splat2(M.xy), mul2(vy, splat2(M.yy))));
+        const float2 rz = fma2(vz, splat2(M.zz), fma2(vx, splat2(M.xz), mul2(vy, splat2(M.yz))));
+        float2 nx, ny, nz;
+        noise_pairs1(rng, nx, ny, nz);
+        const Cf3Pair w = cf3_encode2<false>(rx, ry, rz, nx, ny, nz);
+        out[jk] = w.w0;
+        out[jk + 1] = w.w1;
     }
 }
 
@@ -314,25 +386,41 @@ __device__ __forceinline__ void bssn_cell(const StencilArgs& a, const float* rin
     const Sym g{ring[0 * R * PLANE + cz], ring[1 * (size_t)R * PLANE + cz], ring[2 * (size_t)R * PLANE + cz],
                 ring[3 * (size_t)R * PLANE + cz], ring[4 * (size_t)R * PLANE + cz], ring[5 * (size_t)R * PLANE + cz]};
     const Sym ginv = sym_inverse(g);
-    // three components per pass: six unrolled copies of the body overflow the instruction cache,
-    // a rolled loop spends instructions on addressing
-#pragma unroll 3
-    for (int k = 0; k < 6; k++) {
-        const float* base = ring + (size_t)k * R * PLANE;
-        auto pl = [&](int j) { return base + (size_t)slot[j] * PLANE; };
-        float gx, gy, gz, hx, hy, hz;
-        fd_axes<P, T>(pl, c0, gx, gy, gz, hx, hy, hz);
-        int32_t rd = cell_rng_at(s_pre[(2 * k) * NN + tid], zg);
+    // components two at a time, as the lanes of packed pairs (every lane the scalar operation
+    // sequence); component 2j+1's ring lies R planes after component 2j's
+    constexpr int OFF = R * (int)PLANE;
+    const float2 DX1 = splat2(dx1), DX2 = splat2(dx2);
+#pragma unroll 1
+    for (int j = 0; j < 3; j++) {
+        const int k0 = 2 * j, k1 = 2 * j + 1;
+        const float* base = ring + (size_t)k0 * R * PLANE;
+        auto pl = [&](int jj) { return base + (size_t)slot[jj] * PLANE; };
+        float2 gx, gy, gz, hx, hy, hz;
+        fd_axes2<P, T, OFF>(pl, c0, gx, gy, gz, hx, hy, hz);
+        int32_t rd0 = cell_rng_at(s_pre[(2 * k0) * NN + tid], zg), rd1 = cell_rng_at(s_pre[(2 * k1) * NN + tid], zg);
+        float2 nx, ny, nz;
         // the Hessians are quantised exactly as the reference writes and re-reads them
-        const Cf3Quantised hq = cf3_encode_quantised(__fmul_rn(hx, dx2), __fmul_rn(hy, dx2), __fmul_rn(hz, dx2), rd);
-        const uint32_t gk = cf3_encode(__fmul_rn(gx, dx1), __fmul_rn(gy, dx1), __fmul_rn(gz, dx1), rd);
-        a.grad[k][o] = gk;
-        s_grad[k * NN + tid] = gk;
-        const float3 m = mixed_partials<N, P, T>(pl, c0, x, y, z);
-        int32_t rm = cell_rng_at(s_pre[(2 * k + 1) * NN + tid], zg);
-        const Cf3Quantised oq = cf3_encode_quantised(__fmul_rn(m.x, dx2), __fmul_rn(m.y, dx2), __fmul_rn(m.z, dx2), rm);
-        const Sym H{hq.value.x, oq.value.x, oq.value.y, hq.value.y, oq.value.z, hq.value.z};   // tensors.h:430-435
-        a.lap[k][o] = trace_contra(H, ginv);
+        noise_pairs2(rd0, rd1, nx, ny, nz);
+        const Cf3Pair hq = cf3_encode2<true>(mul2(hx, DX2), mul2(hy, DX2), mul2(hz, DX2), nx, ny, nz);
+        noise_pairs2(rd0, rd1, nx, ny, nz);
+        const Cf3Pair gk = cf3_encode2<false>(mul2(gx, DX1), mul2(gy, DX1), mul2(gz, DX1), nx, ny, nz);
+        a.grad[k0][o] = gk.w0;
+        a.grad[k1][o] = gk.w1;
+        s_grad[k0 * NN + tid] = gk.w0;
+        s_grad[k1 * NN + tid] = gk.w1;
+        float2 mxy, mxz, myz;
+        mixed_partials2<N, P, T, OFF>(pl, c0, x, y, z, mxy, mxz, myz);
+        int32_t rm0 = cell_rng_at(s_pre[(2 * k0 + 1) * NN + tid], zg), rm1 = cell_rng_at(s_pre[(2 * k1 + 1) * NN + tid], zg);
+        noise_pairs2(rm0, rm1, nx, ny, nz);
+        const Cf3Pair oq = cf3_encode2<true>(mul2(mxy, DX2), mul2(mxz, DX2), mul2(myz, DX2), nx, ny, nz);
+        // trace_contra(H, ginv) with H = (hq.x, oq.x, oq.y, hq.y, oq.z, hq.z) (tensors.h:430-435)
+        float2 ta = fma2(hq.vx, splat2(ginv.xx), mul2(hq.vy, splat2(ginv.yy)));
+        ta = fma2(hq.vz, splat2(ginv.zz), ta);
+        float2 tb = fma2(oq.vx, splat2(ginv.xy), mul2(oq.vy, splat2(ginv.xz)));
+        tb = fma2(oq.vz, splat2(ginv.yz), tb);
+        const float2 lap = fma2(tb, splat2(2.f), ta);
+        a.lap[k0][o] = lap.x;
+        a.lap[k1][o] = lap.y;
     }
     uint32_t G[6];
 #pragma unroll
