@@ -23,8 +23,9 @@ namespace amr {
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 add2_rz(float2 a, float2 b) { return __fadd2_rz(a, b); }
-// a - b = a + (-b) exactly, signed zeros included
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+// a - b as fma(b, -1, a): the product is exact, so this is the rounded difference, signed zeros
+// included (x - x = +0 = -x + x), and needs no separate negation of b
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
 

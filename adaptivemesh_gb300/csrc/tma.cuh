@@ -2,7 +2,9 @@
 // Accelerator) into shared memory, tracked by transaction-count mbarriers.
 //
 // Every wait is bounded: after kMaxSpins polls the waiter reports failure so the kernel can
-// raise its error flag and leave instead of hanging the GPU.
+// raise its error flag and leave instead of hanging the GPU.  A poll suspends the thread until the
+// phase completes or kSuspendHintNs pass, so waiting warps leave the issue slots to working ones
+// and a wait gives up after about kMaxSpins * kSuspendHintNs (~1 s).
 #pragma once
 
 #include <cstdint>
@@ -11,6 +13,7 @@
 namespace amr {
 
 constexpr uint32_t kMaxSpins = 1u << 22;
+constexpr uint32_t kSuspendHintNs = 256;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -28,16 +31,16 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
-// Poll phase `parity` of the barrier; true once it completed, false after kMaxSpins polls.
+// Wait for phase `parity` of the barrier; true once it completed, false after kMaxSpins polls.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const uint32_t a = smem_addr(bar);
     for (uint32_t i = 0; i < kMaxSpins; i++) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done) : "r"(a), "r"(parity) : "memory");
+            : "=r"(done) : "r"(a), "r"(parity), "n"(kSuspendHintNs) : "memory");
         if (done) return true;
     }
     return false;
