@@ -454,31 +454,31 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
     }
     __syncthreads();   // the only CTA-wide barrier: the producer warp leaves the compute loop
 
-    // Work units, assigned round-robin; a last round that would leave a quarter or more of the
-    // CTAs idle is cut into z-quarters (see k_stencil).
-    constexpr uint32_t Q = S::Q, NZQ = N / Q;
-    const uint32_t G = gridDim.x;
-    const uint32_t rem = a.n_items % G;
-    const bool split = rem != 0u && Q * rem <= (Q - 1u) * G;
-    const uint32_t n_whole = split ? a.n_items - rem : a.n_items;
-    const uint32_t n_units = n_whole + (split ? rem * Q : 0u);
-    auto unit_of = [&](uint32_t u, uint32_t& item, uint32_t& z0, uint32_t& nz) {
-        if (u < n_whole) { item = u; z0 = 0; nz = N; }
-        else { const uint32_t v = u - n_whole; item = n_whole + v / Q; z0 = (v % Q) * NZQ; nz = NZQ; }
+    // Work: the items' interior planes, item after item, cut into gridDim.x contiguous ranges of
+    // equal length (to a plane), one per CTA.  A range is walked as units -- consecutive planes of
+    // one domain -- whose padded planes (the unit's planes and P more on either side) stream
+    // through the ring.
+    const uint64_t n_planes = (uint64_t)a.n_items * N;
+    const uint32_t p_begin = (uint32_t)((uint64_t)blockIdx.x * n_planes / gridDim.x);
+    const uint32_t p_end = (uint32_t)(((uint64_t)blockIdx.x + 1u) * n_planes / gridDim.x);
+    auto unit_of = [&](uint32_t p, uint32_t& item, uint32_t& z0, uint32_t& nz) {
+        item = p / N;
+        z0 = p - item * N;
+        nz = min((uint32_t)N - z0, p_end - p);
     };
     auto active_node = [&](uint32_t item, uint32_t& node, int& depth) {
         node = a.items ? a.items[item] : item;
         depth = pos_depth(a.positions[node]);
         return depth != -1 && active_depth(a.substep, (uint32_t)depth, a.max_depth);
     };
-    auto next_unit = [&](uint32_t u) {
-        for (; u < n_units; u += G) {
-            uint32_t item, z0, nz, node;
+    auto next_unit = [&](uint32_t p) {   // the first plane at or after p of an active domain, or p_end
+        while (p < p_end) {
+            uint32_t node;
             int depth;
-            unit_of(u, item, z0, nz);
-            if (active_node(item, node, depth)) break;
+            if (active_node(p / N, node, depth)) break;
+            p = (p / N + 1u) * N;
         }
-        return u;
+        return min(p, p_end);
     };
     auto fused_leaf = [&](uint32_t node) {   // restriction fused: a domain without children
         if (!a.children) return false;
@@ -492,8 +492,8 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
         if (lane != 0) return;
         uint32_t q = 0;   // planes requested
         bool ok = true;
-        for (uint32_t u = next_unit(blockIdx.x); ok && u < n_units; u = next_unit(u + G)) {
-            uint32_t item, z0, nz, node;
+        for (uint32_t u = next_unit(p_begin), nz = 0; ok && u < p_end; u = next_unit(u + nz)) {
+            uint32_t item, z0, node;
             int depth;
             unit_of(u, item, z0, nz);
             active_node(item, node, depth);
@@ -535,8 +535,8 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
         s_pre[12 * NN + tid] = cell_rng_prefix(sp ? sp[12] : a.seed_c, x, y);
     }
     uint32_t g_base = 0;   // stream index of the current unit's first padded plane
-    for (uint32_t cu = next_unit(blockIdx.x); cu < n_units; cu = next_unit(cu + G)) {
-        uint32_t item, z0, nz, node;
+    for (uint32_t cu = next_unit(p_begin), nz = 0; cu < p_end; cu = next_unit(cu + nz)) {
+        uint32_t item, z0, node;
         int depth;
         unit_of(cu, item, z0, nz);
         active_node(item, node, depth);
