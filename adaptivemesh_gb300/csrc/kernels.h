@@ -67,6 +67,10 @@ cudaError_t launch_wave_step(Dims d, const Geo& g, int corrector, const float* o
                              uint32_t substep, uint32_t max_depth, cudaStream_t st);
 cudaError_t launch_rasterise(Dims d, const float* data, const int32_t* children, uint32_t used, uint32_t width,
                              uint32_t height, float z_slice, int boxes, float* raster, cudaStream_t st);
+// Write n words into device memory with kernels that carry them as launch parameters (1 000 per
+// launch; *launched counts the launches): a small upload that never queues on a copy engine
+// behind bulk transfers.
+cudaError_t launch_store_words(int32_t* dst, const int32_t* words, uint32_t n, cudaStream_t st, uint32_t* launched);
 cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const uint32_t* hess, float* crit,
                              const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
                              cudaStream_t st);

@@ -279,4 +279,31 @@ cudaError_t launch_rasterise(Dims d, const float* data, const int32_t* children,
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- words carried by a launch
+namespace {
+struct WordBlock {
+    static constexpr uint32_t kMax = 1000;   // 4 KB of parameters
+    int32_t v[kMax];
+    uint32_t n;
+};
+__global__ void k_store_words(int32_t* __restrict__ dst, const __grid_constant__ WordBlock b) {
+    for (uint32_t i = threadIdx.x; i < b.n; i += blockDim.x) dst[i] = b.v[i];
+}
+}  // namespace
+
+cudaError_t launch_store_words(int32_t* dst, const int32_t* words, uint32_t n, cudaStream_t st, uint32_t* launched) {
+    uint32_t count = 0;
+    for (uint32_t at = 0; at < n; at += WordBlock::kMax) {
+        WordBlock b;
+        b.n = n - at < WordBlock::kMax ? n - at : WordBlock::kMax;
+        for (uint32_t i = 0; i < b.n; i++) b.v[i] = words[at + i];
+        k_store_words<<<1, 256, 0, st>>>(dst + at, b);
+        count++;
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) { if (launched) *launched = count; return e; }
+    }
+    if (launched) *launched = count;
+    return cudaSuccess;
+}
+
 }  // namespace amr

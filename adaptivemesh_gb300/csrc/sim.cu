@@ -48,8 +48,12 @@ public:
         : cfg(c), dims(make_dims(c)), geo(make_geo(c)), mode(mode), tree(slots, this) {}
     virtual ~SimBase() {
         if (side_stream) cudaStreamSynchronize(side_stream);
+        for (cudaStream_t t : {up_stream, down_stream}) if (t) cudaStreamSynchronize(t);
         if (stream) cudaStreamSynchronize(stream);
         if (side_stream) cudaStreamDestroy(side_stream);
+        for (cudaStream_t t : {up_stream, down_stream}) if (t) cudaStreamDestroy(t);
+        for (Staging* set : {&up[0][0], &down[0][0]})
+            for (int i = 0; i < 36; i++) set[i].release();
         if (main_mark) cudaEventDestroy(main_mark);
         for (auto& row : side_done)
             for (auto& ev : row) if (ev) cudaEventDestroy(ev);
@@ -244,6 +248,55 @@ public:
             }
         return AMR_OK;
     }
+    // Staged transfers (amr_sim_stage_to_device, amr_sim_snapshot_to_host): per buffer a device
+    // staging copy for uploads and one for downloads; host transfers run on their own streams
+    // (one per direction) and overlap the simulation's work, which meets them only at the
+    // device-to-device copies between a buffer and its staging copy.
+    struct Staging {
+        float* buf = nullptr;
+        uint64_t cap = 0;               // floats
+        cudaEvent_t copied = nullptr;   // stream: the device-to-device copy (into or out of buf) is done
+        cudaEvent_t moved = nullptr;    // transfer stream: the host transfer (into or out of buf) is done
+        bool pending = false;           // download: a host transfer from buf is outstanding
+        int ensure(uint64_t floats) {
+            if (!copied && cudaEventCreateWithFlags(&copied, cudaEventDisableTiming) != cudaSuccess) return AMR_ERR_CUDA;
+            if (!moved && cudaEventCreateWithFlags(&moved, cudaEventDisableTiming) != cudaSuccess) return AMR_ERR_CUDA;
+            if (cap >= floats) return AMR_OK;
+            if (buf) { cudaEventSynchronize(copied); cudaEventSynchronize(moved); cudaFree(buf); buf = nullptr; cap = 0; }
+            if (cudaMalloc(&buf, floats * sizeof(float)) != cudaSuccess) { buf = nullptr; return AMR_ERR_CUDA; }
+            cap = floats;
+            return AMR_OK;
+        }
+        void release() {
+            cudaFree(buf);
+            if (copied) cudaEventDestroy(copied);
+            if (moved) cudaEventDestroy(moved);
+        }
+    };
+    cudaStream_t up_stream = nullptr, down_stream = nullptr;
+    Staging up[6][6], down[6][6];
+    int ensure_transfer_streams() {
+        if (!up_stream && cudaStreamCreateWithFlags(&up_stream, cudaStreamNonBlocking) != cudaSuccess) return AMR_ERR_CUDA;
+        if (!down_stream && cudaStreamCreateWithFlags(&down_stream, cudaStreamNonBlocking) != cudaSuccess) return AMR_ERR_CUDA;
+        return AMR_OK;
+    }
+    // Make `stream` wait for the outstanding downloads of snapshots (so that an event recorded next
+    // follows them).
+    int wait_snapshots() {
+        for (auto& row : down)
+            for (Staging& d : row) {
+                if (!d.pending) continue;
+                cudaError_t e = cudaStreamWaitEvent(stream, d.moved, 0);
+                if (e != cudaSuccess) return cuda_status(e);
+                d.pending = false;
+            }
+        return AMR_OK;
+    }
+    int sync_transfer_streams() {
+        for (cudaStream_t t : {side_stream, up_stream, down_stream})
+            if (t && cudaStreamSynchronize(t) != cudaSuccess) return AMR_ERR_CUDA;
+        return AMR_OK;
+    }
     double timed_ms = 0.0;
     uint64_t timed_launches = 0;
 };
@@ -260,7 +313,6 @@ public:
         }
         for (int k = 0; k < 4; k++) cudaFree(hint[k]);
         cudaFree(d_seeds);
-        for (int k = 0; k < 2; k++) { if (h_seeds[k]) cudaFreeHost(h_seeds[k]); if (seed_ev[k]) cudaEventDestroy(seed_ev[k]); }
     }
     int init() override {
         int st = SimBase::init();
@@ -277,10 +329,6 @@ public:
         }
         for (int k = 0; k < 4 && e == cudaSuccess; k++) e = dev_alloc(&hint[k], inner);   // didjA / didjW
         if (e == cudaSuccess) e = dev_alloc(&d_seeds, (size_t)kSeedsPerSubstep << kDepthLimit);
-        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
-            e = cudaMallocHost(&h_seeds[k], sizeof(int32_t) * ((size_t)kSeedsPerSubstep << kDepthLimit));
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&seed_ev[k], cudaEventDisableTiming);
-        }
         if (e != cudaSuccess) return cuda_status(e);
         return ensure_ghost_stage(6);
     }
@@ -459,14 +507,14 @@ private:
             launches = before;
             graph_valid = true;
         }
-        const int b = seed_buf;
-        seed_buf ^= 1;
-        cudaError_t e = cudaEventSynchronize(seed_ev[b]);       // the buffer's previous upload has finished
-        if (e != cudaSuccess) return cuda_status(e);
+        // the seeds go to the device as launch parameters, not by a copy: a copy could queue behind
+        // a bulk transfer on the copy engine (amr_sim_stage_to_device) and hold up the replay
+        seed_words.resize((size_t)nsub * kSeedsPerSubstep);
         for (uint32_t s = 0; s < nsub; s++)
-            for (int i = 0; i < kSeedsPerSubstep; i++) h_seeds[b][(size_t)s * kSeedsPerSubstep + i] = next_seed();
-        e = cudaMemcpyAsync(d_seeds, h_seeds[b], sizeof(int32_t) * nsub * kSeedsPerSubstep, cudaMemcpyHostToDevice, stream);
-        if (e == cudaSuccess) e = cudaEventRecord(seed_ev[b], stream);
+            for (int i = 0; i < kSeedsPerSubstep; i++) seed_words[(size_t)s * kSeedsPerSubstep + i] = next_seed();
+        uint32_t seed_launches = 0;
+        cudaError_t e = launch_store_words(d_seeds, seed_words.data(), (uint32_t)seed_words.size(), stream, &seed_launches);
+        launches += seed_launches;
         if (e == cudaSuccess) e = cudaGraphLaunch(graph_exec, stream);
         if (e != cudaSuccess) return cuda_status(e);
         launches += graph_launches;
@@ -484,9 +532,7 @@ private:
     uint32_t* chr6[6] = {};
     uint32_t* hint[4] = {};
     int32_t* d_seeds = nullptr;
-    int32_t* h_seeds[2] = {};
-    cudaEvent_t seed_ev[2] = {};
-    int seed_buf = 0;
+    std::vector<int32_t> seed_words;
     bool seeds_from_device = false;
     cudaGraphExec_t graph_exec = nullptr;
     uint64_t graph_launches = 0;
@@ -742,6 +788,53 @@ AMR_API int amr_sim_copy_to_host_side(amr_sim* s, int which, int comp, void* hos
     b->side_pending[which][comp] = true;
     return AMR_OK;
 }
+AMR_API int amr_sim_stage_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count) {
+    if (!s || !host || which < 0 || which >= 6 || comp < 0 || comp >= 6) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    void* dev = nullptr;
+    uint64_t n = 0;
+    int st = b->buffer(which, comp, &dev, &n);
+    if (st) return st;
+    if (count > n) return AMR_ERR_INVALID;
+    if (count == 0) return AMR_OK;
+    SimBase::Staging& u = b->up[which][comp];
+    if ((st = b->ensure_transfer_streams()) || (st = u.ensure(n))) return st;
+    // host -> staging on the upload stream, once the staging copy's previous contents are in place
+    cudaError_t e = cudaStreamWaitEvent(b->up_stream, u.copied, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(u.buf, host, count * 4u, cudaMemcpyHostToDevice, b->up_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(u.moved, b->up_stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    // staging -> buffer on the simulation's stream, after everything enqueued there so far and a
+    // side read of the buffer
+    if ((st = b->wait_side(which, comp))) return st;
+    e = cudaStreamWaitEvent(b->stream, u.moved, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dev, u.buf, count * 4u, cudaMemcpyDeviceToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(u.copied, b->stream);
+    return cuda_status(e);
+}
+AMR_API int amr_sim_snapshot_to_host(amr_sim* s, int which, int comp, void* host, uint64_t count) {
+    if (!s || !host || which < 0 || which >= 6 || comp < 0 || comp >= 6) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    void* dev = nullptr;
+    uint64_t n = 0;
+    int st = b->buffer(which, comp, &dev, &n);
+    if (st) return st;
+    if (count > n) return AMR_ERR_INVALID;
+    if (count == 0) return AMR_OK;
+    SimBase::Staging& d = b->down[which][comp];
+    if ((st = b->ensure_transfer_streams()) || (st = d.ensure(n))) return st;
+    // buffer -> staging on the simulation's stream, once the previous snapshot has left it
+    cudaError_t e = d.pending ? cudaStreamWaitEvent(b->stream, d.moved, 0) : cudaSuccess;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.buf, dev, count * 4u, cudaMemcpyDeviceToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(d.copied, b->stream);
+    // staging -> host on the download stream
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->down_stream, d.copied, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, d.buf, count * 4u, cudaMemcpyDeviceToHost, b->down_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(d.moved, b->down_stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    d.pending = true;
+    return AMR_OK;
+}
 AMR_API int amr_sim_copy_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count) {
     return sim_copy(s, which, comp, const_cast<void*>(host), count, true);
 }
@@ -751,7 +844,8 @@ AMR_API int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, ui
 AMR_API int amr_sim_event_record(amr_sim* s, int slot) {
     if (!s || slot < 0 || slot >= 16) return AMR_ERR_INVALID;
     SimBase* b = s->impl;
-    const int st0 = b->wait_side(-1, 0);   // the event follows side copies too
+    int st0 = b->wait_side(-1, 0);   // the event follows side copies and snapshot downloads too
+    if (!st0) st0 = b->wait_snapshots();
     if (st0) return st0;
     if (!b->user_events[slot]) {
         const int st = cuda_status(cudaEventCreate(&b->user_events[slot]));
@@ -794,7 +888,7 @@ int sim_kind(const SimBase* b) { return dynamic_cast<const WaveSim*>(b) ? AMR_SI
 AMR_API int amr_sim_save(amr_sim* s, const char* dir) {
     if (!s || !dir) return AMR_ERR_INVALID;
     SimBase* b = s->impl;
-    int st = b->side_stream ? cuda_status(cudaStreamSynchronize(b->side_stream)) : AMR_OK;
+    int st = b->sync_transfer_streams();
     if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
     if (st) return st;
     const std::string d(dir);
@@ -831,7 +925,7 @@ AMR_API int amr_sim_save(amr_sim* s, const char* dir) {
 AMR_API int amr_sim_load(amr_sim* s, const char* dir) {
     if (!s || !dir) return AMR_ERR_INVALID;
     SimBase* b = s->impl;
-    int st = b->side_stream ? cuda_status(cudaStreamSynchronize(b->side_stream)) : AMR_OK;
+    int st = b->sync_transfer_streams();
     if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
     if (st) return st;
     const std::string d(dir);
@@ -907,7 +1001,7 @@ AMR_API int amr_sim_stream(amr_sim* s, void** stream) {
 }
 AMR_API int amr_sim_synchronize(amr_sim* s) {
     if (!s) return AMR_ERR_INVALID;
-    int st = s->impl->side_stream ? cuda_status(cudaStreamSynchronize(s->impl->side_stream)) : AMR_OK;
+    int st = s->impl->sync_transfer_streams();
     if (st) return st;
     st = cuda_status(cudaStreamSynchronize(s->impl->stream));
     if (st) return st;

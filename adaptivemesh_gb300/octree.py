@@ -122,6 +122,20 @@ class Sim:
         addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
         check(load().amr_sim_copy_to_host_side(self.h, which, comp, addr, n), "amr_sim_copy_to_host_side")
 
+    def stage_to_device(self, which: int, comp: int, host, count: int | None = None) -> None:
+        """Upload through the buffer's staging copy (amr_sim_stage_to_device): the host transfer
+        overlaps work already enqueued; the buffer receives it after that work."""
+        n = host.numel() if count is None and hasattr(host, "numel") else (count if count is not None else host.size)
+        addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
+        check(load().amr_sim_stage_to_device(self.h, which, comp, addr, n), "amr_sim_stage_to_device")
+
+    def snapshot_to_host(self, which: int, comp: int, host, count: int | None = None) -> None:
+        """Download through a device snapshot (amr_sim_snapshot_to_host): the host transfer
+        overlaps later work, which may overwrite the buffer at once."""
+        n = host.numel() if count is None and hasattr(host, "numel") else (count if count is not None else host.size)
+        addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
+        check(load().amr_sim_snapshot_to_host(self.h, which, comp, addr, n), "amr_sim_snapshot_to_host")
+
     def event_record(self, slot: int) -> None:
         check(load().amr_sim_event_record(self.h, slot), "amr_sim_event_record")
 

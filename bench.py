@@ -12,8 +12,9 @@ Metric: zone-cycles/s = 512 * 16^3 leaf zones x steps / seconds (covered parents
   e2e    the same metric through the C ABI with host buffers: every step uploads its input (the
          new metric; the old one is rewritten from it by the step's first phase) from pinned host
          memory and downloads new metric, gradients, Christoffel symbols and traces to pinned host
-         memory, inside the timed region (downloads on the simulation's side stream, the derived
-         outputs overlapping the next upload)
+         memory, inside the timed region.  The transfers go through device staging copies
+         (amr_sim_stage_to_device / amr_sim_snapshot_to_host): the next step's input is uploaded
+         and this step's output downloaded while the next step computes.
 
 `--impl reference` times the reference path on the CPU: the reference has no CPU solver, so
 this is the oracle's restatement of BSSN_AMR_data::timestep (OpenMP over domains), on a bounded
@@ -256,15 +257,15 @@ def main() -> None:
     d2h = sum(t.numel() * 4 for t in h_out)
 
     def upload():
+        # host -> staging at once (overlapping the work enqueued so far), staging -> buffer on the
+        # simulation's stream after that work
         for (w, k), h in zip(ins, h_in):
-            sim.copy_to_device(w, k, h)
+            sim.stage_to_device(w, k, h)
 
     def download():
-        # on the simulation's side stream: the next step's upload of `new` waits only for the
-        # download of `new`, and overlaps the derived outputs' download (the next timestep waits
-        # for all of them)
+        # buffer -> staging on the simulation's stream, staging -> host overlapping later work
         for (w, k, n), h in zip(outs, h_out):
-            sim.copy_to_host_side(w, k, h)
+            sim.snapshot_to_host(w, k, h)
 
     upload()
     sim.synchronize()
@@ -297,18 +298,19 @@ def main() -> None:
     progress("e2e")
     # ---- end to end through the C ABI with host buffers (e2e)
 
-    def e2e_step():
-        upload()
-        sim.timestep()
-        download()
+    def e2e_steps(k):
+        upload()                  # the first step's input
+        for i in range(k):
+            sim.timestep()
+            download()            # this step's output ...
+            if i + 1 < k:
+                upload()          # ... and the next step's input, both moving while it computes
 
-    for _ in range(args.warmup):
-        e2e_step()
+    e2e_steps(args.warmup)
     barrier()
     sim.event_record(2)
-    for _ in range(args.steps):
-        e2e_step()
-    sim.event_record(3)
+    e2e_steps(args.steps)
+    sim.event_record(3)           # follows the last step's downloads
     barrier()
     ms_e2e = sim.event_elapsed(2, 3)
     e2e_value = zones * args.steps * world / (ms_e2e / 1e3)

@@ -214,6 +214,21 @@ int amr_sim_copy_to_host(amr_sim* s, int which, int comp, void* host, uint64_t c
  * next timestep, copy_bounds, add_node or upload into this buffer waits for it.  Completion:
  * amr_sim_synchronize. */
 int amr_sim_copy_to_host_side(amr_sim* sim, int which, int comp, void* host, uint64_t count);
+/* Transfers that overlap the simulation's work (no counterpart in the reference, whose copies
+ * block).  Each buffer has a device staging copy per direction; host transfers run on an upload
+ * and a download stream, and the simulation's stream meets them only at a device-to-device copy.
+ *   amr_sim_stage_to_device: host -> staging starts at once (after the staging copy's previous
+ *     contents were taken), and staging -> buffer is enqueued on the simulation's stream after the
+ *     work already there.  Calling it right after amr_sim_timestep uploads the next step's input
+ *     while this step computes.
+ *   amr_sim_snapshot_to_host: buffer -> staging is enqueued on the simulation's stream (the next
+ *     timestep may overwrite the buffer at once), staging -> host follows on the download stream,
+ *     overlapping later work.
+ * `host` must stay valid (and, for uploads, unchanged) until the transfer is complete:
+ * amr_sim_synchronize, or an amr_sim_event_record (which follows the downloads) that has
+ * completed. */
+int amr_sim_stage_to_device(amr_sim* sim, int which, int comp, const void* host, uint64_t count);
+int amr_sim_snapshot_to_host(amr_sim* sim, int which, int comp, void* host, uint64_t count);
 /* Checkpoint of a simulation into the existing directory `dir`: the octree arrays
  * (positions.bin, parent.bin, children.bin, boundaries.bin, lifetime.bin), every field buffer
  * amr_sim_buffer names (field_<which>_<comp>.bin), each the raw little-endian bytes of the whole

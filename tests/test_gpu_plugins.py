@@ -343,3 +343,49 @@ def test_side_reads_match_plain_reads(am, cuda):
     for k in range(6):
         _same(side[k].numpy(), plain[k].numpy(), f"chr{k} side vs plain read")
     sim.close()
+
+
+@pytest.mark.gpu
+def test_staged_transfers_match_plain_copies(am, cuda):
+    """Uploads through staging and downloads through snapshots, each overlapping the next step
+    (the benchmark's end-to-end loop), give every step the same input and output as blocking
+    copies on the simulation's stream; each step gets a different input."""
+    import torch
+    cfg = am.Config(16, 3, 100.0)
+    steps = 3
+    plain, st, metric = _bssn_sim(am, cfg, "uneven", am.MODE_GRAPH)
+    staged, _, _ = _bssn_sim(am, cfg, "uneven", am.MODE_GRAPH)
+    used = st["used_slots"]
+    n_pad, n_in = used * cfg.padded_cells, used * cfg.inner_cells
+    rng = np.random.default_rng(11)
+    inputs = [[torch.from_numpy((metric[k] * (1.0 + 0.01 * rng.standard_normal(metric[k].shape))).astype(np.float32))
+               .pin_memory() for k in range(6)] for _ in range(steps)]
+    outs = [(am.Sim.NEW, n_pad, torch.float32)] + [(w, n_in, torch.int32) for w in (am.Sim.DMET, am.Sim.CHR)] + \
+           [(am.Sim.RICCI, n_in, torch.float32)]
+    want = [[[torch.empty(n, dtype=dt, pin_memory=True) for _ in range(6)] for (_, n, dt) in outs] for _ in range(steps)]
+    got = [[[torch.empty(n, dtype=dt, pin_memory=True) for _ in range(6)] for (_, n, dt) in outs] for _ in range(steps)]
+    for i in range(steps):
+        for k in range(6):
+            plain.copy_to_device(am.Sim.NEW, k, inputs[i][k])
+        plain.timestep()
+        for o, (w, n, _) in enumerate(outs):
+            for k in range(6):
+                plain.copy_to_host(w, k, want[i][o][k])
+    plain.synchronize()
+    for k in range(6):
+        staged.stage_to_device(am.Sim.NEW, k, inputs[0][k])
+    for i in range(steps):
+        staged.timestep()
+        for o, (w, n, _) in enumerate(outs):
+            for k in range(6):
+                staged.snapshot_to_host(w, k, got[i][o][k])
+        if i + 1 < steps:
+            for k in range(6):
+                staged.stage_to_device(am.Sim.NEW, k, inputs[i + 1][k])
+    staged.synchronize()
+    for i in range(steps):
+        for o, (w, _, _) in enumerate(outs):
+            for k in range(6):
+                _same(got[i][o][k].numpy(), want[i][o][k].numpy(), f"step {i} buffer {w} comp {k}: staged vs plain")
+    plain.close()
+    staged.close()
