@@ -306,4 +306,49 @@ cudaError_t launch_store_words(int32_t* dst, const int32_t* words, uint32_t n, c
     return cudaSuccess;
 }
 
+// ---------------------------------------------------------------- device-to-device copy
+namespace {
+// n4 float4 with four loads in flight per thread, then the n % 4 trailing words
+__global__ void __launch_bounds__(kBlock) k_copy_words4(float4* __restrict__ dst, const float4* __restrict__ src,
+                                                       uint64_t n4, float* __restrict__ dtail,
+                                                       const float* __restrict__ stail, uint32_t ntail) {
+    const uint64_t stride = (uint64_t)gridDim.x * kBlock;
+    uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        const float4 a = __ldcs(src + i), b = __ldcs(src + i + stride), c = __ldcs(src + i + 2 * stride),
+                     d = __ldcs(src + i + 3 * stride);
+        __stcs(dst + i, a); __stcs(dst + i + stride, b); __stcs(dst + i + 2 * stride, c); __stcs(dst + i + 3 * stride, d);
+    }
+    for (; i < n4; i += stride) __stcs(dst + i, __ldcs(src + i));
+    if (blockIdx.x == 0 && threadIdx.x < ntail) dtail[threadIdx.x] = stail[threadIdx.x];
+}
+__global__ void __launch_bounds__(kBlock) k_copy_words1(float* __restrict__ dst, const float* __restrict__ src, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kBlock) dst[i] = src[i];
+}
+}  // namespace
+
+cudaError_t launch_copy_words(void* dst, const void* src, uint64_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const uint32_t cap = (uint32_t)sms * 8u;
+    if ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 16u == 0u) {
+        const uint64_t n4 = n / 4u;
+        const uint32_t want = (uint32_t)((n4 + 4u * kBlock - 1u) / (4u * kBlock));
+        const uint32_t grid = want < 1u ? 1u : (want < cap ? want : cap);
+        k_copy_words4<<<grid, kBlock, 0, st>>>(static_cast<float4*>(dst), static_cast<const float4*>(src), n4,
+                                              static_cast<float*>(dst) + n4 * 4u,
+                                              static_cast<const float*>(src) + n4 * 4u, (uint32_t)(n % 4u));
+    } else {
+        const uint32_t want = blocks_for(n);
+        k_copy_words1<<<want < cap ? want : cap, kBlock, 0, st>>>(static_cast<float*>(dst), static_cast<const float*>(src), n);
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace amr

@@ -808,8 +808,9 @@ AMR_API int amr_sim_stage_to_device(amr_sim* s, int which, int comp, const void*
     // side read of the buffer
     if ((st = b->wait_side(which, comp))) return st;
     e = cudaStreamWaitEvent(b->stream, u.moved, 0);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dev, u.buf, count * 4u, cudaMemcpyDeviceToDevice, b->stream);
+    if (e == cudaSuccess) e = launch_copy_words(dev, u.buf, count, b->stream);
     if (e == cudaSuccess) e = cudaEventRecord(u.copied, b->stream);
+    b->launches++;
     return cuda_status(e);
 }
 AMR_API int amr_sim_snapshot_to_host(amr_sim* s, int which, int comp, void* host, uint64_t count) {
@@ -825,8 +826,9 @@ AMR_API int amr_sim_snapshot_to_host(amr_sim* s, int which, int comp, void* host
     if ((st = b->ensure_transfer_streams()) || (st = d.ensure(n))) return st;
     // buffer -> staging on the simulation's stream, once the previous snapshot has left it
     cudaError_t e = d.pending ? cudaStreamWaitEvent(b->stream, d.moved, 0) : cudaSuccess;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d.buf, dev, count * 4u, cudaMemcpyDeviceToDevice, b->stream);
+    if (e == cudaSuccess) e = launch_copy_words(d.buf, dev, count, b->stream);
     if (e == cudaSuccess) e = cudaEventRecord(d.copied, b->stream);
+    b->launches++;
     // staging -> host on the download stream
     if (e == cudaSuccess) e = cudaStreamWaitEvent(b->down_stream, d.copied, 0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(host, d.buf, count * 4u, cudaMemcpyDeviceToHost, b->down_stream);

@@ -382,10 +382,16 @@ def test_staged_transfers_match_plain_copies(am, cuda):
         if i + 1 < steps:
             for k in range(6):
                 staged.stage_to_device(am.Sim.NEW, k, inputs[i + 1][k])
+    # a count that is not a multiple of four words (the copies' tail) and a host buffer that is
+    # not 16-byte aligned
+    part = torch.zeros(n_in + 1, dtype=torch.int32, pin_memory=True)
+    staged.snapshot_to_host(am.Sim.CHR, 5, part[1:], n_in - 3)
     staged.synchronize()
     for i in range(steps):
         for o, (w, _, _) in enumerate(outs):
             for k in range(6):
                 _same(got[i][o][k].numpy(), want[i][o][k].numpy(), f"step {i} buffer {w} comp {k}: staged vs plain")
+    _same(part[1:n_in - 2].numpy(), want[-1][2][5][:n_in - 3].numpy(), "partial snapshot")
+    assert int(part[0]) == 0 and int(part[n_in - 2]) == 0 and int(part[n_in]) == 0, "snapshot wrote outside its count"
     plain.close()
     staged.close()
