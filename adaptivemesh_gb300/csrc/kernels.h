@@ -10,8 +10,9 @@
 // Compiled (size_domain, padding_domain) pairs.  (28, 2) is the reference as shipped; (16, 3) and
 // (32, 3) are the benchmark sizes; (8, 2) keeps small test cases cheap.
 #define AMR_FOR_EACH_CONFIG(X) X(16, 3) X(28, 2) X(32, 3) X(8, 2)
-// Pairs whose six-component fused kernel fits in shared memory (six rings of 2p+2 padded planes).
-#define AMR_FOR_EACH_BSSN_CONFIG(X) X(16, 3) X(28, 2) X(8, 2)
+// Pairs with the six-component fused kernel (six rings of 2p+2 padded planes, or of half-plane
+// tiles for 32^3 domains).
+#define AMR_FOR_EACH_BSSN_CONFIG(X) X(16, 3) X(28, 2) X(32, 3) X(8, 2)
 
 namespace amr {
 

@@ -34,15 +34,33 @@ struct StencilShape {
     static constexpr int R = KIND == SK_BSSN ? 2 * P + 2 : 2 * P + 3;
     static constexpr uint32_t PLANE = (uint32_t)(T * T);         // floats per plane
     static constexpr uint32_t PLANE_BYTES = PLANE * 4u;
-    static constexpr size_t RING_BYTES = (size_t)NC * R * PLANE_BYTES;
+    // SK_BSSN works on y-tiles of TY interior rows: the whole plane, or half of it where six
+    // components' rings of whole planes would not fit in shared memory (32^3 domains).  A tile's
+    // padded rows (TY + 2P of them) are contiguous in the plane, so it moves as one bulk copy.
+    static constexpr int TY = KIND == SK_BSSN && N * N > 1024 - 32 ? N / 2 : N;
+    static constexpr int NT = N / TY;                                   // tiles per plane
+    static constexpr uint32_t TILE = (uint32_t)((TY + 2 * P) * T);      // floats per tile plane
+    static constexpr uint32_t TILE_BYTES = TILE * 4u;
+    static constexpr uint32_t CELLS = (uint32_t)(N * TY);               // interior cells per tile plane
+    // The leaves' restriction stores tile 0's padded rows [0, OWN0) and tile 1's [OWN0, T): the
+    // first row boundary past tile 0's interior at which both parts are 16-byte aligned.
+    static constexpr int own0() {
+        int r = TY + P;
+        while ((r * T * 4) % 16 != 0) r++;
+        return r;
+    }
+    static constexpr int OWN0 = NT == 1 ? T : own0();
+    static constexpr size_t RING_BYTES = (size_t)NC * R * (KIND == SK_BSSN ? TILE_BYTES : PLANE_BYTES);
     static constexpr size_t BAR_BYTES = (size_t)R * 8u * (KIND == SK_BSSN ? 2u : 1u);   // full (+ empty) per slot
-    // SK_BSSN runs warp-specialised: ceil(N^2 / 32) compute warps (thread (x, y) per column) and one
-    // producer warp that streams the planes
-    static constexpr uint32_t CW = (uint32_t)(N * N + 31) / 32u;
+    // SK_BSSN runs warp-specialised: ceil(CELLS / 32) compute warps (thread (x, y) per column of the
+    // tile) and one producer warp that streams the planes
+    static constexpr uint32_t CW = (CELLS + 31u) / 32u;
     static constexpr uint32_t THREADS = KIND == SK_BSSN ? 32u * (CW + 1u) : (uint32_t)(N * N);
     // SK_BSSN: per thread, the 13 generator prefixes (d0, m0, d1, m1, ..., c) and the six gradient words
-    static constexpr size_t TABLE_BYTES = KIND == SK_BSSN ? (size_t)(13 + 6) * N * N * 4u : 0u;
+    static constexpr size_t TABLE_BYTES = KIND == SK_BSSN ? (size_t)(13 + 6) * CELLS * 4u : 0u;
     static constexpr size_t SMEM = RING_BYTES + BAR_BYTES + TABLE_BYTES;
+    static_assert(N % TY == 0 && TILE_BYTES % 16u == 0u && (TY * T * 4) % 16 == 0, "tiles are aligned bulk copies");
+    static_assert(NT == 1 || (OWN0 <= TY + 2 * P && OWN0 >= TY), "restriction rows lie in their tile");
     static constexpr uint32_t Q = N >= 16 ? 4u : 2u;              // z-ranges per split domain
     static_assert(N % Q == 0, "split domains into whole planes");
     static_assert(PLANE_BYTES % 16u == 0u, "bulk copies move whole planes of 16-byte multiples");
@@ -381,7 +399,7 @@ __device__ __forceinline__ void bssn_cell(const StencilArgs& a, const float* rin
                                           float dx2, uint32_t tid, const int32_t* s_pre, uint32_t* s_grad) {
     using S = StencilShape<N, P, SK_BSSN>;
     constexpr int T = S::T, R = S::R;
-    constexpr uint32_t PLANE = S::PLANE, NN = N * N;
+    constexpr uint32_t PLANE = S::TILE, NN = S::CELLS;   // ring slots hold tile planes
     const size_t cz = (size_t)slot[P] * PLANE + c0;
     const Sym g{ring[0 * R * PLANE + cz], ring[1 * (size_t)R * PLANE + cz], ring[2 * (size_t)R * PLANE + cz],
                 ring[3 * (size_t)R * PLANE + cz], ring[4 * (size_t)R * PLANE + cz], ring[5 * (size_t)R * PLANE + cz]};
@@ -437,9 +455,10 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
     k_stencil_bssn(const __grid_constant__ StencilArgs a) {
     using S = StencilShape<N, P, SK_BSSN>;
     constexpr int T = S::T, NC = 6, R = S::R;
-    constexpr uint32_t PLANE = S::PLANE, NN = N * N, CW = S::CW;
+    constexpr uint32_t PLANE = S::PLANE, TILE = S::TILE, NN = S::CELLS, CW = S::CW;
+    constexpr uint32_t TY = S::TY, NT = S::NT;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* ring = reinterpret_cast<float*>(smem_raw);
+    float* ring = reinterpret_cast<float*>(smem_raw);   // [component][slot] tile planes
     uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + S::RING_BYTES);
     uint64_t* empty = full + R;
     int32_t* s_pre = reinterpret_cast<int32_t*>(smem_raw + S::RING_BYTES + S::BAR_BYTES);   // [13][NN]
@@ -454,16 +473,18 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
     }
     __syncthreads();   // the only CTA-wide barrier: the producer warp leaves the compute loop
 
-    // Work: the items' interior planes, item after item, cut into gridDim.x contiguous ranges of
-    // equal length (to a plane), one per CTA.  A range is walked as units -- consecutive planes of
-    // one domain -- whose padded planes (the unit's planes and P more on either side) stream
-    // through the ring.
-    const uint64_t n_planes = (uint64_t)a.n_items * N;
+    // Work: the items' interior tile planes (item after item, tile after tile, z last), cut into
+    // gridDim.x contiguous ranges of equal length (to a plane), one per CTA.  A range is walked as
+    // units -- consecutive planes of one tile of one domain -- whose padded planes (the unit's
+    // planes and P more on either side) stream through the ring.
+    const uint64_t n_planes = (uint64_t)a.n_items * NT * N;
     const uint32_t p_begin = (uint32_t)((uint64_t)blockIdx.x * n_planes / gridDim.x);
     const uint32_t p_end = (uint32_t)(((uint64_t)blockIdx.x + 1u) * n_planes / gridDim.x);
-    auto unit_of = [&](uint32_t p, uint32_t& item, uint32_t& z0, uint32_t& nz) {
-        item = p / N;
-        z0 = p - item * N;
+    auto unit_of = [&](uint32_t p, uint32_t& item, uint32_t& tile, uint32_t& z0, uint32_t& nz) {
+        item = p / (NT * N);
+        const uint32_t r = p - item * (NT * N);
+        tile = r / N;
+        z0 = r - tile * N;
         nz = min((uint32_t)N - z0, p_end - p);
     };
     auto active_node = [&](uint32_t item, uint32_t& node, int& depth) {
@@ -475,8 +496,8 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
         while (p < p_end) {
             uint32_t node;
             int depth;
-            if (active_node(p / N, node, depth)) break;
-            p = (p / N + 1u) * N;
+            if (active_node(p / (NT * N), node, depth)) break;
+            p = (p / (NT * N) + 1u) * (NT * N);
         }
         return min(p, p_end);
     };
@@ -493,22 +514,22 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
         uint32_t q = 0;   // planes requested
         bool ok = true;
         for (uint32_t u = next_unit(p_begin), nz = 0; ok && u < p_end; u = next_unit(u + nz)) {
-            uint32_t item, z0, node;
+            uint32_t item, tile, z0, node;
             int depth;
-            unit_of(u, item, z0, nz);
+            unit_of(u, item, tile, z0, nz);
             active_node(item, node, depth);
             const bool leaf = fused_leaf(node);
-            const size_t src = ((size_t)node * T + z0) * PLANE;
+            const size_t src = ((size_t)node * T + z0) * PLANE + (size_t)tile * TY * T;
             for (uint32_t j = 0; j < nz + 2u * P; j++, q++) {
                 const uint32_t s = q % R;
                 // the slot's previous plane (q - R) must have been released by every compute warp
                 if (q >= (uint32_t)R && !mbar_wait(&empty[s], ((q / R) - 1u) & 1u)) { ok = false; break; }
                 if (s_abort) { ok = false; break; }
-                mbar_arrive_expect_tx(&full[s], NC * S::PLANE_BYTES);
+                mbar_arrive_expect_tx(&full[s], NC * S::TILE_BYTES);
 #pragma unroll
                 for (int k = 0; k < NC; k++)
-                    bulk_g2s(ring + ((size_t)k * R + s) * PLANE, (leaf ? a.leaf_src[k] : a.field[k]) + src + (size_t)j * PLANE,
-                             S::PLANE_BYTES, &full[s]);
+                    bulk_g2s(ring + ((size_t)k * R + s) * TILE, (leaf ? a.leaf_src[k] : a.field[k]) + src + (size_t)j * PLANE,
+                             S::TILE_BYTES, &full[s]);
             }
         }
         if (!ok) {   // abort: let the copies in flight land before the CTA's shared memory goes
@@ -519,27 +540,32 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
         return;
     }
 
-    // ---------------- compute warps: thread (x, y) per column; the last warp may be partial
+    // ---------------- compute warps: thread (x, ty) per column of the tile; the last warp may be
+    // partial.  At N = 16 a warp takes rows ty and ty + 8 (176 floats = 16 banks apart), so that
+    // every shared-memory access of the warp is conflict-free.
     const bool lane_active = tid < NN;
     const uint32_t t = lane_active ? tid : 0u;
     const uint32_t x = t % N;
-    const uint32_t y = N == 16 ? ((t / N) >> 1) | (((t / N) & 1u) << 3) : t / N;
-    const int c0 = (int)((y + P) * T + (x + P));
-    if (lane_active) {   // per-cell generators: the part that depends on (seed, x, y) only
-        const int32_t* sp = a.seed_ptr;
-#pragma unroll
-        for (int k = 0; k < NC; k++) {
-            s_pre[(2 * k) * NN + tid] = cell_rng_prefix(sp ? sp[2 * k] : a.seed_d[k], x, y);
-            s_pre[(2 * k + 1) * NN + tid] = cell_rng_prefix(sp ? sp[2 * k + 1] : a.seed_m[k], x, y);
-        }
-        s_pre[12 * NN + tid] = cell_rng_prefix(sp ? sp[12] : a.seed_c, x, y);
-    }
+    const uint32_t ty = N == 16 ? ((t / N) >> 1) | (((t / N) & 1u) << 3) : t / N;
+    const int c0 = (int)((ty + P) * T + (x + P));   // in a ring slot's tile plane
     uint32_t g_base = 0;   // stream index of the current unit's first padded plane
+    uint32_t pre_tile = NT;   // the tile the generator prefixes below are for
     for (uint32_t cu = next_unit(p_begin), nz = 0; cu < p_end; cu = next_unit(cu + nz)) {
-        uint32_t item, z0, node;
+        uint32_t item, tile, z0, node;
         int depth;
-        unit_of(cu, item, z0, nz);
+        unit_of(cu, item, tile, z0, nz);
         active_node(item, node, depth);
+        const uint32_t y = tile * TY + ty;   // the cell's row in the domain
+        if (tile != pre_tile && lane_active) {   // per-cell generators: the part that depends on (seed, x, y) only
+            const int32_t* sp = a.seed_ptr;
+#pragma unroll
+            for (int k = 0; k < NC; k++) {
+                s_pre[(2 * k) * NN + tid] = cell_rng_prefix(sp ? sp[2 * k] : a.seed_d[k], x, y);
+                s_pre[(2 * k + 1) * NN + tid] = cell_rng_prefix(sp ? sp[2 * k + 1] : a.seed_m[k], x, y);
+            }
+            s_pre[12 * NN + tid] = cell_rng_prefix(sp ? sp[12] : a.seed_c, x, y);
+        }
+        pre_tile = tile;
         const float dx1 = a.geo.inv_dx[depth], dx2 = a.geo.inv_dx2[depth];
         const bool leaf = fused_leaf(node);
 #pragma unroll 1
@@ -557,10 +583,13 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
 #pragma unroll
             for (int j = 0; j <= 2 * P; j++) slot[j] = base_s + j >= (uint32_t)R ? base_s + j - R : base_s + j;
             // fused restriction: each padded plane of a leaf goes to field[k] once -- by the unit
-            // whose interior it is, the end units also taking the ghost planes beyond -- stored out
-            // of the ring by lane 0 of one compute warp per plane, in turn
+            // whose interior it is, the end units also taking the ghost planes beyond; of a plane,
+            // each tile stores its rows [row0, row1) -- stored out of the ring by lane 0 of one
+            // compute warp per plane, in turn
             const bool storer = leaf && tid == 32u * (g % CW);
             if (storer) {
+                const uint32_t row0 = tile == 0u ? 0u : (uint32_t)S::OWN0;
+                const uint32_t row1 = tile + 1u == NT ? (uint32_t)T : (uint32_t)S::OWN0;
                 for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {
                     const uint32_t jj = zl + (uint32_t)j;   // plane index within the unit
                     const bool own = (jj >= P && jj < nz + P) || (z0 == 0 && jj < P) || (z0 + nz == N && jj >= nz + P);
@@ -568,8 +597,8 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <=
                     const uint32_t sl = base_s + (uint32_t)j >= (uint32_t)R ? base_s + j - R : base_s + j;
 #pragma unroll
                     for (int k = 0; k < NC; k++)
-                        bulk_s2g(const_cast<float*>(a.field[k]) + ((size_t)node * T + z0 + jj) * PLANE,
-                                 ring + ((size_t)k * R + sl) * PLANE, S::PLANE_BYTES);
+                        bulk_s2g(const_cast<float*>(a.field[k]) + ((size_t)node * T + z0 + jj) * PLANE + (size_t)row0 * T,
+                                 ring + ((size_t)k * R + sl) * TILE + (size_t)(row0 - tile * TY) * T, (row1 - row0) * T * 4u);
                 }
                 bulk_commit();
             }

@@ -39,7 +39,12 @@ sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 N, P, OUTER, DEPTH = 16, 3, 100.0, 3
 METRIC = "BSSN zone-cycles/s"
 UNIT = "zone-cycles/s"
-WORKLOAD = "BSSN fragment timestep (reference semantics), uniform depth-3 octree: 512 leaf + 73 parent domains of 16^3, padding 3"
+def workload(depth: int = DEPTH) -> str:
+    return (f"BSSN fragment timestep (reference semantics), uniform depth-{depth} octree: {8 ** depth} leaf + "
+            f"{sum(8 ** d for d in range(depth))} parent domains of {N}^3, padding {P}")
+
+
+WORKLOAD = workload()
 
 
 def progress(msg: str) -> None:
@@ -192,9 +197,10 @@ def reference_arm(args) -> None:
     vals = [port.sample() for _ in range(args.steps)]
     v = statistics.median(x["value"] for x in vals)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 512 * N ** 3 / v * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 8 ** args.depth * N ** 3 / v * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "leaf_domains": 512, "zones_per_domain": N ** 3, "parallelism": "replicas"},
+            "config": {"workload": workload(args.depth), "leaf_domains": 8 ** args.depth, "zones_per_domain": N ** 3,
+                       "parallelism": "replicas"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
                              "sample": vals[0]["sample"]},
@@ -203,6 +209,7 @@ def reference_arm(args) -> None:
 
 
 def main() -> None:
+    global N, P
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -212,7 +219,10 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--depth", type=int, default=DEPTH, help="uniform octree depth (3 = the benchmark workload)")
+    ap.add_argument("--size", type=int, default=N, help="size_domain (16 = the benchmark workload; 8, 16, 28, 32)")
+    ap.add_argument("--padding", type=int, default=P, help="padding_domain (3 = the benchmark workload)")
     args = ap.parse_args()
+    N, P = args.size, args.padding
     if args.impl == "reference":
         reference_arm(args)
         return
@@ -243,6 +253,7 @@ def main() -> None:
     metric = cases.metric_fields(xyz, OUTER, 500)
     T3 = cfg.total ** 3
     padded, inner = used * T3, used * N ** 3
+    state_mb = 12 * padded * 4 / 1e6   # old and new, six components each
     # host buffers (page-locked) of the state and of the step's outputs; every copy goes through
     # the C ABI on the simulation's stream
     # A timestep's inputs are the six `new` fields: its first phase (restriction at substep 0, when
@@ -339,9 +350,11 @@ def main() -> None:
     pk = peaks()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"] if achieved else None, "traffic": None,
-                "kernel": "k_stencil_bssn<16,3> (fused BSSN derivatives)", "peak_source": pk["source"],
+                "kernel": f"k_stencil_bssn<{N},{P}> (fused BSSN derivatives)", "peak_source": pk["source"],
                 "avg_launch_ms": k_ms / k_n if k_n else None, "launches_timed": k_n}
     try:   # DRAM bytes per domain from an ncu capture of the same kernel and workload, scaled per launch
+        if (N, P) != (16, 3):
+            raise OSError("the capture is of the 16/3 workload")
         with open(os.path.join(ROOT, "profiles", "k_stencil_bssn_16p3.traffic.json")) as f:
             tr = json.load(f)
         roofline["traffic"] = (tr["corrector_dram_bytes_per_domain"] * per_step / 2 +
@@ -352,9 +365,9 @@ def main() -> None:
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "leaf_domains": 512 * world, "zones_per_domain": N ** 3,
-                       "parallelism": "replicas" if world > 1 else "single", "mode": args.mode,
-                       "l2": "state 299 MB > L2 129 MB, no flush"},
+            "config": {"workload": workload(args.depth), "leaf_domains": zones // N ** 3 * world,
+                       "zones_per_domain": N ** 3, "parallelism": "replicas" if world > 1 else "single",
+                       "mode": args.mode, "l2": f"state {state_mb:.0f} MB > L2 129 MB, no flush"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": ms_e2e / args.steps},
             "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clocks.summary()}

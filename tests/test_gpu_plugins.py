@@ -55,7 +55,7 @@ def _same(a, b, what):
     assert bad == 0, f"{what}: {bad} of {a.size} words differ"
 
 
-@pytest.mark.parametrize("n,p,tree", [(16, 3, "wave"), (16, 3, "bssn"), (28, 2, "uneven")])
+@pytest.mark.parametrize("n,p,tree", [(16, 3, "wave"), (16, 3, "bssn"), (28, 2, "uneven"), (32, 3, "uneven")])
 def test_bssn_modes_agree(am, cuda, n, p, tree):
     cfg = am.Config(n, p, 100.0)
     results = []
@@ -138,15 +138,17 @@ def test_bssn_timestep_matches_reference_plugin(am, cuda, ref16, steps):
     sim.close()
 
 
-def test_bssn_timestep_matches_oracle(am, cuda, orc):
-    cfg = am.Config(16, 3, 100.0)
+@pytest.mark.parametrize("n,p", [(16, 3), (32, 3)])
+def test_bssn_timestep_matches_oracle(am, cuda, orc, n, p):
+    """One batched timestep (the fused pass; half-plane tiles at 32^3) against the oracle."""
+    cfg = am.Config(n, p, 100.0)
     sim, st, metric = _bssn_sim(am, cfg, "uneven", am.MODE_BATCHED)
     seed0 = sim.rng
     sim.timestep()
     sim.synchronize()
     mine = _dump(am, sim, st, cfg)
-    used, n = st["used_slots"], 16
-    c = orc.cfg(16, 3, 100.0)
+    used = st["used_slots"]
+    c = orc.cfg(n, p, 100.0)
     old6 = [m.copy() for m in metric]
     new6 = [m.copy() for m in metric]
     dm = [np.zeros(used * n ** 3, np.uint32) for _ in range(6)]
