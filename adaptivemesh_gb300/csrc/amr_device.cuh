@@ -317,12 +317,10 @@ template <> struct FD<3> {
 
 // ------------------------------------------------------------------ 10-point interpolation (AMR.h:672-699)
 // d points at the nearest source cell; strides 1, sy, sz; r = offset from it in cells.
-template <class S>
-__device__ __forceinline__ float interp10_strided(const float* __restrict__ d, S sy, S sz, float rx, float ry, float rz) {
-    const float f = d[0];
-    float fx = d[1], fy = d[sy], fz = d[sz];
-    float fxx = d[-1], fyy = d[-sy], fzz = d[-sz];
-    float fxy = d[sy + 1], fxz = d[sz + 1], fyz = d[sz + sy];
+// The arithmetic of the 10-point interpolation on its loaded taps: f at the nearest cell, fx/fy/fz
+// one cell up and fxx/fyy/fzz one cell down each axis, fxy/fxz/fyz the three upper diagonals.
+__device__ __forceinline__ float interp10_taps(float f, float fx, float fy, float fz, float fxx, float fyy, float fzz,
+                                              float fxy, float fxz, float fyz, float rx, float ry, float rz) {
     fxy = __fadd_rn(fxy, __fsub_rn(__fsub_rn(f, fx), fy));
     fxz = __fadd_rn(fxz, __fsub_rn(__fsub_rn(f, fx), fz));
     fyz = __fadd_rn(fyz, __fsub_rn(__fsub_rn(f, fy), fz));
@@ -339,6 +337,10 @@ __device__ __forceinline__ float interp10_strided(const float* __restrict__ d, S
     acc = __fmaf_rn(__fmul_rn(fxz, rx), rz, acc);
     acc = __fmaf_rn(__fmul_rn(fyz, ry), rz, acc);
     return acc;
+}
+template <class S>
+__device__ __forceinline__ float interp10_strided(const float* __restrict__ d, S sy, S sz, float rx, float ry, float rz) {
+    return interp10_taps(d[0], d[1], d[sy], d[sz], d[-1], d[-sy], d[-sz], d[sy + 1], d[sz + 1], d[sz + sy], rx, ry, rz);
 }
 // interp10_strided on two fields at once: d holds (a, b) pairs, the result is
 // (interp10_strided(a), interp10_strided(b)), each lane the same operation sequence.

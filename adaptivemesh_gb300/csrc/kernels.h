@@ -92,8 +92,13 @@ cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t ch
 // Staging for the ghost fill (the innermost layer of the three lower faces, old and new):
 // 2 * ncomp * 3 * n^2 floats per slot.
 size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp);
+// sources_restricted: the caller guarantees that every domain active at `substep` has had old <- new
+// (restriction) since its new field last changed -- as inside a plugin's timestep, whose phase
+// order is restriction, predictor, ghost fill.  A copy_only_new fill then reads the innermost lower
+// layer of an active source's new field from old (equal before the fill) and writes every ghost
+// value in place, in one launch without staging.
 cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* boundaries, uint32_t used,
                                    uint32_t substep, uint32_t max_depth, int copy_only_new, float* scratch,
-                                   cudaStream_t st);
+                                   cudaStream_t st, bool sources_restricted = false);
 
 }  // namespace amr

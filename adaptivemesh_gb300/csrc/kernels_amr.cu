@@ -219,7 +219,7 @@ struct GhostBox {
 template <int N, int P>
 __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face(const __grid_constant__ FieldSet f, const uint64_t* __restrict__ bds, uint32_t used,
                                                       uint32_t substep, uint32_t max_depth, int copy_only_new,
-                                                      float* __restrict__ stage) {
+                                                      int in_place, float* __restrict__ stage) {
     using G = GhostShape<N, P>;
     constexpr uint32_t T = G::T, BOX = GhostBox<N, P>::MAX;
     extern __shared__ float sbox[];
@@ -237,7 +237,10 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
     const float t0 = __fmul_rn(tm, rel_scale), t1 = __fmul_rn(__fadd_rn(tm, 1.f), rel_scale);
     const uint32_t normal = face % 3u;
     const uint64_t n_staged = (uint64_t)used * G::STAGED;
-    const bool staged_face = face >= 3u;
+    const bool staged_face = face >= 3u && !in_place;
+    // In place (see launch_copy_boundaries): new's innermost lower layer of an active source is
+    // read from old, which holds its value before this fill.
+    const bool redirect = in_place && !root && active_depth(substep, (uint32_t)(j.cd - (int)j.dd), max_depth);
 
     // written coordinate range and source box per axis
     uint32_t wlo[3], whi[3], ext[3];
@@ -271,7 +274,13 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
                                         : (uint64_t)slot * G::CELLS + w[0] + (w[1] + w[2] * T) * T;
             for (int k = 0; k < f.ncomp; k++) {
                 const float od = interp10<T>(f.old_f[k] + rin, r[0], r[1], r[2]);
-                const float nw = interp10<T>(f.new_f[k] + rin, r[0], r[1], r[2]);
+                const float* o = f.old_f[k] + rin;
+                const float* d = f.new_f[k] + rin;
+                constexpr uint32_t T2 = T * T;
+                const float nw = interp10_taps(d[0], d[1], d[T], d[T2], (redirect && ri[0] == P ? o : d)[-1],
+                                               (redirect && ri[1] == P ? o : d)[-(int)T],
+                                               (redirect && ri[2] == P ? o : d)[-(int)T2], d[T + 1], d[T2 + 1],
+                                               d[T2 + T], r[0], r[1], r[2]);
                 float* dst_old = staged ? stage + (uint64_t)k * 2u * n_staged : f.old_f[k];
                 float* dst_new = staged ? stage + ((uint64_t)k * 2u + 1u) * n_staged : f.new_f[k];
                 if (!copy_only_new) dst_old[out] = __fmaf_rn(od, __fsub_rn(1.f, t0), __fmul_rn(nw, t0));
@@ -314,11 +323,16 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
     constexpr uint32_t EPT = (BOX + kBlock - 1) / kBlock;   // box elements per thread, at most
     constexpr bool kCached = EPT <= 8;
     uint32_t e_gi[kCached ? EPT : 1];
+    uint32_t e_low = 0;   // bit e: element e lies in the source's innermost lower layer (redirect only)
+    auto low_layer = [&](uint32_t bx, uint32_t by, uint32_t bz) {
+        return (uint32_t)lo[0] + bx == P - 1u || (uint32_t)lo[1] + by == P - 1u || (uint32_t)lo[2] + bz == P - 1u;
+    };
     if (kCached) {
         uint32_t bx = bx0, by = by0, bz = bz0;
 #pragma unroll
         for (uint32_t e = 0; e < EPT; e++) {
             e_gi[e] = bx + (by + bz * T) * T;
+            if (redirect && low_layer(bx, by, bz)) e_low |= 1u << e;
             bx += A; by += B; bz += C;
             if (bx >= sy) { bx -= sy; by++; }
             if (by >= ext[1]) { by -= ext[1]; bz++; }
@@ -337,7 +351,7 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
                 const uint32_t i = threadIdx.x + e * kBlock;
                 if (i < box) {
                     cp_async4(buf + 2u * i, go + e_gi[kCached ? e : 0]);
-                    cp_async4(buf + 2u * i + 1u, gn + e_gi[kCached ? e : 0]);
+                    cp_async4(buf + 2u * i + 1u, ((e_low >> e) & 1u ? go : gn) + e_gi[kCached ? e : 0]);
                 }
             }
         } else {
@@ -345,7 +359,7 @@ __global__ void __launch_bounds__(kBlock, GhostBox<N, P>::MIN_CTAS) k_ghost_face
             for (uint32_t i = threadIdx.x; i < box; i += kBlock) {
                 const uint32_t gi = bx + (by + bz * T) * T;
                 cp_async4(buf + 2u * i, go + gi);
-                cp_async4(buf + 2u * i + 1u, gn + gi);
+                cp_async4(buf + 2u * i + 1u, (redirect && low_layer(bx, by, bz) ? go : gn) + gi);
                 bx += A; by += B; bz += C;
                 if (bx >= sy) { bx -= sy; by++; }
                 if (by >= ext[1]) { by -= ext[1]; bz++; }
@@ -438,7 +452,8 @@ size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp) {
 }
 cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* boundaries, uint32_t used,
                                    uint32_t substep, uint32_t max_depth, int copy_only_new, float* scratch,
-                                   cudaStream_t st) {
+                                   cudaStream_t st, bool sources_restricted) {
+    const int in_place = copy_only_new && sources_restricted ? 1 : 0;
 #define AMR_GHOST(N, P)                                                                                     \
     if (d.n == N && d.p == P) {                                                                             \
         static bool configured = false;                                                                     \
@@ -450,9 +465,10 @@ cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* bo
         }                                                                                                   \
         if (used == 0 || f.ncomp == 0) return cudaSuccess;                                                  \
         k_ghost_face<N, P><<<used * 6u, kBlock, GhostBox<N, P>::SMEM, st>>>(f, boundaries, used, substep,     \
-                                                                          max_depth, copy_only_new, scratch); \
+                                                                          max_depth, copy_only_new, in_place, \
+                                                                          scratch);                           \
         cudaError_t e = cudaGetLastError();                                                                 \
-        if (e != cudaSuccess) return e;                                                                     \
+        if (e != cudaSuccess || in_place) return e;                                                         \
         k_ghost_commit<N, P><<<blocks_for((uint64_t)used * 3u * N * N), kBlock, 0, st>>>(                   \
             f, boundaries, used, substep, max_depth, copy_only_new, scratch);                               \
         return cudaGetLastError();                                                                          \

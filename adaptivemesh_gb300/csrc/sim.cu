@@ -95,17 +95,22 @@ public:
     virtual int copy_bounds() = 0;
     virtual int corrector() = 0;
     virtual int timestep() {
+        in_timestep = true;
+        int st = AMR_OK;
         do {
-            int st;
-            if ((st = copy_back())) return st;
-            if ((st = modify_nodes())) return st;
-            if ((st = predictor())) return st;
-            if ((st = copy_bounds())) return st;
-            if ((st = corrector())) return st;
+            if ((st = copy_back())) break;
+            if ((st = modify_nodes())) break;
+            if ((st = predictor())) break;
+            if ((st = copy_bounds())) break;
+            if ((st = corrector())) break;
             tree.increment_timer();
         } while (tree.timer() != 0u);
-        return AMR_OK;
+        in_timestep = false;
+        return st;
     }
+    // Set while timestep() runs its substeps: each copy_bounds then follows the substep's copy_back,
+    // so every active domain has old == new outside the cells its children cover.
+    bool in_timestep = false;
     virtual int buffer(int which, int comp, void** ptr, uint64_t* count) = 0;
 
     void node_dtor(int32_t) override {}
@@ -387,8 +392,9 @@ public:
         }
         f.ncomp = 6;
         for (int k = 0; k < 6; k++) { f.old_f[k] = old6[k]; f.new_f[k] = new6[k]; }
-        st = check(launch_copy_boundaries(dims, f, d_boundaries, used, s, md, 1, ghost_stage, stream));
-        if (!st) launches++;
+        // inside a timestep the fill writes in place, in one launch (launch_copy_boundaries)
+        st = check(launch_copy_boundaries(dims, f, d_boundaries, used, s, md, 1, ghost_stage, stream, in_timestep));
+        if (!st && !in_timestep) launches++;   // + the commit launch
         return st;
     }
 
