@@ -24,6 +24,7 @@ LIB_PATH = _build.LIB
 OK = 0
 ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_DEVICE, ERR_CAPACITY = 1, 2, 3, 4, 5
 SIM_BSSN, SIM_WAVE = 1, 2
+DTYPE_UINT32, DTYPE_INT32, DTYPE_FLOAT32 = 0, 1, 2
 MODE_PLAIN, MODE_BATCHED, MODE_GRAPH = 0, 1, 2
 CHRISTOFFEL_REFERENCE, CHRISTOFFEL_RAISED = 0, 1
 
@@ -108,6 +109,9 @@ EXPORTS = {
     "amr_sim_kernel_launches": (U64, [VP]),
     "amr_sim_enable_kernel_timing": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_kernel_timing": (ctypes.c_int, [VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(U64)]),
+    "amr_inclusive_scan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP]),
+    "amr_reduce_max": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP, VP]),
+    "amr_reduce_min": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP, VP]),
 }
 
 _LIB = None

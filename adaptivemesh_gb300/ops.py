@@ -99,3 +99,36 @@ def rasterise(cfg: Config, field, children, used: int, width: int, height: int, 
     check(load().amr_rasterise(ctypes.byref(cfg), _p(field), _p(children), used, width, height, z_slice,
                                1 if bounding_boxes else 0, _p(raster), _s(stream)))
 
+
+
+def _dtype_of(t) -> int:
+    import torch
+    from . import DTYPE_FLOAT32, DTYPE_INT32, DTYPE_UINT32
+    return {torch.float32: DTYPE_FLOAT32, torch.int32: DTYPE_INT32, torch.uint32: DTYPE_UINT32}[t.dtype]
+
+
+def inclusive_scan(data, ncomp: int = 1, stream=None) -> None:
+    """In-place inclusive cumulative sum (apply_incl_cum_sum, AdaptiveMesh/parallel.h:62-82) of a
+    contiguous CUDA tensor of elements of `ncomp` values (float32, int32 or uint32)."""
+    check(load().amr_inclusive_scan(_dtype_of(data), ncomp, _p(data), data.numel() // ncomp, _s(stream)),
+          "amr_inclusive_scan")
+
+
+def reduce_max(data, ncomp: int = 1, stream=None):
+    """Component-wise maximum (find_maximum_val, AdaptiveMesh/parallel.h:239-251); the tensor is
+    used as scratch as by the reference.  Returns a list of `ncomp` values."""
+    return _extreme(load().amr_reduce_max, "amr_reduce_max", data, ncomp, stream)
+
+
+def reduce_min(data, ncomp: int = 1, stream=None):
+    """Component-wise minimum (find_minimum_val, AdaptiveMesh/parallel.h:409-421), with the
+    reference's treatment of a partial last block (its missing elements count as 0)."""
+    return _extreme(load().amr_reduce_min, "amr_reduce_min", data, ncomp, stream)
+
+
+def _extreme(fn, name, data, ncomp, stream):
+    import numpy as np
+    import torch
+    out = np.zeros(ncomp, {torch.float32: np.float32, torch.int32: np.int32, torch.uint32: np.uint32}[data.dtype])
+    check(fn(_dtype_of(data), ncomp, _p(data), data.numel() // ncomp, out.ctypes.data, _s(stream)), name)
+    return out.tolist()

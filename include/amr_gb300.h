@@ -260,6 +260,26 @@ uint64_t amr_sim_kernel_launches(const amr_sim* s);
 int amr_sim_enable_kernel_timing(amr_sim* s, int enable);
 int amr_sim_kernel_timing(amr_sim* s, double* ms, uint64_t* launches);
 
+/* ---------------------------------------------------------------- scan and reductions
+ * The reference's general-purpose device algorithms (AdaptiveMesh/parallel.h) on a device array
+ * of `count` elements (count < 2^32), each `ncomp` (1-4) consecutive values of type `dtype` (the
+ * reference's uint/int/float and their 2-4 component vector types).  The values computed and the
+ * values left in the array are the reference's, float rounding included.  All three run on
+ * `stream` (NULL: the default stream); the reductions return after writing `ncomp` values to
+ * host memory at `result`. */
+#define AMR_DTYPE_UINT32 0
+#define AMR_DTYPE_INT32 1
+#define AMR_DTYPE_FLOAT32 2
+/* In place inclusive cumulative sum, apply_incl_cum_sum (parallel.h:62-82). */
+int amr_inclusive_scan(int dtype, int ncomp, void* data, uint64_t count, void* stream);
+/* Component-wise maximum, find_maximum_val (parallel.h:239-251); the array is used as scratch
+ * as by the reference (elements k * 512^j end with partial results). */
+int amr_reduce_max(int dtype, int ncomp, void* data, uint64_t count, void* result, void* stream);
+/* Component-wise minimum, find_minimum_val (parallel.h:409-421).  As in the reference, a block
+ * of 512 that runs past the end of the array counts its missing elements as 0 (parallel.h:389),
+ * so the result is at most 0 unless every pass fills its blocks. */
+int amr_reduce_min(int dtype, int ncomp, void* data, uint64_t count, void* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

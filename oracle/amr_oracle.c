@@ -743,3 +743,120 @@ void orc_set_num_threads(int n) {
     (void)n;
 #endif
 }
+
+
+/* ------------------------------------------------------------------ scan and reductions, parallel.h
+ * Multi-pass over blocks of 512 slots.  The scan's slot t of block b at stride s is element
+ * (t + 512 b + 1) s - 1; its up pass (parallel.h:10-27) adds node k - d into node k = (t+1) 2d - 1
+ * for d = 1 .. 256, its down pass (parallel.h:29-60) first adds element 512 b s - 1 to the nodes
+ * 2^i - 1 (i = 0..8) of blocks b > 0, then for d = 128 .. 1 adds node m = (t+1) 2d - 1 into m + d.
+ * The reductions' slot t is element (t + 512 b) s; node 2td takes in node 2td + d (d = 1 .. 256)
+ * and the block's result is written to its first element (parallel.h:215-237, 385-407); missing
+ * elements are the lowest value (maximum) or 0 (minimum, parallel.h:389). */
+enum { SCAN_POW = 9, SCAN_BLK = 1 << SCAN_POW };
+
+typedef union { uint32_t u; int32_t i; float f; } orc_word;
+
+/* the device's floating-point arithmetic returns one NaN, 0x7FFFFFFF, whatever the operands' */
+static inline float canonical_nan(float f) { return f != f ? bitsf(0x7FFFFFFFu) : f; }
+static orc_word word_add(int dtype, orc_word a, orc_word b) {
+    orc_word r;
+    if (dtype == 2) r.f = canonical_nan(ftz(ftz(a.f) + ftz(b.f)));
+    else r.u = a.u + b.u;   /* int32 and uint32 both wrap */
+    return r;
+}
+static orc_word word_extreme(int dtype, int is_max, orc_word a, orc_word b) {
+    orc_word r;
+    if (dtype == 2) {
+        const float x = ftz(a.f), y = ftz(b.f);
+        /* fmaxf / fminf: a NaN operand yields the other; of two zeros the maximum is +0 and the
+           minimum -0 */
+        if (x != x) r.f = canonical_nan(y);
+        else if (y != y) r.f = x;
+        else if (x == y) r.f = is_max ? (signbit(x) ? y : x) : (signbit(x) ? x : y);
+        else r.f = is_max ? (x > y ? x : y) : (x < y ? x : y);
+    } else if (dtype == 1) {
+        r.i = is_max ? (a.i > b.i ? a.i : b.i) : (a.i < b.i ? a.i : b.i);
+    } else {
+        r.u = is_max ? (a.u > b.u ? a.u : b.u) : (a.u < b.u ? a.u : b.u);
+    }
+    return r;
+}
+
+void orc_scan(int dtype, int ncomp, void* data, uint32_t n) {
+    orc_word* d = (orc_word*)data;
+    static orc_word a[SCAN_BLK][4];
+    uint64_t stride = 1;
+    for (; stride < n; stride <<= SCAN_POW) {
+        const uint64_t blocks = (n + SCAN_BLK * stride - 1) / (SCAN_BLK * stride);
+        for (uint64_t b = 0; b < blocks; b++) {
+            for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                const uint64_t i = (t + SCAN_BLK * b + 1) * stride - 1;
+                for (int c = 0; c < ncomp; c++) a[t][c].u = i < n ? d[i * ncomp + c].u : 0u;
+            }
+            for (uint32_t dd = 1; dd < SCAN_BLK; dd <<= 1)
+                for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                    const uint64_t k = (uint64_t)(t + 1) * 2 * dd - 1;
+                    if (k < SCAN_BLK)
+                        for (int c = 0; c < ncomp; c++) a[k][c] = word_add(dtype, a[k][c], a[k - dd][c]);
+                }
+            for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                const uint64_t i = (t + SCAN_BLK * b + 1) * stride - 1;
+                if (i < n) for (int c = 0; c < ncomp; c++) d[i * ncomp + c] = a[t][c];
+            }
+        }
+    }
+    for (stride >>= SCAN_POW; stride > 0; stride >>= SCAN_POW) {
+        const uint64_t blocks = (n + SCAN_BLK * stride - 1) / (SCAN_BLK * stride);
+        /* blocks read their carry before any block of this pass writes (on the device the carry
+           element is final already and rewritten unchanged) */
+        for (uint64_t b = blocks; b-- > 0;) {
+            for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                const uint64_t i = (t + SCAN_BLK * b + 1) * stride - 1;
+                for (int c = 0; c < ncomp; c++) a[t][c].u = i < n ? d[i * ncomp + c].u : 0u;
+            }
+            if (b > 0)
+                for (uint32_t t = 0; t < SCAN_BLK / 2; t = 2 * t + 1)   /* t + 1 = 1, 2, 4, ..., 256 */
+                    for (int c = 0; c < ncomp; c++)
+                        a[t][c] = word_add(dtype, a[t][c], d[(SCAN_BLK * b * stride - 1) * ncomp + c]);
+            for (uint32_t dd = SCAN_BLK / 4; dd >= 1; dd >>= 1)
+                for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                    const uint64_t m = (uint64_t)(t + 1) * 2 * dd - 1;
+                    if (m + dd < SCAN_BLK)
+                        for (int c = 0; c < ncomp; c++) a[m + dd][c] = word_add(dtype, a[m + dd][c], a[m][c]);
+                }
+            for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                const uint64_t i = (t + SCAN_BLK * b + 1) * stride - 1;
+                if (i < n) for (int c = 0; c < ncomp; c++) d[i * ncomp + c] = a[t][c];
+            }
+        }
+    }
+}
+
+void orc_extreme(int dtype, int ncomp, int is_max, void* data, uint32_t n, void* result) {
+    orc_word* d = (orc_word*)data;
+    static orc_word a[SCAN_BLK][4];
+    orc_word pad;
+    if (!is_max) pad.u = 0u;
+    else if (dtype == 2) pad.f = -INFINITY;
+    else if (dtype == 1) pad.i = INT32_MIN;
+    else pad.u = 0u;
+    for (uint64_t stride = 1; stride < n; stride <<= SCAN_POW) {
+        const uint64_t blocks = (n + SCAN_BLK * stride - 1) / (SCAN_BLK * stride);
+        for (uint64_t b = 0; b < blocks; b++) {
+            for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                const uint64_t i = (t + SCAN_BLK * b) * stride;
+                for (int c = 0; c < ncomp; c++) a[t][c] = i < n ? d[i * ncomp + c] : pad;
+            }
+            for (uint32_t dd = 1; dd < SCAN_BLK; dd <<= 1)
+                for (uint32_t t = 0; t < SCAN_BLK; t++) {
+                    const uint64_t k = (uint64_t)t * 2 * dd;
+                    if (k < SCAN_BLK)
+                        for (int c = 0; c < ncomp; c++) a[k][c] = word_extreme(dtype, is_max, a[k][c], a[k + dd][c]);
+                }
+            const uint64_t i0 = SCAN_BLK * b * stride;
+            if (i0 < n) for (int c = 0; c < ncomp; c++) d[i0 * ncomp + c] = a[0][c];
+        }
+    }
+    memcpy(result, d, sizeof(orc_word) * (size_t)ncomp);
+}

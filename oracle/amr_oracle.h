@@ -112,6 +112,11 @@ void orc_bssn_timestep(const orc_cfg* c, float* const* old6, float* const* new6,
                        const uint64_t* boundaries, uint32_t used, uint32_t max_depth, uint32_t* timer, int32_t* rng,
                        uint32_t slot_begin, uint32_t slot_end);
 
+/* parallel.h:10-82, 215-251, 385-421 -- the reference's scan and reductions over `n` elements of
+ * `ncomp` values; dtype 0 uint32, 1 int32, 2 float32 (flushing subnormals as the device build).
+ * The array ends as the reference leaves it; orc_extreme writes the result to `result`. */
+void orc_scan(int dtype, int ncomp, void* data, uint32_t n);
+void orc_extreme(int dtype, int ncomp, int is_max, void* data, uint32_t n, void* result);
 int orc_num_threads(void);
 void orc_set_num_threads(int n);
 

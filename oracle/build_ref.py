@@ -31,7 +31,8 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ROOT = "/root/reference/AdaptiveMesh"
 OUT = os.path.join(HERE, "_ref")
-HEADERS = ["helper_math.h", "tensors.h", "AMR.h", "BSSN.h", "SimpleWave.h", "CUDA_memory.h", "image_process.h"]
+HEADERS = ["helper_math.h", "tensors.h", "AMR.h", "BSSN.h", "SimpleWave.h", "CUDA_memory.h", "image_process.h",
+           "parallel.h"]
 CONFIGS = {"n28p2": (28, 2), "n16p3": (16, 3)}
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 

@@ -60,6 +60,8 @@ _SIGS = {
     "orc_wave_step": (None, [VP, ctypes.c_int, VP, VP, VP, VP, VP, U32, U32, U32]),
     "orc_criterion": (None, [VP, VP, VP, VP, VP, U32, U32, U32]),
     "orc_rasterise": (None, [VP, VP, VP, U32, U32, ctypes.c_float, ctypes.c_int, VP]),
+    "orc_scan": (None, [ctypes.c_int, ctypes.c_int, VP, U32]),
+    "orc_extreme": (None, [ctypes.c_int, ctypes.c_int, ctypes.c_int, VP, U32, VP]),
     "orc_differentiate_f64": (None, [VP, VP, VP, VP, VP, VP, U32]),
     "orc_bssn_timestep": (None, [VP, VP, VP, VP, VP, VP, VP, VP, VP, U32, U32, VP, VP, U32, U32]),
     "orc_num_threads": (ctypes.c_int, []),

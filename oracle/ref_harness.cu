@@ -16,6 +16,7 @@
 #include "AMR.h"
 #include "BSSN.h"
 #include "SimpleWave.h"
+#include "parallel.h"
 
 #include <cstdint>
 
@@ -385,4 +386,46 @@ REF_API int32_t refd_wave_rng_seed(void* h) { return ((RefWave*)h)->amr.sim_data
 REF_API void refd_wave_octree_state(void* h, uint32_t* positions, int32_t* parent, int32_t* children, uint64_t* boundaries,
                                     uint32_t* lifetime, uint32_t* scalars) {
     dump_octree(((RefWave*)h)->amr, positions, parent, children, boundaries, lifetime, scalars);
+}
+
+
+// ------------------------------------------------------------------ parallel.h: scan and reductions
+// The reference's apply_incl_cum_sum / find_maximum_val / find_minimum_val on a caller's device
+// array (wrapped without taking ownership); dtype 0 uint, 1 int, 2 float; ncomp 1-4 selects the
+// scalar or the helper_math vector type.
+template <class T>
+static smart_gpu_buffer<T> ref_view(void* d, uint32_t n) {
+    smart_gpu_buffer<T> b;
+    b.dedicated_len = n;
+    b.gpu_buffer_ptr = static_cast<T*>(d);
+    return b;
+}
+template <class T>
+static void ref_scan(void* d, uint32_t n) {
+    smart_gpu_buffer<T> b = ref_view<T>(d, n);
+    apply_incl_cum_sum(b);
+}
+template <class T>
+static void ref_extreme(int is_max, void* d, uint32_t n, void* result) {
+    smart_gpu_buffer<T> b = ref_view<T>(d, n);
+    const T r = is_max ? find_maximum_val(b) : find_minimum_val(b);
+    std::memcpy(result, &r, sizeof(T));
+}
+#define REF_TYPES(F, ...)                                                                                   \
+    switch (dtype * 4 + ncomp - 1) {                                                                        \
+        case 0: F<uint>(__VA_ARGS__); break;   case 1: F<uint2>(__VA_ARGS__); break;                        \
+        case 2: F<uint3>(__VA_ARGS__); break;  case 3: F<uint4>(__VA_ARGS__); break;                        \
+        case 4: F<int>(__VA_ARGS__); break;    case 5: F<int2>(__VA_ARGS__); break;                         \
+        case 6: F<int3>(__VA_ARGS__); break;   case 7: F<int4>(__VA_ARGS__); break;                         \
+        case 8: F<float>(__VA_ARGS__); break;  case 9: F<float2>(__VA_ARGS__); break;                       \
+        case 10: F<float3>(__VA_ARGS__); break; case 11: F<float4>(__VA_ARGS__); break;                     \
+        default: return -1;                                                                                  \
+    }
+REF_API int refd_scan(int dtype, int ncomp, void* d, uint32_t n) {
+    REF_TYPES(ref_scan, d, n)
+    return (int)cudaDeviceSynchronize();
+}
+REF_API int refd_extreme(int dtype, int ncomp, int is_max, void* d, uint32_t n, void* result) {
+    REF_TYPES(ref_extreme, is_max, d, n, result)
+    return (int)cudaDeviceSynchronize();
 }

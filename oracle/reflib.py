@@ -56,6 +56,8 @@ _SIGS = {
     "refd_wave_step": (_c.c_int, [_c.c_int, VP, VP, VP, VP, VP, U32, U32, U32]),
     "refd_criterion": (_c.c_int, [VP, VP, VP, VP, U32, U32, U32]),
     "refd_rasterise": (_c.c_int, [VP, VP, VP, U32, U32, _c.c_float]),
+    "refd_scan": (_c.c_int, [_c.c_int, _c.c_int, VP, U32]),
+    "refd_extreme": (_c.c_int, [_c.c_int, _c.c_int, _c.c_int, VP, U32, VP]),
     "refd_bssn_create": (VP, [U32]),
     "refd_bssn_destroy": (None, [VP]),
     "refd_bssn_add_node": (None, [VP, I32, I32]),

@@ -421,3 +421,58 @@ def test_rasterise(am, cuda, orc, cfgname, tree, width, height, z_slice):
         orc.lib().orc_rasterise(ctypes.byref(orc.cfg(c.n, c.p, OUTER)), orc.P(c.f_new), orc.P(c.st["children"]),
                                 width, height, z_slice, 1, orc.P(o))
         assert_same(mine, o, f"raster {width}x{height} vs oracle")
+
+
+# ----------------------------------------------------------------------------- scan and reductions
+def _reduce_input(rng, dtype, n, ncomp, specials):
+    if dtype == 2:
+        a = (rng.standard_normal(n * ncomp) * 10.0 ** rng.integers(-3, 4, n * ncomp)).astype(np.float32)
+        if specials:   # zeros of both signs, infinities, NaN, subnormals
+            k = rng.choice(n * ncomp, size=min(n * ncomp, 64), replace=False)
+            pool = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-40, -1e-40, 3e38], np.float32)
+            a[k] = pool[rng.integers(0, pool.size, k.size)]
+        return a
+    a = rng.integers(-2 ** 31, 2 ** 31, n * ncomp, dtype=np.int64)
+    return (a if dtype == 1 else a % 2 ** 32).astype(np.int32 if dtype == 1 else np.uint32)
+
+
+@pytest.mark.parametrize("dtype", [0, 1, 2])
+@pytest.mark.parametrize("ncomp", [1, 2, 3, 4])
+def test_scan_and_reductions(am, cuda, orc, dtype, ncomp):
+    """amr_inclusive_scan / amr_reduce_max / amr_reduce_min against the reference's parallel.h on the
+    GPU and the oracle: the results and the arrays they leave behind, bit for bit."""
+    import torch
+    ref = ref_lib("n16p3")
+    tdt = {0: torch.uint32, 1: torch.int32, 2: torch.float32}[dtype]
+    rng = np.random.default_rng(100 * dtype + ncomp)
+    for n in (1, 7, 512, 513, 4097, 262144, 262145, 600001):
+        for specials in ((False, True) if dtype == 2 else (False,)):
+            a = _reduce_input(rng, dtype, n, ncomp, specials)
+            for op in ("scan", "max", "min"):
+                d = torch.from_numpy(a.view(np.int32)).cuda().view(tdt)
+                if op == "scan":
+                    am.ops.inclusive_scan(d, ncomp)
+                    res = None
+                else:
+                    res = (am.ops.reduce_max if op == "max" else am.ops.reduce_min)(d, ncomp)
+                torch.cuda.synchronize()
+                mine = d.view(torch.int32).cpu().numpy().view(np.uint32)
+                o = a.copy()
+                r = np.zeros(ncomp, a.dtype)
+                if op == "scan":
+                    orc.lib().orc_scan(dtype, ncomp, o.ctypes.data, n)
+                else:
+                    orc.lib().orc_extreme(dtype, ncomp, 1 if op == "max" else 0, o.ctypes.data, n, r.ctypes.data)
+                what = f"{op} dtype {dtype} x{ncomp} n={n}{' specials' if specials else ''}"
+                assert_same(mine, o.view(np.uint32), f"{what}: array vs oracle")
+                if res is not None:
+                    assert_same(np.array(res, a.dtype).view(np.uint32), r.view(np.uint32), f"{what}: result vs oracle")
+                if ref is not None and n <= 262145:
+                    rd = torch.from_numpy(a.view(np.int32)).cuda()
+                    rr = np.zeros(ncomp, a.dtype)
+                    st = ref.refd_scan(dtype, ncomp, rd.data_ptr(), n) if op == "scan" else \
+                        ref.refd_extreme(dtype, ncomp, 1 if op == "max" else 0, rd.data_ptr(), n, rr.ctypes.data)
+                    assert st == 0
+                    assert_same(mine, rd.cpu().numpy().view(np.uint32), f"{what}: array vs reference")
+                    if res is not None:
+                        assert_same(np.array(res, a.dtype).view(np.uint32), rr.view(np.uint32), f"{what}: result vs reference")

@@ -112,3 +112,25 @@ def test_octree_script_matches_reference(am, hg):
     for k in ("positions", "parent", "children", "boundaries", "lifetime"):
         assert np.array_equal(st[k], hg[f"tree/script/final/{k}"]), k
     o.close()
+
+
+def test_oracle_scan_and_reductions_on_integers(orc):
+    """The oracle's restatement of parallel.h on integers: an inclusive scan is the cumulative sum
+    (wrapping), the maximum is the maximum, and the minimum counts a partial block's missing
+    elements as 0, as the reference's kernel does (parallel.h:389)."""
+    rng = np.random.default_rng(7)
+    for n in (1, 5, 512, 513, 1000, 262144, 262145):
+        for nc in (1, 3):
+            a = rng.integers(-1000, 1000, size=n * nc).astype(np.int32)
+            b = a.copy()
+            orc.lib().orc_scan(1, nc, b.ctypes.data, n)
+            assert np.array_equal(b, np.cumsum(a.reshape(n, nc), axis=0).astype(np.int32).ravel())
+            r = np.zeros(nc, np.int32)
+            work = a.copy()   # named: the oracle writes into it
+            orc.lib().orc_extreme(1, nc, 1, work.ctypes.data, n, r.ctypes.data)
+            assert np.array_equal(r, a.reshape(n, nc).max(axis=0))
+            pos = np.abs(a) + 1
+            work = pos.copy()
+            orc.lib().orc_extreme(1, nc, 0, work.ctypes.data, n, r.ctypes.data)
+            full = n in (1, 512, 262144)   # every pass's blocks are whole
+            assert np.array_equal(r, pos.reshape(n, nc).min(axis=0) if full else np.zeros(nc, np.int32)), (n, nc)
