@@ -81,6 +81,8 @@ EXPORTS = {
     "amr_octree_destroy": (ctypes.c_int, [VP]),
     "amr_octree_add_node": (ctypes.c_int, [VP, I32, I32]),
     "amr_octree_remove_node": (ctypes.c_int, [VP, I32]),
+    "amr_octree_add_nodes": (ctypes.c_int, [VP, VP, VP, U32]),
+    "amr_octree_remove_nodes": (ctypes.c_int, [VP, VP, U32]),
     "amr_octree_increment_timer": (ctypes.c_int, [VP]),
     "amr_octree_find_node_idx": (U32, [VP, U32, U32]),
     "amr_octree_state": (ctypes.c_int, [VP, VP, VP, VP, VP, VP, VP]),
@@ -89,6 +91,8 @@ EXPORTS = {
     "amr_sim_set_mode": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_add_node": (ctypes.c_int, [VP, I32, I32]),
     "amr_sim_remove_node": (ctypes.c_int, [VP, I32]),
+    "amr_sim_add_nodes": (ctypes.c_int, [VP, VP, VP, U32]),
+    "amr_sim_remove_nodes": (ctypes.c_int, [VP, VP, U32]),
     "amr_sim_octree_state": (ctypes.c_int, [VP, VP, VP, VP, VP, VP, VP]),
     "amr_sim_buffer": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(VP), ctypes.POINTER(U64)]),
     "amr_sim_copy_to_device": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, VP, U64]),

@@ -291,6 +291,23 @@ AMR_API int amr_octree_remove_node(amr_octree* o, int32_t node) {
     o->tree.remove_node(node);
     return AMR_OK;
 }
+AMR_API int amr_octree_add_nodes(amr_octree* o, const int32_t* parents, const int32_t* offsets, uint32_t n) {
+    AMR_REQUIRE(o && (n == 0 || (parents && offsets)));
+    for (uint32_t i = 0; i < n; i++)
+        AMR_REQUIRE(parents[i] >= 0 && (uint32_t)parents[i] < o->tree.max_slots() && offsets[i] >= 0 && offsets[i] < 8);
+    o->tree.begin_batch();
+    for (uint32_t i = 0; i < n; i++) o->tree.add_node(parents[i], offsets[i]);
+    o->tree.end_batch();
+    return AMR_OK;
+}
+AMR_API int amr_octree_remove_nodes(amr_octree* o, const int32_t* nodes, uint32_t n) {
+    AMR_REQUIRE(o && (n == 0 || nodes));
+    for (uint32_t i = 0; i < n; i++) AMR_REQUIRE(nodes[i] >= -1 && nodes[i] < (int32_t)o->tree.max_slots());
+    o->tree.begin_batch();
+    for (uint32_t i = 0; i < n; i++) o->tree.remove_node(nodes[i]);
+    o->tree.end_batch();
+    return AMR_OK;
+}
 AMR_API int amr_octree_increment_timer(amr_octree* o) {
     AMR_REQUIRE(o);
     o->tree.increment_timer();

@@ -89,6 +89,10 @@ cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* po
                                    const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
                                    cudaStream_t st, bool parents_only = false);
 cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t child, int32_t parent, cudaStream_t st);
+// Prolongation of n_items new nodes at once into each of nbuf (<= 12) buffers; items holds
+// (child, parent, offset) triples in device memory, none a parent of another.
+cudaError_t launch_copy_to_children(Dims d, float* const* bufs, int nbuf, const int32_t* items, uint32_t n_items,
+                                    cudaStream_t st);
 // Staging for the ghost fill (the innermost layer of the three lower faces, old and new):
 // 2 * ncomp * 3 * n^2 floats per slot.
 size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp);

@@ -83,10 +83,26 @@ __global__ void __launch_bounds__(kBlock) k_copy_new_to_old(const __grid_constan
 }
 
 // ---------------------------------------------------------------- prolongation, AMR.h:1053-1073
+__device__ __forceinline__ void prolongate_cell(Dims d, float inv_n, float* buf, uint32_t offset, int32_t child,
+                                                int32_t parent, uint32_t cell);
 __global__ void k_copy_to_child(Dims d, float inv_n, float* buf, uint32_t offset, int32_t child, int32_t parent) {
-    const uint32_t cells = d.t * d.t * d.t;
     const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= cells) return;
+    if (cell >= d.t * d.t * d.t) return;
+    prolongate_cell(d, inv_n, buf, offset, child, parent, cell);
+}
+struct BufList {
+    float* p[12];
+};
+// blockIdx.y: the item, blockIdx.z: the buffer
+__global__ void k_copy_to_children(Dims d, float inv_n, const __grid_constant__ BufList bufs, const int32_t* __restrict__ items) {
+    const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= d.t * d.t * d.t) return;
+    const int32_t* it = items + 3u * blockIdx.y;
+    prolongate_cell(d, inv_n, bufs.p[blockIdx.z], (uint32_t)it[2], it[0], it[1], cell);
+}
+__device__ __forceinline__ void prolongate_cell(Dims d, float inv_n, float* buf, uint32_t offset, int32_t child,
+                                                int32_t parent, uint32_t cell) {
+    const uint32_t cells = d.t * d.t * d.t;
     const uint32_t w[3] = {cell % d.t, (cell / d.t) % d.t, cell / (d.t * d.t)};
     const float off[3] = {(float)(offset & 1u), (float)((offset & 2u) >> 1), (float)((offset & 4u) >> 2)};
     uint32_t ri[3];
@@ -446,6 +462,21 @@ cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t ch
     const float inv_n = 1.f / (float)d.n;
     k_copy_to_child<<<blocks_for((uint64_t)d.t * d.t * d.t), kBlock, 0, st>>>(d, inv_n, buf, offset, child, parent);
     return cudaGetLastError();
+}
+cudaError_t launch_copy_to_children(Dims d, float* const* bufs, int nbuf, const int32_t* items, uint32_t n_items,
+                                    cudaStream_t st) {
+    if (nbuf < 1 || nbuf > 12) return cudaErrorInvalidValue;
+    if (n_items == 0) return cudaSuccess;
+    BufList b;
+    for (int i = 0; i < 12; i++) b.p[i] = i < nbuf ? bufs[i] : nullptr;
+    const float inv_n = 1.f / (float)d.n;
+    for (uint32_t i = 0; i < n_items; i += 65535u) {   // grid y holds at most 65535 items
+        k_copy_to_children<<<dim3(blocks_for((uint64_t)d.t * d.t * d.t), std::min(n_items - i, 65535u), (uint32_t)nbuf),
+                             kBlock, 0, st>>>(d, inv_n, b, items + 3u * (size_t)i);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 size_t ghost_scratch_floats(Dims d, uint32_t used, int ncomp) {
     return (size_t)ncomp * 2u * used * 3u * d.n * d.n;

@@ -81,6 +81,7 @@ Octree::Octree(uint32_t node_slots, NodeHooks* hooks)
       children_((size_t)node_slots * 8u, -1), boundaries_((size_t)node_slots * 6u, kNoBoundary),
       lifetime_(node_slots, 0) {
     positions_[0] = 0u;   // the root
+    depth_count_[0] = 1u;
 }
 
 void Octree::restore(const uint32_t* positions, const int32_t* parent, const int32_t* children,
@@ -96,6 +97,69 @@ void Octree::restore(const uint32_t* positions, const int32_t* parent, const int
     first_free_slot_ = first_free;
     final_used_slot_ = final_used;
     dirty_ = true;
+    for (uint32_t& c : depth_count_) c = 0u;
+    for (uint32_t p : positions_)
+        if (pos_depth_host(p) != -1) depth_count_[pos_depth_host(p)]++;
+}
+
+int Octree::counted_max_depth() const {
+    for (int d = 31; d > 0; d--)
+        if (depth_count_[d]) return d;
+    return 0;
+}
+void Octree::note_change(int depth) {
+    if (batching_) batch_min_depth_ = std::min(batch_min_depth_, depth);
+    else refresh_boundaries(depth);
+}
+void Octree::begin_batch() {
+    batching_ = true;
+    batch_min_depth_ = 32;
+    pending_ctor_.clear();
+}
+void Octree::end_batch() {
+    batching_ = false;
+    if (batch_min_depth_ < 32) refresh_boundaries(batch_min_depth_);
+    batch_min_depth_ = 32;
+    if (hooks_ && !pending_ctor_.empty()) run_pending_ctors();
+    pending_ctor_.clear();
+}
+void Octree::run_pending_ctors() {
+    const size_t n = pending_ctor_.size();
+    // Depth order matches the calls' order if every slot is written once and each constructor
+    // that reads a slot written in the batch comes after that write and deeper.
+    bool by_depth = true;
+    std::vector<int32_t> writer(max_slots_, -1);
+    for (size_t i = 0; i < n && by_depth; i++) {
+        int32_t& w = writer[(size_t)pending_ctor_[i].c.node];
+        if (w != -1) by_depth = false;
+        w = (int32_t)i;
+    }
+    for (size_t i = 0; i < n && by_depth; i++) {
+        const int32_t j = writer[(size_t)pending_ctor_[i].c.parent];
+        if (j != -1 && !((size_t)j < i && pending_ctor_[(size_t)j].depth < pending_ctor_[i].depth)) by_depth = false;
+    }
+    if (by_depth)
+        std::stable_sort(pending_ctor_.begin(), pending_ctor_.end(),
+                         [](const PendingCtor& a, const PendingCtor& b) { return a.depth < b.depth; });
+    std::vector<NodeCtor> items(n);
+    std::vector<uint32_t> ends;
+    for (size_t i = 0; i < n; i++) {
+        items[i] = pending_ctor_[i].c;
+        if (i + 1 == n || !by_depth || pending_ctor_[i + 1].depth != pending_ctor_[i].depth) ends.push_back((uint32_t)i + 1u);
+    }
+    hooks_->node_ctor_groups(items.data(), ends.data(), (uint32_t)ends.size());
+}
+void Octree::refresh_node(uint32_t node) {
+    for (uint32_t f = 0; f < 6; f++) boundaries_[(size_t)node * 6u + f] = yield_boundary((int32_t)node, f);
+}
+// Inside a batch, a node about to be removed gets the boundaries it would have had from the last
+// call (since the batch began) that refreshed it: its value now, before the tree changes.
+void Octree::refresh_subtree_before_removal(int32_t node) {
+    if (node == -1) return;
+    const int d = pos_depth_host(positions_[node]);
+    if (d == -1) return;
+    if (d >= batch_min_depth_) refresh_node((uint32_t)node);
+    for (uint32_t i = 0; i < 8u; i++) refresh_subtree_before_removal(children_[(size_t)node * 8u + i]);
 }
 void Octree::increment_timer() {
     for (uint32_t i = 0; i <= final_used_slot_; i++) {
@@ -115,13 +179,17 @@ void Octree::add_node(int32_t parent, int32_t offset) {
     children_[(size_t)parent * 8u + offset] = (int32_t)slot;
     positions_[slot] = pos_child(positions_[parent], (uint32_t)offset);
     const int new_depth = pos_depth_host(positions_[slot]);
+    depth_count_[new_depth]++;
     const int change = std::max(max_depth_, new_depth) - max_depth_;
     timer_ <<= change;
     max_depth_ += change;
-    if (hooks_) hooks_->node_ctor((int32_t)slot);
+    if (hooks_) {
+        if (batching_) pending_ctor_.push_back({{(int32_t)slot, parent, pos_final_offset(positions_[slot])}, new_depth});
+        else hooks_->node_ctor((int32_t)slot);
+    }
     final_used_slot_ = std::max(final_used_slot_, slot);
     while (first_free_slot_ < max_slots_ && pos_depth_host(positions_[first_free_slot_]) != -1) first_free_slot_++;
-    refresh_boundaries(new_depth);
+    note_change(new_depth);
     dirty_ = true;
 }
 
@@ -131,6 +199,7 @@ void Octree::remove_node_recursive(int32_t node) {
     for (uint32_t i = 0; i < 8u; i++) remove_node_recursive(children_[(size_t)node * 8u + i]);
     children_[(size_t)parent_[node] * 8u + pos_final_offset(positions_[node])] = -1;
     parent_[node] = -1;
+    depth_count_[pos_depth_host(positions_[node])]--;
     positions_[node] = ~0u;
     first_free_slot_ = std::min(first_free_slot_, (uint32_t)node);
 }
@@ -139,14 +208,13 @@ void Octree::remove_node(int32_t node) {
     if (node == -1) return;
     const int curr_depth = pos_depth_host(positions_[node]);
     if (curr_depth == -1) return;
+    if (batching_) refresh_subtree_before_removal(node);
     remove_node_recursive(node);
     const int old_max = max_depth_;
-    max_depth_ = 0;
-    for (uint32_t i = 0; i < max_slots_; i++)
-        if (i != (uint32_t)node) max_depth_ = std::max(max_depth_, pos_depth_host(positions_[i]));
+    max_depth_ = counted_max_depth();   // the deepest node left (AMR.h:243-246)
     timer_ >>= (old_max - max_depth_);
     while (pos_depth_host(positions_[final_used_slot_]) == -1 && final_used_slot_ > 0u) final_used_slot_--;
-    refresh_boundaries(curr_depth);
+    note_change(curr_depth);
     dirty_ = true;
 }
 

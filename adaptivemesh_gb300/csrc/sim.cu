@@ -57,7 +57,7 @@ public:
         if (main_mark) cudaEventDestroy(main_mark);
         for (auto& row : side_done)
             for (auto& ev : row) if (ev) cudaEventDestroy(ev);
-        cudaFree(d_positions); cudaFree(d_children); cudaFree(d_boundaries); cudaFree(d_items);
+        cudaFree(d_positions); cudaFree(d_children); cudaFree(d_boundaries); cudaFree(d_items); cudaFree(ctor_items);
         cudaFree(ghost_stage);
         for (auto& ev : events) cudaEventDestroy(ev);
         for (auto& ev : user_events) if (ev) cudaEventDestroy(ev);
@@ -114,6 +114,35 @@ public:
     virtual int buffer(int which, int comp, void** ptr, uint64_t* count) = 0;
 
     void node_dtor(int32_t) override {}
+    // Batched node_ctor: upload the deferred constructors once, then prolongate each group into
+    // every buffer of `bufs` with one launch; errors are kept for take_ctor_status().
+    void prolongate_groups(const NodeCtor* items, const uint32_t* group_end, uint32_t groups, float* const* bufs,
+                           int nbuf) {
+        const size_t n = groups ? group_end[groups - 1] : 0u;
+        if (n == 0) return;
+        if (!ctor_items || ctor_items_cap < n) {
+            cudaError_t e = cudaStreamSynchronize(stream);   // a launch of the last batch may still read it
+            cudaFree(ctor_items);
+            ctor_items = nullptr;
+            ctor_items_cap = 0;
+            const size_t cap = std::max<size_t>(n, tree.max_slots());
+            if (e == cudaSuccess) e = cudaMalloc(&ctor_items, sizeof(NodeCtor) * cap);
+            if (e != cudaSuccess) { ctor_status = cuda_status(e); return; }
+            ctor_items_cap = cap;
+        }
+        cudaError_t e = cudaMemcpyAsync(ctor_items, items, sizeof(NodeCtor) * n, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);   // `items` is pageable and short-lived
+        for (uint32_t g = 0, b = 0; g < groups && e == cudaSuccess; b = group_end[g++]) {
+            e = launch_copy_to_children(dims, bufs, nbuf, reinterpret_cast<const int32_t*>(ctor_items + b),
+                                        group_end[g] - b, stream);
+            launches++;
+        }
+        if (e != cudaSuccess) ctor_status = cuda_status(e);
+    }
+    int take_ctor_status() { const int st = ctor_status; ctor_status = AMR_OK; return st; }
+    NodeCtor* ctor_items = nullptr;
+    size_t ctor_items_cap = 0;
+    int ctor_status = AMR_OK;
 
     // AMR<T>::copy_to_gpu (AMR.h:268-275): upload the octree arrays if they changed.
     int sync_octree() {
@@ -345,6 +374,12 @@ public:
         for (int k = 0; k < 6; k++) check(launch_copy_to_child(dims, new6[k], off, node, parent, stream));
         graph_valid = false;
     }
+    void node_ctor_groups(const NodeCtor* items, const uint32_t* group_end, uint32_t groups) override {
+        float* bufs[12];
+        for (int k = 0; k < 6; k++) { bufs[k] = old6[k]; bufs[6 + k] = new6[k]; }
+        prolongate_groups(items, group_end, groups, bufs, 12);
+        graph_valid = false;
+    }
 
     // --- phases
     int copy_back() override {                                   // BSSN.h:126-130
@@ -573,6 +608,10 @@ public:
         check(launch_copy_to_child(dims, old_f, off, node, parent, stream));
         check(launch_copy_to_child(dims, new_f, off, node, parent, stream));
     }
+    void node_ctor_groups(const NodeCtor* items, const uint32_t* group_end, uint32_t groups) override {
+        float* bufs[2] = {old_f, new_f};
+        prolongate_groups(items, group_end, groups, bufs, 2);
+    }
     int copy_back() override {                                   // SimpleWave.h:214-218
         int st = sync_octree();
         if (st) return st;
@@ -619,6 +658,9 @@ public:
         float ax = avg1 / (float)active, ay = (avg2 * .125f) / (float)active;
         if (used == 1u) ax = ay = .15f;
         const float urgency = (float)(used - 1u) / (float)tree.max_slots();
+        // one batch: each decision still sees the tree as the calls before it left it, but the
+        // boundary refresh runs once and the new nodes are prolongated per depth level
+        tree.begin_batch();
         for (uint32_t i = 1, s = used; i < s; i++) {               // root cannot be removed
             const float ratio = (float)pos_depth_host(tree.positions()[i]) / (float)tree.read_max_depth();
             if (ratio <= 0.f) continue;
@@ -630,7 +672,8 @@ public:
             const float weight = ay * 3.f / (1.f - urgency);
             if (c[i] > weight && tree.children()[i] == -1) tree.add_node((int32_t)(i >> 3u), (int32_t)(i & 7u));
         }
-        return AMR_OK;
+        tree.end_batch();
+        return take_ctor_status();
     }
     int predictor() override {                                   // SimpleWave.h:249-255
         int st = sync_octree();
@@ -747,6 +790,27 @@ AMR_API int amr_sim_add_node(amr_sim* s, int32_t parent, int32_t offset) {
 AMR_API int amr_sim_remove_node(amr_sim* s, int32_t node) {
     if (!s || node < -1 || node >= (int32_t)s->impl->tree.max_slots()) return AMR_ERR_INVALID;
     s->impl->tree.remove_node(node);
+    return AMR_OK;
+}
+AMR_API int amr_sim_add_nodes(amr_sim* s, const int32_t* parents, const int32_t* offsets, uint32_t n) {
+    if (!s || (n && (!parents || !offsets))) return AMR_ERR_INVALID;
+    for (uint32_t i = 0; i < n; i++)
+        if (parents[i] < 0 || (uint32_t)parents[i] >= s->impl->tree.max_slots() || offsets[i] < 0 || offsets[i] > 7)
+            return AMR_ERR_INVALID;
+    const int st = s->impl->wait_side(-1, 0);   // node_ctor writes the new slots' fields
+    if (st) return st;
+    s->impl->tree.begin_batch();
+    for (uint32_t i = 0; i < n; i++) s->impl->tree.add_node(parents[i], offsets[i]);
+    s->impl->tree.end_batch();
+    return s->impl->take_ctor_status();
+}
+AMR_API int amr_sim_remove_nodes(amr_sim* s, const int32_t* nodes, uint32_t n) {
+    if (!s || (n && !nodes)) return AMR_ERR_INVALID;
+    for (uint32_t i = 0; i < n; i++)
+        if (nodes[i] < -1 || nodes[i] >= (int32_t)s->impl->tree.max_slots()) return AMR_ERR_INVALID;
+    s->impl->tree.begin_batch();
+    for (uint32_t i = 0; i < n; i++) s->impl->tree.remove_node(nodes[i]);
+    s->impl->tree.end_batch();
     return AMR_OK;
 }
 AMR_API int amr_sim_octree_state(const amr_sim* s, uint32_t* positions, int32_t* parent, int32_t* children,

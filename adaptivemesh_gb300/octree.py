@@ -37,6 +37,16 @@ class Octree:
     def remove_node(self, node: int) -> None:
         check(load().amr_octree_remove_node(self.h, node), "amr_octree_remove_node")
 
+    def add_nodes(self, parents, offsets) -> None:
+        """add_node for each (parent, offset) in order, as one batch (amr_octree_add_nodes)."""
+        p, o = np.ascontiguousarray(parents, np.int32), np.ascontiguousarray(offsets, np.int32)
+        check(load().amr_octree_add_nodes(self.h, p.ctypes.data, o.ctypes.data, p.size), "amr_octree_add_nodes")
+
+    def remove_nodes(self, nodes) -> None:
+        """remove_node for each node in order, as one batch (amr_octree_remove_nodes)."""
+        n = np.ascontiguousarray(nodes, np.int32)
+        check(load().amr_octree_remove_nodes(self.h, n.ctypes.data, n.size), "amr_octree_remove_nodes")
+
     def increment_timer(self) -> None:
         check(load().amr_octree_increment_timer(self.h), "amr_octree_increment_timer")
 
@@ -79,6 +89,17 @@ class Sim:
 
     def remove_node(self, node: int) -> None:
         check(load().amr_sim_remove_node(self.h, node), "amr_sim_remove_node")
+
+    def add_nodes(self, parents, offsets) -> None:
+        """add_node for each (parent, offset) in order, as one batch: the new nodes are prolongated
+        at the end, one launch per depth level (amr_sim_add_nodes)."""
+        p, o = np.ascontiguousarray(parents, np.int32), np.ascontiguousarray(offsets, np.int32)
+        check(load().amr_sim_add_nodes(self.h, p.ctypes.data, o.ctypes.data, p.size), "amr_sim_add_nodes")
+
+    def remove_nodes(self, nodes) -> None:
+        """remove_node for each node in order, as one batch (amr_sim_remove_nodes)."""
+        n = np.ascontiguousarray(nodes, np.int32)
+        check(load().amr_sim_remove_nodes(self.h, n.ctypes.data, n.size), "amr_sim_remove_nodes")
 
     def state(self) -> dict:
         return _state(load().amr_sim_octree_state, self.h, self.slots)

@@ -171,6 +171,13 @@ int amr_octree_create(uint32_t node_slots, amr_octree** out);
 int amr_octree_destroy(amr_octree* o);
 int amr_octree_add_node(amr_octree* o, int32_t parent, int32_t offset);        /* AMR.h:208-232 */
 int amr_octree_remove_node(amr_octree* o, int32_t node);                       /* AMR.h:233-254 */
+/* The same calls in order, as one batch: the final state equals n single calls, but the
+ * boundary refresh each single call makes over all nodes at or below its depth (AMR.h:231,
+ * 253) is done once, and the maximum depth after a removal is kept by counts per depth instead
+ * of a scan of all slots (AMR.h:243-246).  A batch of removals must not contain a node added in
+ * the same batch. */
+int amr_octree_add_nodes(amr_octree* o, const int32_t* parents, const int32_t* offsets, uint32_t n);
+int amr_octree_remove_nodes(amr_octree* o, const int32_t* nodes, uint32_t n);
 int amr_octree_increment_timer(amr_octree* o);                                 /* AMR.h:180-188 */
 uint32_t amr_octree_find_node_idx(const amr_octree* o, uint32_t packed_pos, uint32_t max_depth); /* AMR.h:255-263 */
 /* scalars: timer_helper, max_depth, first_free_slot, curr_used_slots, max_slots.  Any output
@@ -196,6 +203,10 @@ int amr_sim_destroy(amr_sim* s);
 int amr_sim_set_mode(amr_sim* s, int mode);
 int amr_sim_add_node(amr_sim* s, int32_t parent, int32_t offset);     /* runs node_ctor (prolongation) */
 int amr_sim_remove_node(amr_sim* s, int32_t node);
+/* Batches of the same (see amr_octree_add_nodes); the new nodes' node_ctor prolongations run at
+ * the end of the batch, one launch per depth level, parents before children. */
+int amr_sim_add_nodes(amr_sim* s, const int32_t* parents, const int32_t* offsets, uint32_t n);
+int amr_sim_remove_nodes(amr_sim* s, const int32_t* nodes, uint32_t n);
 int amr_sim_octree_state(const amr_sim* s, uint32_t* positions, int32_t* parent, int32_t* children,
                          uint64_t* boundaries, uint32_t* lifetime, uint32_t* scalars5);
 /* Device address and element count of a simulation buffer.

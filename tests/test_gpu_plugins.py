@@ -397,3 +397,39 @@ def test_staged_transfers_match_plain_copies(am, cuda):
     assert int(part[0]) == 0 and int(part[n_in - 2]) == 0 and int(part[n_in]) == 0, "snapshot wrote outside its count"
     plain.close()
     staged.close()
+
+
+def test_batched_regrid_matches_single_calls(am, cuda):
+    """amr_sim_add_nodes / amr_sim_remove_nodes (constructors deferred, one prolongation launch per
+    depth level) leave every buffer and the octree as the same add_node / remove_node calls one by
+    one do, through removals, slot reuse and further timesteps."""
+    cfg = am.Config(16, 3, 100.0)
+    rng = np.random.default_rng(11)
+    single, _st, _ = _bssn_sim(am, cfg, "uneven", am.MODE_BATCHED)
+    batched, _st, _ = _bssn_sim(am, cfg, "uneven", am.MODE_BATCHED)
+    for sim in (single, batched):
+        sim.timestep()
+
+    def live(depth_below):
+        st = single.state()
+        pos = st["positions"][: st["used_slots"]]
+        return [i for i, p in enumerate(pos) if p != 0xFFFFFFFF and (int(p) >> 27) < depth_below]
+    for rnd in range(3):
+        adds = []
+        for _ in range(int(rng.integers(6, 20))):   # nodes added earlier in the list may be parents
+            pa, off = int(rng.choice(live(3))), int(rng.integers(0, 8))
+            adds.append((pa, off))
+            single.add_node(pa, off)
+        batched.add_nodes([a[0] for a in adds], [a[1] for a in adds])
+        for sim in (single, batched):
+            sim.timestep()
+        removes = [int(x) for x in rng.choice(live(9)[1:], size=3, replace=False)]
+        for node in removes:
+            single.remove_node(node)
+        batched.remove_nodes(removes)
+        single.synchronize()
+        batched.synchronize()
+        _assert_states_equal(_full_state(am, batched, am.SIM_BSSN), _full_state(am, single, am.SIM_BSSN),
+                             f"regrid round {rnd}")
+    single.close()
+    batched.close()

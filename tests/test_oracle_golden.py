@@ -134,3 +134,59 @@ def test_oracle_scan_and_reductions_on_integers(orc):
             orc.lib().orc_extreme(1, nc, 0, work.ctypes.data, n, r.ctypes.data)
             full = n in (1, 512, 262144)   # every pass's blocks are whole
             assert np.array_equal(r, pos.reshape(n, nc).min(axis=0) if full else np.zeros(nc, np.int32)), (n, nc)
+
+
+def _random_regrid_ops(rng, o, n_ops, max_slots):
+    """A random sequence of runs of add_node and of remove_node calls on the octree `o` (applied
+    one by one), returned as [(kind, list of arguments)] for replay."""
+    runs = []
+    for _ in range(n_ops):
+        st = o.state()
+        live = [i for i in range(st["used_slots"]) if st["positions"][i] != 0xFFFFFFFF]
+        if rng.random() < 0.7 or len(live) < 3:
+            k = int(rng.integers(1, 12))
+            args = []
+            for _ in range(k):
+                st = o.state()
+                live = [i for i in range(st["used_slots"]) if st["positions"][i] != 0xFFFFFFFF]
+                parent = int(rng.choice(live)) if rng.random() < 0.9 else int(rng.integers(0, st["used_slots"]))
+                args.append((parent, int(rng.integers(0, 8))))
+                o.add_node(*args[-1])
+            runs.append(("add", args))
+        else:
+            k = int(rng.integers(1, 4))
+            args = []
+            for _ in range(k):
+                st = o.state()
+                live = [i for i in range(1, st["used_slots"]) if st["positions"][i] != 0xFFFFFFFF]
+                node = int(rng.choice(live)) if live else 0
+                args.append(node)
+                o.remove_node(node)
+            runs.append(("remove", args))
+        if rng.random() < 0.3:
+            o.increment_timer()
+            runs.append(("timer", []))
+    return runs
+
+
+def test_octree_batches_equal_single_calls(am):
+    """amr_octree_add_nodes / amr_octree_remove_nodes leave exactly the state the same calls one
+    by one leave (boundaries of every slot, removed ones included, lifetimes, counters)."""
+    rng = np.random.default_rng(3)
+    for trial in range(6):
+        slots = 300
+        single = am.Octree(slots)
+        runs = _random_regrid_ops(rng, single, 40, slots)
+        batched = am.Octree(slots)
+        for kind, args in runs:
+            if kind == "add":
+                batched.add_nodes([a[0] for a in args], [a[1] for a in args])
+            elif kind == "remove":
+                batched.remove_nodes(args)
+            else:
+                batched.increment_timer()
+            a, b = single.state(), batched.state()
+        for k in a:
+            assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), (trial, k)
+        single.close()
+        batched.close()
