@@ -26,6 +26,8 @@ ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_DEVICE, ERR_CAPACITY = 1, 2, 3, 4
 SIM_BSSN, SIM_WAVE = 1, 2
 DTYPE_UINT32, DTYPE_INT32, DTYPE_FLOAT32 = 0, 1, 2
 MODE_PLAIN, MODE_BATCHED, MODE_GRAPH = 0, 1, 2
+# the plugin interface's phases, in the order of the reference's timestep loop (AMR.h:324-333)
+PHASE_COPY_BACK, PHASE_MODIFY_NODES, PHASE_PREDICTOR, PHASE_COPY_BOUNDS, PHASE_CORRECTOR, PHASE_INCREMENT_TIMER = range(6)
 CHRISTOFFEL_REFERENCE, CHRISTOFFEL_RAISED = 0, 1
 
 VP = ctypes.c_void_p
@@ -106,6 +108,8 @@ EXPORTS = {
     "amr_sim_load": (ctypes.c_int, [VP, ctypes.c_char_p]),
     "amr_sim_timestep": (ctypes.c_int, [VP]),
     "amr_sim_copy_bounds": (ctypes.c_int, [VP]),
+    "amr_sim_phase": (ctypes.c_int, [VP, I32]),
+    "amr_sim_set_octree": (ctypes.c_int, [VP, VP, VP, VP, VP, VP, VP]),
     "amr_sim_rng": (ctypes.c_int, [VP, ctypes.POINTER(I32)]),
     "amr_sim_set_rng": (ctypes.c_int, [VP, I32]),
     "amr_sim_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),

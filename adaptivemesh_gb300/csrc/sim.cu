@@ -399,16 +399,17 @@ public:
         if ((st = build_items())) return st;
         f.ncomp = 6;
         for (int k = 0; k < 6; k++) { f.old_f[k] = old6[k]; f.new_f[k] = new6[k]; }
-        // With the fused predictor, leaves restrict themselves as the predictor streams their planes
-        // (old <- new plane by plane); only the domains with children are restricted here.
-        const bool fused = bssn_fused_supported(&cfg);
+        // Inside timestep(), with the fused predictor, leaves restrict themselves as the predictor
+        // streams their planes (old <- new plane by plane); only the domains with children are
+        // restricted here.  A phase called on its own restricts every active domain.
+        const bool fused = in_timestep && bssn_fused_supported(&cfg);
         if ((fused ? parent_count[s] : item_count[s]) == 0u) return AMR_OK;   // nothing to launch
         return check(launch_copy_new_to_old(dims, f, d_positions, d_children,
                                             d_items + (fused ? parent_offset[s] : item_offset[s]),
                                             fused ? parent_count[s] : item_count[s], s, md, stream, fused));
     }
     int modify_nodes() override { return AMR_OK; }              // BSSN.h:139-142
-    int predictor() override { return derivatives(old6, seed_slot(0), true); }
+    int predictor() override { return derivatives(old6, seed_slot(0), in_timestep); }
     int corrector() override { return derivatives(new6, seed_slot(1)); }
     int copy_bounds() override {                                 // BSSN.h:149-153
         int st = sync_octree();
@@ -994,6 +995,54 @@ AMR_API int amr_sim_save(amr_sim* s, const char* dir) {
     return AMR_OK;
 }
 
+// The device kernels index with these arrays: parents, children and boundary targets must name
+// slots, and positions must be free or no deeper than the depth limit.
+static bool octree_arrays_valid(uint32_t slots, const uint32_t* pos, const int32_t* par, const int32_t* ch,
+                                const uint64_t* bd) {
+    for (uint32_t i = 0; i < slots; i++)
+        if (pos_depth_host(pos[i]) > (int)kDepthLimit || par[i] < -1 || par[i] >= (int32_t)slots) return false;
+    for (size_t i = 0; i < (size_t)slots * 8u; i++)
+        if (ch[i] < -1 || ch[i] >= (int32_t)slots) return false;
+    for (size_t i = 0; i < (size_t)slots * 6u; i++) {
+        const uint32_t nd = (uint32_t)bd[i];
+        const int32_t target = (int32_t)((nd & 16777215u) | ((nd & (1u << 23)) ? 4278190080u : 0u));
+        if (target < -1 || target >= (int32_t)slots) return false;
+    }
+    return true;
+}
+
+AMR_API int amr_sim_set_octree(amr_sim* s, const uint32_t* positions, const int32_t* parent, const int32_t* children,
+                               const uint64_t* boundaries, const uint32_t* lifetime, const uint32_t* scalars5) {
+    if (!s || !positions || !parent || !children || !boundaries || !lifetime || !scalars5) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    const uint32_t slots = b->tree.max_slots();
+    const uint32_t timer = scalars5[0], max_depth = scalars5[1], first_free = scalars5[2], used = scalars5[3];
+    if (scalars5[4] != slots || max_depth > kDepthLimit || timer >= (1u << max_depth) || first_free > slots ||
+        used == 0u || used > slots || !octree_arrays_valid(slots, positions, parent, children, boundaries))
+        return AMR_ERR_INVALID;
+    int st = b->wait_side(-1, 0);   // side reads of the old tree's domains finish first
+    if (st) return st;
+    b->tree.restore(positions, parent, children, boundaries, lifetime, timer, (int)max_depth, first_free, used - 1u);
+    b->graph_valid = false;
+    return AMR_OK;
+}
+
+AMR_API int amr_sim_phase(amr_sim* s, int phase) {
+    if (!s) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    if (phase < AMR_PHASE_COPY_BACK || phase > AMR_PHASE_INCREMENT_TIMER) return AMR_ERR_INVALID;
+    const int st = b->wait_side(-1, 0);   // the phase may overwrite a buffer a side read still copies
+    if (st) return st;
+    switch (phase) {
+        case AMR_PHASE_COPY_BACK: return b->copy_back();
+        case AMR_PHASE_MODIFY_NODES: return b->modify_nodes();
+        case AMR_PHASE_PREDICTOR: return b->predictor();
+        case AMR_PHASE_COPY_BOUNDS: return b->copy_bounds();
+        case AMR_PHASE_CORRECTOR: return b->corrector();
+        default: b->tree.increment_timer(); return AMR_OK;
+    }
+}
+
 AMR_API int amr_sim_load(amr_sim* s, const char* dir) {
     if (!s || !dir) return AMR_ERR_INVALID;
     SimBase* b = s->impl;
@@ -1019,14 +1068,7 @@ AMR_API int amr_sim_load(amr_sim* s, const char* dir) {
         !read_file(d + "/boundaries.bin", bd.data(), (size_t)slots * 48u) ||
         !read_file(d + "/lifetime.bin", life.data(), slots * 4u))
         return AMR_ERR_INVALID;
-    // the device kernels index with these: children and boundary targets must name slots
-    for (int32_t c : ch)
-        if (c < -1 || c >= (int32_t)slots) return AMR_ERR_INVALID;
-    for (uint64_t v : bd) {
-        const uint32_t nd = (uint32_t)v;
-        const int32_t target = (int32_t)((nd & 16777215u) | ((nd & (1u << 23)) ? 4278190080u : 0u));
-        if (target < -1 || target >= (int32_t)slots) return AMR_ERR_INVALID;
-    }
+    if (!octree_arrays_valid(slots, pos.data(), par.data(), ch.data(), bd.data())) return AMR_ERR_INVALID;
     std::vector<uint8_t> host;
     for (int which = 0; which < 6; which++)
         for (int comp = 0; comp < 6; comp++) {

@@ -90,6 +90,20 @@ class Sim:
     def remove_node(self, node: int) -> None:
         check(load().amr_sim_remove_node(self.h, node), "amr_sim_remove_node")
 
+    def phase(self, phase: int) -> None:
+        """One phase of the plugin's timestep loop (amr_sim_phase; PHASE_* constants)."""
+        check(load().amr_sim_phase(self.h, phase), "amr_sim_phase")
+
+    def set_octree(self, state: dict) -> None:
+        """Replace the octree with arrays in the layout of state() (amr_sim_set_octree)."""
+        arrays = [np.ascontiguousarray(state[k], t) for k, t in
+                  (("positions", np.uint32), ("parent", np.int32), ("children", np.int32),
+                   ("boundaries", np.uint64), ("lifetime", np.uint32))]
+        sc = np.array([state["timer"], state["max_depth"], state["first_free"], state["used_slots"],
+                       state["max_slots"]], np.uint32)
+        check(load().amr_sim_set_octree(self.h, *[a.ctypes.data for a in arrays], sc.ctypes.data),
+              "amr_sim_set_octree")
+
     def add_nodes(self, parents, offsets) -> None:
         """add_node for each (parent, offset) in order, as one batch: the new nodes are prolongated
         at the end, one launch per depth level (amr_sim_add_nodes)."""

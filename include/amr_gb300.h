@@ -258,6 +258,27 @@ int amr_sim_event_record(amr_sim* s, int slot);
 int amr_sim_event_elapsed(amr_sim* s, int first, int second, float* ms);
 int amr_sim_timestep(amr_sim* s);                                      /* the plugin's timestep() */
 int amr_sim_copy_bounds(amr_sim* s);                                   /* the plugin's copy_bounds() */
+/* One phase of the plugin interface (AMR.h:296-334), for a caller that runs the reference's loop
+ *   do { copy_back; modify_nodes; predictor; copy_bounds; corrector; increment_timer } while (timer)
+ * itself (AMR.h:324-333): each call issues that phase's work on the simulation's stream and draws
+ * its seeds from the simulation's generator, so the loop of phases gives amr_sim_timestep's
+ * results bit for bit.  A single phase is self-contained (the BSSN copy_back restricts every
+ * active domain; inside amr_sim_timestep the leaves' restriction is fused into the predictor). */
+#define AMR_PHASE_COPY_BACK 0
+#define AMR_PHASE_MODIFY_NODES 1
+#define AMR_PHASE_PREDICTOR 2
+#define AMR_PHASE_COPY_BOUNDS 3
+#define AMR_PHASE_CORRECTOR 4
+#define AMR_PHASE_INCREMENT_TIMER 5   /* AMR<T>::increment_timer (AMR.h:180-188) */
+int amr_sim_phase(amr_sim* s, int phase);
+/* Replace the simulation's octree with arrays in the layout amr_sim_octree_state returns (the
+ * reference's AMR<T> arrays, AMR.h:118-136, and scalars5 = timer, max depth, first free slot,
+ * used slots, node_slots), as AMR<T>::copy_to_gpu uploads them (AMR.h:268-275), for a caller that
+ * keeps its own octree.  Children, parents and boundary targets must name slots and positions be
+ * free or at most 8 deep (AMR.h:9), else AMR_ERR_INVALID.  Fields are not touched (prolongate new nodes with
+ * amr_copy_to_child on amr_sim_buffer's addresses). */
+int amr_sim_set_octree(amr_sim* s, const uint32_t* positions, const int32_t* parent, const int32_t* children,
+                       const uint64_t* boundaries, const uint32_t* lifetime, const uint32_t* scalars5);
 int amr_sim_rng(const amr_sim* s, int32_t* seed);
 int amr_sim_set_rng(amr_sim* s, int32_t seed);
 int amr_sim_stream(amr_sim* s, void** stream);

@@ -433,3 +433,64 @@ def test_batched_regrid_matches_single_calls(am, cuda):
                              f"regrid round {rnd}")
     single.close()
     batched.close()
+
+
+@pytest.mark.parametrize("kind,mode", [("bssn", "plain"), ("bssn", "batched"), ("bssn", "graph"), ("wave", "batched")])
+def test_phase_loop_matches_timestep(am, cuda, kind, mode):
+    """The reference's loop of plugin phases, called one by one through amr_sim_phase, gives
+    amr_sim_timestep's state bit for bit; so does a simulation whose octree is uploaded with
+    amr_sim_set_octree from the other's arrays."""
+    import torch
+    mode_id = {"plain": am.MODE_PLAIN, "batched": am.MODE_BATCHED, "graph": am.MODE_GRAPH}[mode]
+    if kind == "bssn":
+        cfg = am.Config(16, 3, 100.0)
+        whole, _st, _ = _bssn_sim(am, cfg, "uneven", mode_id)
+        phased, _st, _ = _bssn_sim(am, cfg, "uneven", mode_id)
+        sim_kind, steps = am.SIM_BSSN, 2
+    else:
+        cfg = am.Config(28, 2, 100.0)
+        t = cfg.total
+        sims = []
+        for _ in range(2):
+            sim = am.Sim(cfg, am.SIM_WAVE, slots=128, mode=mode_id)
+            xyz = cases.cell_coordinates(sim.state()["positions"], 1, 28, 2, 100.0)
+            f0 = cases.smooth_field(xyz, 100.0, 0, 77, noise=0.0) * np.float32(0.5)
+            for which in (am.Sim.OLD, am.Sim.NEW):
+                sim.tensor(which)[: t ** 3].copy_(torch.from_numpy(f0).cuda())
+            torch.cuda.synchronize()
+            for c in range(8):
+                sim.add_node(0, c)
+            sims.append(sim)
+        whole, phased = sims
+        sim_kind, steps = am.SIM_WAVE, 3
+    for _ in range(steps):
+        whole.timestep()
+        while True:
+            for ph in (am.PHASE_COPY_BACK, am.PHASE_MODIFY_NODES, am.PHASE_PREDICTOR, am.PHASE_COPY_BOUNDS,
+                       am.PHASE_CORRECTOR, am.PHASE_INCREMENT_TIMER):
+                phased.phase(ph)
+            if phased.state()["timer"] == 0:
+                break
+    whole.synchronize()
+    phased.synchronize()
+    want = _full_state(am, whole, sim_kind)
+    _assert_states_equal(_full_state(am, phased, sim_kind), want, f"{kind} {mode} phases")
+    # a copy driven through an uploaded octree
+    copy = am.Sim(cfg, sim_kind, slots=128, mode=mode_id)
+    copy.set_octree(whole.state())
+    for which in range(6):
+        for k in (range(6) if sim_kind == am.SIM_BSSN else [0]):
+            try:
+                src = whole.tensor(which, k)
+            except am.AmrError:
+                continue
+            copy.tensor(which, k).copy_(src)
+    copy.rng = whole.rng
+    torch.cuda.synchronize()
+    whole.timestep()
+    copy.timestep()
+    whole.synchronize()
+    copy.synchronize()
+    _assert_states_equal(_full_state(am, copy, sim_kind), _full_state(am, whole, sim_kind), f"{kind} {mode} uploaded")
+    for sim in (whole, phased, copy):
+        sim.close()
