@@ -287,17 +287,18 @@ def main() -> None:
             dist.barrier()
 
     progress("value: device-resident timesteps")
-    # ---- device-resident timesteps (value); clocks are sampled from the warm-up on
-    with ClockSampler(local) as clocks:
-        for _ in range(args.warmup):
-            sim.timestep()
-        barrier()
-        launches0 = sim.kernel_launches
-        sim.event_record(0)
-        for _ in range(args.steps):
-            sim.timestep()
-        sim.event_record(1)
-        barrier()
+    # ---- device-resident timesteps (value); clocks are sampled from the warm-up on, through the
+    # end-to-end region below
+    clocks = ClockSampler(local).__enter__()
+    for _ in range(args.warmup):
+        sim.timestep()
+    barrier()
+    launches0 = sim.kernel_launches
+    sim.event_record(0)
+    for _ in range(args.steps):
+        sim.timestep()
+    sim.event_record(1)
+    barrier()
     ms = sim.event_elapsed(0, 1)
     gpu_launches = sim.kernel_launches - launches0
     if dist is not None:
@@ -324,6 +325,7 @@ def main() -> None:
     sim.event_record(3)           # follows the last step's downloads
     barrier()
     ms_e2e = sim.event_elapsed(2, 3)
+    clocks.__exit__(None, None, None)
     e2e_value = zones * args.steps * world / (ms_e2e / 1e3)
 
     progress("kernel timing")

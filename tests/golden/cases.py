@@ -59,7 +59,41 @@ def tree_uniform(o, depth: int):
         level = nxt
 
 
+def tree_root(o):
+    """The root alone: one domain at depth 0, no ghost fill."""
+
+
+def tree_deep(o):
+    """Nested refinement towards the centre down to the depth limit, 8 (AMR.h:9): 65 nodes.  Then
+    one add below a depth-8 node, which the octree ignores (AMR.h:211)."""
+    children = []
+    for c in range(8):
+        children.append(o.state()["first_free"])
+        o.add_node(0, c)
+    for _d in range(1, 8):
+        for c in range(8):
+            new_idx = o.state()["first_free"]
+            o.add_node(children[c], (~c) & 7)
+            children[c] = new_idx
+    o.add_node(children[0], 0)
+
+
+def tree_full(o):
+    """Root and eight children in a 9-slot octree: a further add is ignored (AMR.h:210) until a
+    removal frees a slot, which the next add reuses."""
+    for c in range(8):
+        o.add_node(0, c)
+    o.add_node(1, 0)
+    o.remove_node(3)
+    o.add_node(1, 0)
+    o.add_node(2, 5)
+
+
 TREES = {"wave": tree_wave, "bssn": tree_bssn, "uneven": tree_uneven}
+# limits: the depth limit and a full slot array (slots: deep 80, full 9)
+EDGE_TREES = {"root": tree_root, "deep": tree_deep, "full": tree_full}
+EDGE_SLOTS = {"root": 64, "deep": 80, "full": 9}
+ALL_TREES = {**TREES, **EDGE_TREES}
 
 
 # ---------------------------------------------------------------- field inputs

@@ -11,8 +11,8 @@ run the reference's __host__ code, are called).  Writes <out>/host_golden.npz wi
   morton/*     yield_sum_coordinates / yield_diff_coordinates / reverse_bits on random operands
   boundary/*   domain_boundary words between every pair of nodes of the 'bssn' and 'uneven' trees
   inverse/*    float3x3_sym::inverse on random symmetric positive-definite matrices
-  tree/<name>/*  the octree arrays (AMR.h:118-294) after building each tree of cases.TREES,
-               a uniform depth-2 tree and a random script of add / remove / timer / find
+  tree/<name>/*  the octree arrays (AMR.h:118-294) after building each tree of cases.TREES and
+               cases.EDGE_TREES (depth limit, full slot array), a uniform depth-2 tree and a random script of add / remove / timer / find
                operations; for the script also the state digest after every operation
 
 The committed copy is tests/golden/host_golden.npz, checked on the CPU by
@@ -146,6 +146,11 @@ def main(out_dir: str):
             out[f"boundary/{name}/pairs"] = np.array(pairs, np.int32)
             out[f"boundary/{name}/words"] = np.array(
                 [lib.refh_boundary(int(pos[i]), int(pos[j]), j) for i, j in pairs], np.uint64)
+        o.close()
+    for name, build in cases.EDGE_TREES.items():
+        o = reflib.RefOctree(lib, cases.EDGE_SLOTS[name])
+        build(o)
+        put_state(out, f"tree/{name}", o.state())
         o.close()
     o = reflib.RefOctree(lib, 80)
     cases.tree_uniform(o, 2)

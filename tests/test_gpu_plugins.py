@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 def _bssn_sim(am, cfg, tree, mode, seed=500):
     import torch
     sim = am.Sim(cfg, am.SIM_BSSN, slots=128, mode=mode)
-    cases.TREES[tree](sim)
+    cases.ALL_TREES[tree](sim)
     sim.synchronize()   # node_ctor prolongations run on the simulation's stream
     st = sim.state()
     used, t = st["used_slots"], cfg.total
@@ -55,7 +55,8 @@ def _same(a, b, what):
     assert bad == 0, f"{what}: {bad} of {a.size} words differ"
 
 
-@pytest.mark.parametrize("n,p,tree", [(16, 3, "wave"), (16, 3, "bssn"), (28, 2, "uneven"), (32, 3, "uneven")])
+@pytest.mark.parametrize("n,p,tree", [(16, 3, "wave"), (16, 3, "bssn"), (28, 2, "uneven"), (32, 3, "uneven"),
+                                      (16, 3, "root"), (16, 3, "deep"), (32, 3, "deep")])
 def test_bssn_modes_agree(am, cuda, n, p, tree):
     cfg = am.Config(n, p, 100.0)
     results = []
@@ -138,11 +139,11 @@ def test_bssn_timestep_matches_reference_plugin(am, cuda, ref16, steps):
     sim.close()
 
 
-@pytest.mark.parametrize("n,p", [(16, 3), (32, 3)])
-def test_bssn_timestep_matches_oracle(am, cuda, orc, n, p):
+@pytest.mark.parametrize("n,p,tree", [(16, 3, "uneven"), (32, 3, "uneven"), (16, 3, "root")])
+def test_bssn_timestep_matches_oracle(am, cuda, orc, n, p, tree):
     """One batched timestep (the fused pass; half-plane tiles at 32^3) against the oracle."""
     cfg = am.Config(n, p, 100.0)
-    sim, st, metric = _bssn_sim(am, cfg, "uneven", am.MODE_BATCHED)
+    sim, st, metric = _bssn_sim(am, cfg, tree, am.MODE_BATCHED)
     seed0 = sim.rng
     sim.timestep()
     sim.synchronize()

@@ -84,13 +84,15 @@ def test_inverse_within_contraction_noise(orc, hg):
     assert np.all(np.abs(out - ref) <= 2e-6 * scale)
 
 
-@pytest.mark.parametrize("tree", ["wave", "bssn", "uneven", "uniform2"])
+@pytest.mark.parametrize("tree", ["wave", "bssn", "uneven", "uniform2", "root", "deep", "full"])
 def test_octree_matches_reference(am, hg, tree):
-    o = am.Octree(80 if tree == "uniform2" else hgen.SLOTS)
+    """The octree arrays after building each tree equal the reference octree's, including the
+    depth limit ('deep') and a full slot array ('full')."""
+    o = am.Octree(80 if tree == "uniform2" else cases.EDGE_SLOTS.get(tree, hgen.SLOTS))
     if tree == "uniform2":
         cases.tree_uniform(o, 2)
     else:
-        cases.TREES[tree](o)
+        cases.ALL_TREES[tree](o)
     st = o.state()
     for k in ("positions", "parent", "children", "boundaries", "lifetime"):
         assert np.array_equal(st[k], hg[f"tree/{tree}/{k}"]), f"{tree}: {k}"
