@@ -59,6 +59,15 @@ struct StencilShape {
     // SK_BSSN: per thread, the 13 generator prefixes (d0, m0, d1, m1, ..., c) and the six gradient words
     static constexpr size_t TABLE_BYTES = KIND == SK_BSSN ? (size_t)(13 + 6) * CELLS * 4u : 0u;
     static constexpr size_t SMEM = RING_BYTES + BAR_BYTES + TABLE_BYTES;
+    // SK_BSSN: draw the Christoffel encodes' noise inside the unrolled component passes (faster
+    // at 32^3; at 16^3 the unrolled code is slower, measured, and at 28^3 it spills registers)
+    static constexpr bool kEarlyChristoffelDraws = N >= 32;
+    // SK_BSSN: CTAs per SM the launch bounds ask for, and the registers a thread may then use
+    static constexpr int CTAS = N * N <= 256 ? 2 : 1;
+    static constexpr int REG_BUDGET = 65536 / ((int)THREADS * CTAS);
+    // SK_BSSN: draw the mixed partials' noise at the top of a component pass, beside the other
+    // generator chains, where the registers allow it (not at 28^3: 72 registers a thread)
+    static constexpr bool kEarlyMixedDraws = REG_BUDGET >= 96;
     static_assert(N % TY == 0 && TILE_BYTES % 16u == 0u && (TY * T * 4) % 16 == 0, "tiles are aligned bulk copies");
     static_assert(NT == 1 || (OWN0 <= TY + 2 * P && OWN0 >= TY), "restriction rows lie in their tile");
     static constexpr uint32_t Q = N >= 16 ? 4u : 2u;              // z-ranges per split domain
@@ -200,7 +209,8 @@ __device__ __forceinline__ void mixed_partials2(const PL& pl, int c0, uint32_t x
 
 // Christoffel symbols of one cell from the six compressed metric gradients (BSSN.h:72-90).
 // `M` multiplies the lowered symbols: the metric itself (reference) or its inverse.
-__device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M, int32_t& rng, uint32_t* out) {
+// `noise` holds the encodes' noise pairs in draw order (noise_pairs1 per symbol pair).
+__device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M, const float2* noise, uint32_t* out) {
     float3 d[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) d[k] = cf3_decode(G[k]);
@@ -224,9 +234,8 @@ __device__ __forceinline__ void christoffel_cell(const uint32_t* G, const Sym& M
         const float2 rx = fma2(vz, splat2(M.xz), fma2(vx, splat2(M.xx), mul2(vy, splat2(M.xy))));
         const float2 ry = fma2(vz, splat2(M.yz), fma2(vx, splat2(M.xy), mul2(vy, splat2(M.yy))));
         const float2 rz = fma2(vz, splat2(M.zz), fma2(vx, splat2(M.xz), mul2(vy, splat2(M.yz))));
-        float2 nx, ny, nz;
-        noise_pairs1(rng, nx, ny, nz);
-        const Cf3Pair w = cf3_encode2<false>(rx, ry, rz, nx, ny, nz);
+        const Cf3Pair w = cf3_encode2<false>(rx, ry, rz, noise[3 * (jk / 2)], noise[3 * (jk / 2) + 1],
+                                             noise[3 * (jk / 2) + 2]);
         out[jk] = w.w0;
         out[jk + 1] = w.w1;
     }
@@ -408,11 +417,19 @@ __device__ __forceinline__ void bssn_cell(const StencilArgs& a, const float* rin
     // sequence); component 2j+1's ring lies R planes after component 2j's
     constexpr int OFF = R * (int)PLANE;
     const float2 DX1 = splat2(dx1), DX2 = splat2(dx2);
-#pragma unroll 1
-    for (int j = 0; j < 3; j++) {
+    // One pass: components 2j and 2j+1.
+    auto pass = [&](int j) {
         const int k0 = 2 * j, k1 = 2 * j + 1;
         const float* base = ring + (size_t)k0 * R * PLANE;
         auto pl = [&](int jj) { return base + (size_t)slot[jj] * PLANE; };
+        // the mixed partials' draws are independent of the others: drawn here, in the same
+        // straight-line block, the four generator chains interleave
+        float2 mnx, mny, mnz;
+        auto mixed_draws = [&] {
+            int32_t rm0 = cell_rng_at(s_pre[(2 * k0 + 1) * NN + tid], zg), rm1 = cell_rng_at(s_pre[(2 * k1 + 1) * NN + tid], zg);
+            noise_pairs2(rm0, rm1, mnx, mny, mnz);
+        };
+        if constexpr (S::kEarlyMixedDraws) mixed_draws();
         float2 gx, gy, gz, hx, hy, hz;
         fd_axes2<P, T, OFF>(pl, c0, gx, gy, gz, hx, hy, hz);
         int32_t rd0 = cell_rng_at(s_pre[(2 * k0) * NN + tid], zg), rd1 = cell_rng_at(s_pre[(2 * k1) * NN + tid], zg);
@@ -428,9 +445,8 @@ __device__ __forceinline__ void bssn_cell(const StencilArgs& a, const float* rin
         s_grad[k1 * NN + tid] = gk.w1;
         float2 mxy, mxz, myz;
         mixed_partials2<N, P, T, OFF>(pl, c0, x, y, z, mxy, mxz, myz);
-        int32_t rm0 = cell_rng_at(s_pre[(2 * k0 + 1) * NN + tid], zg), rm1 = cell_rng_at(s_pre[(2 * k1 + 1) * NN + tid], zg);
-        noise_pairs2(rm0, rm1, nx, ny, nz);
-        const Cf3Pair oq = cf3_encode2<true>(mul2(mxy, DX2), mul2(mxz, DX2), mul2(myz, DX2), nx, ny, nz);
+        if constexpr (!S::kEarlyMixedDraws) mixed_draws();
+        const Cf3Pair oq = cf3_encode2<true>(mul2(mxy, DX2), mul2(mxz, DX2), mul2(myz, DX2), mnx, mny, mnz);
         // trace_contra(H, ginv) with H = (hq.x, oq.x, oq.y, hq.y, oq.z, hq.z) (tensors.h:430-435)
         float2 ta = fma2(hq.vx, splat2(ginv.xx), mul2(hq.vy, splat2(ginv.yy)));
         ta = fma2(hq.vz, splat2(ginv.zz), ta);
@@ -439,19 +455,36 @@ __device__ __forceinline__ void bssn_cell(const StencilArgs& a, const float* rin
         const float2 lap = fma2(tb, splat2(2.f), ta);
         a.lap[k0][o] = lap.x;
         a.lap[k1][o] = lap.y;
+    };
+    // The Christoffel encodes' generator is one chain of 18 draws.  With kEarlyChristoffelDraws
+    // the three passes are unrolled and each advances it by 6 draws alongside its own chains;
+    // otherwise the passes share one loop body (smaller code: faster at 16^3, measured) and the
+    // chain runs after them.
+    int32_t rc = cell_rng_at(s_pre[12 * NN + tid], zg);
+    float2 cn[9];
+    if constexpr (S::kEarlyChristoffelDraws) {
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            noise_pairs1(rc, cn[3 * j], cn[3 * j + 1], cn[3 * j + 2]);
+            pass(j);
+        }
+    } else {
+#pragma unroll 1
+        for (int j = 0; j < 3; j++) pass(j);
+#pragma unroll
+        for (int j = 0; j < 3; j++) noise_pairs1(rc, cn[3 * j], cn[3 * j + 1], cn[3 * j + 2]);
     }
     uint32_t G[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) G[k] = s_grad[k * NN + tid];
-    int32_t rc = cell_rng_at(s_pre[12 * NN + tid], zg);
     uint32_t out[6];
-    christoffel_cell(G, a.christoffel_mode == AMR_CHRISTOFFEL_RAISED ? ginv : g, rc, out);
+    christoffel_cell(G, a.christoffel_mode == AMR_CHRISTOFFEL_RAISED ? ginv : g, cn, out);
 #pragma unroll
     for (int k = 0; k < 6; k++) a.chr[k][o] = out[k];
 }
 
 template <int N, int P>
-__global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, N * N <= 256 ? 2 : 1)
+__global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, StencilShape<N, P, SK_BSSN>::CTAS)
     k_stencil_bssn(const __grid_constant__ StencilArgs a) {
     using S = StencilShape<N, P, SK_BSSN>;
     constexpr int T = S::T, NC = 6, R = S::R;
