@@ -120,6 +120,7 @@ EXPORTS = {
     "amr_inclusive_scan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP]),
     "amr_reduce_max": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP, VP]),
     "amr_reduce_min": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP, VP]),
+    "amr_field_norms": (ctypes.c_int, [CP, VP, VP, VP, U32, VP, VP]),
 }
 
 _LIB = None

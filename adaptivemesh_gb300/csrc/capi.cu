@@ -214,6 +214,13 @@ AMR_API int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_
     if (!stage && used) return cuda_status(e);
     return cuda_status(launch_copy_boundaries(d, f, boundaries, used, substep, max_depth, copy_only_new, stage, S(stream)));
 }
+AMR_API int amr_field_norms(const amr_config* cfg, const float* field, const uint32_t* positions, const int32_t* children,
+                            uint32_t used, double* out4, void* stream) {
+    AMR_REQUIRE_CFG(cfg);
+    AMR_REQUIRE(field && positions && children && out4);
+    return field_norms(cfg->size_domain, cfg->padding_domain, field, positions, children, used, out4,
+                       static_cast<cudaStream_t>(stream));
+}
 AMR_API int amr_copy_new_to_old(const amr_config* cfg, float* old_f, const float* new_f, const uint32_t* positions,
                                 const int32_t* children, uint32_t used, uint32_t substep, uint32_t max_depth,
                                 void* stream) {

@@ -91,6 +91,10 @@ cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* po
 cudaError_t launch_copy_to_child(Dims d, float* buf, uint32_t offset, int32_t child, int32_t parent, cudaStream_t st);
 // Prolongation of n_items new nodes at once into each of nbuf (<= 12) buffers; items holds
 // (child, parent, offset) triples in device memory, none a parent of another.
+// FP64 norms of a padded field over the leaf domains' interior cells (reduce.cu): out4 = sum, sum
+// of squares, largest magnitude, cell count; synchronises the stream; returns an AMR_* status.
+int field_norms(uint32_t n, uint32_t p, const float* field, const uint32_t* positions, const int32_t* children,
+                uint32_t used, double* out4, cudaStream_t st);
 cudaError_t launch_copy_to_children(Dims d, float* const* bufs, int nbuf, const int32_t* items, uint32_t n_items,
                                     cudaStream_t st);
 // Staging for the ghost fill (the innermost layer of the three lower faces, old and new):

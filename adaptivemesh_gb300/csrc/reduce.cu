@@ -1,5 +1,6 @@
 // reduce.cu -- the reference's general-purpose scan and reductions (AdaptiveMesh/parallel.h) on
-// arrays of 1-4 component elements of uint32, int32 or float32.
+// arrays of 1-4 component elements of uint32, int32 or float32, and FP64 norms of a field over
+// the leaf domains (no counterpart in the reference).
 //
 // The results, including the values these functions leave in the buffer, are the reference's:
 // the same multi-pass scheme over 512-element blocks, each block combining its elements in the
@@ -192,7 +193,98 @@ struct Min {
     static int run(S* d, uint32_t n, void* r, cudaStream_t st) { return status_of(extreme<S, NC, false>(d, n, r, st)); }
 };
 
+// ---------------------------------------------------------------- FP64 norms of a padded field
+// Over the interior cells of the leaf domains (live slots without children): sum, sum of squares
+// and largest magnitude, in double.  Every cell's value is exact in double and so is its square;
+// the sums are taken in a fixed order (a thread's cells in index order, then fixed trees over the
+// threads of a domain and over the domains), so a result is the same on every run.
+constexpr uint32_t kNormThreads = 256;
+struct NormPart {
+    double sum, sq, max_abs, cells;
+};
+__device__ __forceinline__ NormPart norm_join(NormPart a, const NormPart& b) {
+    a.sum += b.sum;
+    a.sq += b.sq;
+    a.max_abs = (a.max_abs != a.max_abs || b.max_abs != b.max_abs) ? __longlong_as_double(0x7FF8000000000000ll)
+                                                                  : fmax(a.max_abs, b.max_abs);
+    a.cells += b.cells;
+    return a;
+}
+__device__ NormPart norm_block(NormPart v) {   // fixed tree: lanes by xor distance, then warps in order
+    __shared__ NormPart warp_part[kNormThreads / 32];
+    for (int d = 16; d >= 1; d >>= 1) {
+        NormPart o;
+        o.sum = __shfl_xor_sync(0xFFFFFFFFu, v.sum, d);
+        o.sq = __shfl_xor_sync(0xFFFFFFFFu, v.sq, d);
+        o.max_abs = __shfl_xor_sync(0xFFFFFFFFu, v.max_abs, d);
+        o.cells = __shfl_xor_sync(0xFFFFFFFFu, v.cells, d);
+        v = (threadIdx.x & (uint32_t)d) ? norm_join(o, v) : norm_join(v, o);   // lower lane's value first
+    }
+    if ((threadIdx.x & 31u) == 0u) warp_part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    NormPart r = warp_part[0];
+    for (uint32_t w = 1; w < kNormThreads / 32; w++) r = norm_join(r, warp_part[w]);
+    return r;
+}
+__global__ void __launch_bounds__(kNormThreads) k_norms_domain(const float* __restrict__ f, const uint32_t* __restrict__ pos,
+                                                               const int32_t* __restrict__ children, uint32_t n,
+                                                               uint32_t p, NormPart* __restrict__ part) {
+    const uint32_t slot = blockIdx.x, t = n + 2u * p;
+    bool leaf = pos[slot] != 0xFFFFFFFFu;
+    for (int c = 0; c < 8; c++) leaf &= children[(size_t)slot * 8u + c] == -1;
+    NormPart v{0.0, 0.0, 0.0, 0.0};
+    if (leaf) {   // uniform in the block
+        const float* d = f + (size_t)slot * t * t * t;
+        for (uint32_t i = threadIdx.x; i < n * n * n; i += kNormThreads) {
+            const uint32_t x = i % n, y = (i / n) % n, z = i / (n * n);
+            const double a = (double)d[((z + p) * t + y + p) * t + x + p];
+            v.sum += a;
+            v.sq = fma(a, a, v.sq);
+            v.max_abs = (a != a || v.max_abs != v.max_abs) ? a + v.max_abs : fmax(v.max_abs, fabs(a));
+            v.cells += 1.0;
+        }
+    }
+    const NormPart r = norm_block(v);
+    if (threadIdx.x == 0) part[slot] = r;
+}
+__global__ void __launch_bounds__(kNormThreads) k_norms_total(const NormPart* __restrict__ part, uint32_t used,
+                                                              NormPart* __restrict__ out) {
+    NormPart v{0.0, 0.0, 0.0, 0.0};
+    for (uint32_t s = threadIdx.x; s < used; s += kNormThreads) v = norm_join(v, part[s]);
+    const NormPart r = norm_block(v);
+    if (threadIdx.x == 0) *out = r;
+}
+
 }  // namespace
+
+int field_norms(uint32_t n, uint32_t p, const float* field, const uint32_t* positions, const int32_t* children,
+                uint32_t used, double* out4, cudaStream_t st) {
+    if (used == 0) {
+        for (int i = 0; i < 4; i++) out4[i] = 0.0;
+        return AMR_OK;
+    }
+    NormPart* part = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&part), sizeof(NormPart) * (used + 1u), st);
+    if (e != cudaSuccess) return AMR_ERR_CUDA;
+    k_norms_domain<<<used, kNormThreads, 0, st>>>(field, positions, children, n, p, part);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_norms_total<<<1, kNormThreads, 0, st>>>(part, used, part + used);
+        e = cudaGetLastError();
+    }
+    NormPart r{};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&r, part + used, sizeof(r), cudaMemcpyDeviceToHost, st);
+    const cudaError_t f = cudaFreeAsync(part, st);
+    if (e == cudaSuccess) e = f;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return AMR_ERR_CUDA;
+    out4[0] = r.sum;
+    out4[1] = r.sq;
+    out4[2] = r.max_abs;
+    out4[3] = r.cells;
+    return AMR_OK;
+}
+
 }  // namespace amr
 
 #define AMR_API extern "C" __attribute__((visibility("default")))

@@ -132,3 +132,13 @@ def _extreme(fn, name, data, ncomp, stream):
     out = np.zeros(ncomp, {torch.float32: np.float32, torch.int32: np.int32, torch.uint32: np.uint32}[data.dtype])
     check(fn(_dtype_of(data), ncomp, _p(data), data.numel() // ncomp, out.ctypes.data, _s(stream)), name)
     return out.tolist()
+
+
+def field_norms(cfg: Config, field, positions, children, used: int, stream=None) -> dict:
+    """FP64 sum, sum of squares, largest magnitude and cell count of a padded field over the leaf
+    domains' interior cells (amr_field_norms)."""
+    import numpy as np
+    out = np.zeros(4, np.float64)
+    check(load().amr_field_norms(ctypes.byref(cfg), _p(field), _p(positions), _p(children), used, out.ctypes.data,
+                                 _s(stream)), "amr_field_norms")
+    return {"sum": float(out[0]), "sum_sq": float(out[1]), "max_abs": float(out[2]), "cells": int(out[3])}

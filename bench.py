@@ -361,6 +361,16 @@ def main() -> None:
             tr = json.load(f)
         roofline["traffic"] = (tr["corrector_dram_bytes_per_domain"] * per_step / 2 +
                                tr["predictor_dram_bytes_per_domain"] * per_step / 2) / (2 << md)
+        # The kernel is issue-bound: its instruction rate against the SMs' issue peak (4 warp
+        # instructions per SM and cycle at the SM clock sampled under load)
+        inst = (tr["corrector_warp_instructions_per_domain"] * per_step / 2 +
+                tr["predictor_warp_instructions_per_domain"] * per_step / 2) / (2 << md)
+        sm_mhz = clocks.summary()["sm_mhz"] or 2070.0
+        issue_peak = torch.cuda.get_device_properties(local).multi_processor_count * 4 * sm_mhz * 1e6
+        if k_n:
+            rate = inst / (k_ms / k_n / 1e3)
+            roofline["issue"] = {"achieved": rate, "peak": issue_peak, "unit": "warp-instructions/s",
+                                 "frac": rate / issue_peak, "instructions_per_launch": inst}
     except (OSError, KeyError, ValueError):
         pass
 

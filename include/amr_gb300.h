@@ -311,6 +311,14 @@ int amr_reduce_max(int dtype, int ncomp, void* data, uint64_t count, void* resul
  * of 512 that runs past the end of the array counts its missing elements as 0 (parallel.h:389),
  * so the result is at most 0 unless every pass fills its blocks. */
 int amr_reduce_min(int dtype, int ncomp, void* data, uint64_t count, void* result, void* stream);
+/* Norms of a padded field (slot-major, the layout of cyij_old / old_field) over the interior cells
+ * of the leaf domains (live slots with no children, from the device arrays positions[used] and
+ * children[8 * used]), in double precision, for monitoring a field or a constraint residual:
+ * out4 = {sum, sum of squares, largest magnitude (NaN if any cell is NaN), number of cells}.  The
+ * reduction order is fixed, so a result repeats exactly.  Synchronises the stream.  No counterpart
+ * in the reference, which has no FP64 reductions. */
+int amr_field_norms(const amr_config* cfg, const float* field, const uint32_t* positions, const int32_t* children,
+                    uint32_t used_slots, double* out4, void* stream);
 
 #ifdef __cplusplus
 }

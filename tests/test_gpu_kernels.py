@@ -476,3 +476,36 @@ def test_scan_and_reductions(am, cuda, orc, dtype, ncomp):
                     assert_same(mine, rd.cpu().numpy().view(np.uint32), f"{what}: array vs reference")
                     if res is not None:
                         assert_same(np.array(res, a.dtype).view(np.uint32), rr.view(np.uint32), f"{what}: result vs reference")
+
+
+@pytest.mark.parametrize("cfgname,tree", [("n16p3", "uneven"), ("n28p2", "bssn"), ("n16p3", "root")])
+def test_field_norms(am, cuda, cfgname, tree):
+    """amr_field_norms against float64 sums over the same leaf interior cells: count and largest
+    magnitude exact, sums within a few ulp (their order differs), identical on repeat; a NaN cell
+    makes the largest magnitude NaN."""
+    import torch
+    n, p = {"n16p3": (16, 3), "n28p2": (28, 2)}[cfgname]
+    cfg = am.Config(n, p, 100.0)
+    t = n + 2 * p
+    o = am.Octree(64)
+    cases.ALL_TREES[tree](o)
+    st = o.state()
+    used = st["used_slots"]
+    rng = np.random.default_rng(5)
+    f = (rng.standard_normal(used * t ** 3) * 3.0).astype(np.float32)
+    ch = st["children"][: used * 8].reshape(used, 8)
+    leaves = [s for s in range(used) if st["positions"][s] != 0xFFFFFFFF and (ch[s] == -1).all()]
+    cube = f.reshape(used, t, t, t)[leaves][:, p:p + n, p:p + n, p:p + n].astype(np.float64)
+    d_f = torch.from_numpy(f).cuda()
+    d_pos = torch.from_numpy(st["positions"][:used].view(np.int32)).cuda()
+    d_ch = torch.from_numpy(st["children"][: used * 8]).cuda()
+    r = am.ops.field_norms(cfg, d_f, d_pos, d_ch, used)
+    assert r["cells"] == cube.size
+    assert r["max_abs"] == np.abs(cube).max()
+    assert abs(r["sum"] - cube.sum()) <= 1e-12 * np.abs(cube).sum()
+    assert abs(r["sum_sq"] - (cube * cube).sum()) <= 1e-12 * (cube * cube).sum()
+    assert am.ops.field_norms(cfg, d_f, d_pos, d_ch, used) == r
+    s = leaves[-1]
+    d_f[s * t ** 3 + (p * t + p) * t + p + 1] = float("nan")
+    assert np.isnan(am.ops.field_norms(cfg, d_f, d_pos, d_ch, used)["max_abs"])
+    o.close()

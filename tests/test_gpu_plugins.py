@@ -495,3 +495,26 @@ def test_phase_loop_matches_timestep(am, cuda, kind, mode):
     _assert_states_equal(_full_state(am, copy, sim_kind), _full_state(am, whole, sim_kind), f"{kind} {mode} uploaded")
     for sim in (whole, phased, copy):
         sim.close()
+
+
+def test_set_octree_refuses_bad_arrays(am, cuda):
+    """amr_sim_set_octree checks every index the device kernels would use before taking the
+    arrays; a refused upload leaves the simulation's octree as it was."""
+    cfg = am.Config(16, 3, 100.0)
+    sim = am.Sim(cfg, am.SIM_BSSN, slots=32, mode=am.MODE_BATCHED)
+    for c in range(8):
+        sim.add_node(0, c)
+    good = sim.state()
+    sim.set_octree(good)
+    for key, idx, bad in (("children", 3, 32), ("children", 0, -2), ("parent", 4, 99),
+                          ("positions", 5, (9 << 27) | 1), ("boundaries", 7, 0x00000000007FFFFF),
+                          ("max_slots", None, 64), ("used_slots", None, 0), ("timer", None, 2)):
+        st = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in good.items()}
+        if idx is None:
+            st[key] = bad
+        else:
+            st[key][idx] = bad
+        with pytest.raises(am.AmrError):
+            sim.set_octree(st)
+    _assert_states_equal(sim.state(), good, "after refused uploads")
+    sim.close()
