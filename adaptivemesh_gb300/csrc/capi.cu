@@ -55,13 +55,10 @@ cudaError_t launch_stencil(const amr_config& c, int kind, const StencilArgs& a, 
 // Persistent grid for the streaming stencil: as many CTAs as fit on the device at once, but no
 // more than there are work items.
 uint32_t stencil_grid(const amr_config& c, int kind, uint32_t n_items) {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+    int dev = 0, sms = 0;   // the current device's
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
     size_t smem = 0;
 #define AMR_SMEM(N, P) \
     if (c.size_domain == N && c.padding_domain == P) smem = kind == SK_BSSN ? stencil_smem_bytes<N, P, SK_BSSN>() : stencil_smem_bytes<N, P, SK_GRAD>();
@@ -75,37 +72,22 @@ uint32_t stencil_grid(const amr_config& c, int kind, uint32_t n_items) {
     return n_items < cap ? n_items : cap;
 }
 
-// Device error flag shared by the operator entry points (set by bounded waits that give up).
+// Error flag of the current device, shared by the operator entry points and the simulations on
+// that device (set by bounded waits that give up); allocated on first use per device.
 int* device_error_flag() {
-    static int* flag = nullptr;
+    constexpr int kMaxDevices = 64;
+    static int* flag[kMaxDevices] = {};
     static std::mutex mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
     std::lock_guard<std::mutex> lock(mu);
-    if (!flag) {
-        if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) { flag = nullptr; return nullptr; }
-        cudaMemset(flag, 0, sizeof(int));
+    if (!flag[dev]) {
+        int* p = nullptr;
+        if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
+        if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) { cudaFree(p); return nullptr; }
+        flag[dev] = p;
     }
-    return flag;
-}
-
-// Per-process staging buffer for amr_copy_boundaries: allocated on first use, grown on demand.
-static float* ghost_stage(size_t floats, cudaStream_t st, cudaError_t* err) {
-    static float* buf = nullptr;
-    static size_t cap = 0;
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lock(mu);
-    *err = cudaSuccess;
-    if (floats <= cap) return buf;
-    if (buf) {
-        *err = cudaStreamSynchronize(st);
-        if (*err != cudaSuccess) return nullptr;
-        cudaFree(buf);
-        buf = nullptr;
-        cap = 0;
-    }
-    *err = cudaMalloc(&buf, floats * sizeof(float));
-    if (*err != cudaSuccess) { buf = nullptr; return nullptr; }
-    cap = floats;
-    return buf;
+    return flag[dev];
 }
 
 }  // namespace amr
@@ -209,10 +191,19 @@ AMR_API int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_
     f.old_f[0] = old_f;
     f.new_f[0] = new_f;
     f.ncomp = 1;
-    cudaError_t e;
-    float* stage = ghost_stage(ghost_scratch_floats(d, used, 1), S(stream), &e);
-    if (!stage && used) return cuda_status(e);
-    return cuda_status(launch_copy_boundaries(d, f, boundaries, used, substep, max_depth, copy_only_new, stage, S(stream)));
+    // staging from the device's stream-ordered pool: nothing is shared between calls, streams or
+    // devices, and the memory returns to the pool after the fill
+    float* stage = nullptr;
+    const size_t bytes = ghost_scratch_floats(d, used, 1) * sizeof(float);
+    cudaError_t e = cudaSuccess;
+    if (bytes) e = cudaMallocAsync(reinterpret_cast<void**>(&stage), bytes, S(stream));
+    if (e != cudaSuccess) return cuda_status(e);
+    e = launch_copy_boundaries(d, f, boundaries, used, substep, max_depth, copy_only_new, stage, S(stream));
+    if (stage) {
+        const cudaError_t e2 = cudaFreeAsync(stage, S(stream));
+        if (e == cudaSuccess) e = e2;
+    }
+    return cuda_status(e);
 }
 AMR_API int amr_field_norms(const amr_config* cfg, const float* field, const uint32_t* positions, const int32_t* children,
                             uint32_t used, double* out4, void* stream) {

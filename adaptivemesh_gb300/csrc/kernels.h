@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstddef>
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -15,6 +16,21 @@
 #define AMR_FOR_EACH_BSSN_CONFIG(X) X(16, 3) X(28, 2) X(32, 3) X(8, 2)
 
 namespace amr {
+
+// cudaFuncSetAttribute(kernel, MaxDynamicSharedMemorySize) once per device: the attribute belongs
+// to a device's context, so `mask` keeps one bit per device ordinal (< 64) where it is set.
+// Concurrent first calls set it twice, which is harmless.
+template <class K>
+cudaError_t ensure_smem_limit(K* kernel, size_t bytes, std::atomic<uint64_t>& mask) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (mask.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) mask.fetch_or(bit, std::memory_order_release);
+    return e;
+}
 
 enum StencilKind { SK_GRAD = 0, SK_GRAD_HESS = 1, SK_MIXED = 2, SK_BSSN = 3 };
 

@@ -487,13 +487,9 @@ cudaError_t launch_copy_boundaries(Dims d, const FieldSet& f, const uint64_t* bo
     const int in_place = copy_only_new && sources_restricted ? 1 : 0;
 #define AMR_GHOST(N, P)                                                                                     \
     if (d.n == N && d.p == P) {                                                                             \
-        static bool configured = false;                                                                     \
-        if (!configured) {                                                                                  \
-            cudaError_t e = cudaFuncSetAttribute(k_ghost_face<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                                 (int)GhostBox<N, P>::SMEM);                                \
-            if (e != cudaSuccess) return e;                                                                 \
-            configured = true;                                                                              \
-        }                                                                                                   \
+        static std::atomic<uint64_t> configured{0};                                                         \
+        if (const cudaError_t e0 = ensure_smem_limit(k_ghost_face<N, P>, GhostBox<N, P>::SMEM, configured))   \
+            return e0;                                                                                      \
         if (used == 0 || f.ncomp == 0) return cudaSuccess;                                                  \
         k_ghost_face<N, P><<<used * 6u, kBlock, GhostBox<N, P>::SMEM, st>>>(f, boundaries, used, substep,     \
                                                                           max_depth, copy_only_new, in_place, \

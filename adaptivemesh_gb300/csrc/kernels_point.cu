@@ -329,13 +329,10 @@ __global__ void __launch_bounds__(kBlock) k_copy_words1(float* __restrict__ dst,
 
 cudaError_t launch_copy_words(void* dst, const void* src, uint64_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+    int dev = 0, sms = 0;   // the current device's
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
     const uint32_t cap = (uint32_t)sms * 8u;
     if ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) % 16u == 0u) {
         const uint64_t n4 = n / 4u;

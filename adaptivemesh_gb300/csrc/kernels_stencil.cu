@@ -658,15 +658,12 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, StencilS
 template <int N, int P, int KIND>
 cudaError_t launch_stencil_t(const StencilArgs& a, uint32_t grid, cudaStream_t st) {
     using S = StencilShape<N, P, KIND>;
-    static bool configured = false;
+    static std::atomic<uint64_t> configured{0};
     void (*kernel)(const StencilArgs);
     if constexpr (KIND == SK_BSSN) kernel = k_stencil_bssn<N, P>;
     else kernel = k_stencil<N, P, KIND>;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    const cudaError_t e = ensure_smem_limit(kernel, S::SMEM, configured);
+    if (e != cudaSuccess) return e;
     if (grid == 0) return cudaSuccess;
     kernel<<<grid, S::THREADS, S::SMEM, st>>>(a);
     return cudaGetLastError();

@@ -90,8 +90,8 @@ int amr_christoffel(const amr_config* cfg, float* const* metric6, uint32_t* cons
 /* Face ghost fill with space (10-point) and time interpolation from the coarser-or-equal
  * neighbour.  Replaces copy_boundaries(), AMR.h:880-900.  All reads see the fields as they
  * were before the call (the reference's single launch races where a domain reads a coarser
- * neighbour's innermost ghost layer); the values are staged in a per-device scratch buffer that
- * the library allocates on first use and grows when needed. */
+ * neighbour's innermost ghost layer); the values are staged in scratch memory that each call
+ * takes from the device's stream-ordered pool (cudaMallocAsync) and returns after the fill. */
 int amr_copy_boundaries(const amr_config* cfg, float* old_f, float* new_f, const uint64_t* boundaries,
                         uint32_t used_slots, uint32_t substep, uint32_t max_depth, int copy_only_new,
                         void* stream);
