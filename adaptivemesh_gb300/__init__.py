@@ -72,6 +72,7 @@ EXPORTS = {
     "amr_rasterise": (ctypes.c_int, [CP, VP, VP, U32, U32, U32, ctypes.c_float, ctypes.c_int, VP, VP]),
     "amr_partition_morton": (ctypes.c_int, [VP, U32, U32, VP]),
     "amr_ghost_exchange_plan": (ctypes.c_int, [CP, VP, VP, U32, U32, U32, U32, VP, U32, VP]),
+    "amr_restriction_exchange_plan": (ctypes.c_int, [CP, VP, VP, VP, U32, U32, U32, U32, VP, U32, VP]),
     "amr_pack_boxes": (ctypes.c_int, [CP, VP, U32, VP, VP, U32, VP, VP]),
     "amr_unpack_boxes": (ctypes.c_int, [CP, VP, U32, VP, VP, U32, VP, VP]),
     "amr_copy_new_to_old": (ctypes.c_int, [CP, VP, VP, VP, VP, U32, U32, U32, VP]),

@@ -131,3 +131,36 @@ int amr_ghost_exchange_plan(const amr_config* cfg, const uint64_t* boundaries, c
     for (size_t i = 0; i < kept.size(); i++) std::memcpy(boxes + 8u * i, kept[i].data(), 8u * sizeof(uint32_t));
     return AMR_OK;
 }
+
+// The restriction (copy_new_to_old, AMR.h:961-996) of an active domain with children averages each
+// child's new field over 2x2x2 cells, which covers the child's whole interior.  So before the
+// restriction of `substep`, `rank` needs the interior of every child that another rank owns of every
+// active domain that it owns; same records as the ghost plan.
+extern "C" __attribute__((visibility("default")))
+int amr_restriction_exchange_plan(const amr_config* cfg, const uint32_t* positions, const int32_t* children,
+                                  const int32_t* owner, uint32_t used_slots, uint32_t substep, uint32_t max_depth,
+                                  uint32_t rank, uint32_t* boxes, uint32_t capacity, uint32_t* n_boxes) {
+    if (!cfg) return AMR_ERR_INVALID;
+    if (!config_supported(cfg)) return AMR_ERR_UNSUPPORTED;
+    if (!positions || !children || !owner || !n_boxes || (capacity && !boxes) || max_depth > kDepthLimit)
+        return AMR_ERR_INVALID;
+    const uint32_t n = cfg->size_domain, p = cfg->padding_domain;
+    std::vector<uint32_t> out;
+    for (uint32_t s = 0; s < used_slots; s++) {
+        const int d = pos_depth_host(positions[s]);
+        if (owner[s] != (int32_t)rank || d == -1 || d > (int)max_depth) continue;
+        if ((substep & ((1u << (max_depth - (uint32_t)d)) - 1u)) != 0u) continue;   // not active
+        for (uint32_t i = 0; i < 8u; i++) {
+            const int32_t c = children[(size_t)s * 8u + i];
+            if (c == -1) continue;
+            if (c < 0 || (uint32_t)c >= used_slots || owner[c] < 0) return AMR_ERR_INVALID;
+            if (owner[c] == (int32_t)rank) continue;
+            const uint32_t rec[8] = {(uint32_t)c, (uint32_t)owner[c], p, p, p, n, n, n};
+            out.insert(out.end(), rec, rec + 8);
+        }
+    }
+    *n_boxes = (uint32_t)(out.size() / 8u);
+    if (*n_boxes > capacity) return AMR_ERR_CAPACITY;
+    if (!out.empty()) std::memcpy(boxes, out.data(), out.size() * sizeof(uint32_t));
+    return AMR_OK;
+}

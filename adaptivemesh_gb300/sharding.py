@@ -1,10 +1,12 @@
 """Sharding the per-timestep path by domain across ranks.
 
 Domains are independent given their ghost cells, so ranks own contiguous Morton ranges of the
-octree's slots (amr_partition_morton) and compute only those.  The one exchange per substep comes
-before the ghost fill: each rank receives, from the owners, the source boxes its faces interpolate
-from (amr_ghost_exchange_plan; the boxes the fill kernel itself reads), for the old and the new
-field of every component, then fills its own domains' ghosts locally.  The reference runs on one
+octree's slots (amr_partition_morton) and compute only those.  Two exchanges per substep: before
+the restriction, each rank receives the new field's interior of the children, owned elsewhere, of
+its active domains (amr_restriction_exchange_plan); before the ghost fill, it receives from the
+owners the source boxes its faces interpolate from (amr_ghost_exchange_plan; the boxes the fill
+kernel itself reads), for the old and the new field of every component, then fills its own
+domains' ghosts locally.  The reference runs on one
 GPU (AdaptiveMesh/AMR.h:880-933 fills all faces in one launch); this module is the host side of
 the multi-rank form.  Transport is torch.distributed point-to-point (NCCL on GPUs, gloo on CPUs);
 packing and unpacking are passed in, so device buffers use amr_pack_boxes / amr_unpack_boxes and
@@ -45,6 +47,25 @@ def exchange_plan(cfg: Config, boundaries: np.ndarray, owner: np.ndarray, used: 
     if n.value:
         check(lib.amr_ghost_exchange_plan(ctypes.byref(cfg), bd.ctypes.data, own.ctypes.data, used, substep,
                                           max_depth, rank, boxes.ctypes.data, n.value, ctypes.byref(n)))
+    return boxes
+
+
+def restriction_plan(cfg: Config, positions: np.ndarray, children: np.ndarray, owner: np.ndarray, used: int,
+                     substep: int, max_depth: int, rank: int) -> np.ndarray:
+    """The boxes (children's interiors of the new field) `rank` receives before the restriction of
+    `substep`, as an (n, 8) uint32 array (amr_restriction_exchange_plan)."""
+    lib = load()
+    pos = np.ascontiguousarray(positions[:used], dtype=np.uint32)
+    ch = np.ascontiguousarray(children[: used * 8], dtype=np.int32)
+    own = np.ascontiguousarray(owner[:used], dtype=np.int32)
+    n = ctypes.c_uint32(0)
+    args = (ctypes.byref(cfg), pos.ctypes.data, ch.ctypes.data, own.ctypes.data, used, substep, max_depth, rank)
+    st = lib.amr_restriction_exchange_plan(*args, None, 0, ctypes.byref(n))
+    if st != ERR_CAPACITY:
+        check(st)
+    boxes = np.zeros((n.value, BOX_WORDS), np.uint32)
+    if n.value:
+        check(lib.amr_restriction_exchange_plan(*args, boxes.ctypes.data, n.value, ctypes.byref(n)))
     return boxes
 
 

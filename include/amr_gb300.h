@@ -132,6 +132,13 @@ int amr_partition_morton(const uint32_t* positions, uint32_t used_slots, uint32_
 int amr_ghost_exchange_plan(const amr_config* cfg, const uint64_t* boundaries, const int32_t* owner,
                             uint32_t used_slots, uint32_t substep, uint32_t max_depth, uint32_t rank,
                             uint32_t* boxes, uint32_t capacity, uint32_t* n_boxes);
+/* The boxes that `rank` must receive before the restriction of `substep` (amr_copy_new_to_old;
+ * AMR.h:961-996): the interior (new field) of every child, owned by another rank, of an active
+ * domain that `rank` owns.  Same records, capacity and count rules as amr_ghost_exchange_plan;
+ * positions / children are the host octree arrays.  Host only. */
+int amr_restriction_exchange_plan(const amr_config* cfg, const uint32_t* positions, const int32_t* children,
+                                  const int32_t* owner, uint32_t used_slots, uint32_t substep, uint32_t max_depth,
+                                  uint32_t rank, uint32_t* boxes, uint32_t capacity, uint32_t* n_boxes);
 /* Copy the boxes of one padded field (used_slots domains) into `out` (box b, x fastest, at float
  * offset offsets[b]), or back from `in`.  boxes / offsets are device arrays; a record outside the
  * slot range or its cube is skipped. */

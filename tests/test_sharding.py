@@ -125,23 +125,31 @@ def _rank_main(rank: int, world: int, port: int, n: int, p: int, tree: str):
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     try:
         pos, bd, used, md = _tree(tree)
+        ch = np.load(os.path.join(GOLDEN, "host_golden.npz"))[f"tree/{tree}/children"]
         t = n + 2 * p
         cfg, oc = am.Config(n, p, OUTER), orc.cfg(n, p, OUTER)
         f_old, f_new = _fields(pos, used, n, p)
         owner = sharding.partition_morton(pos, used, world)
         mine = _owned_mask(owner, rank, t)
+        pack = lambda f, b: torch.from_numpy(_pack_host(f, b, t))                 # noqa: E731
+        unpack = lambda f, b, buf: _unpack_host(f, b, t, buf.numpy())            # noqa: E731
         for s in range(1 << md):
-            # this rank's state: its own domains only
+            # this rank's state: its own domains only; a substep's restriction, then its ghost fill
             lo = np.where(mine, f_old, np.nan).astype(np.float32)
             ln = np.where(mine, f_new, np.nan).astype(np.float32)
+            plans = [sharding.restriction_plan(cfg, pos, ch, owner, used, s, md, q) for q in range(world)]
+            sharding.exchange(dist, rank, world, plans, [ln], pack=pack, unpack=unpack)
+            orc.lib().orc_copy_new_to_old(ctypes.byref(oc), orc.P(lo), orc.P(ln), orc.P(pos), orc.P(ch), used, s, md)
             plans = [sharding.exchange_plan(cfg, bd, owner, used, s, md, q) for q in range(world)]
-            sharding.exchange(dist, rank, world, plans, [lo, ln],
-                              pack=lambda f, b: torch.from_numpy(_pack_host(f, b, t)),
-                              unpack=lambda f, b, buf: _unpack_host(f, b, t, buf.numpy()))
+            sharding.exchange(dist, rank, world, plans, [lo, ln], pack=pack, unpack=unpack)
             orc.lib().orc_copy_boundaries(ctypes.byref(oc), orc.P(lo), orc.P(ln), orc.P(bd), used, s, md, 0)
             full_old, full_new = f_old.copy(), f_new.copy()
+            orc.lib().orc_copy_new_to_old(ctypes.byref(oc), orc.P(full_old), orc.P(full_new), orc.P(pos), orc.P(ch),
+                                          used, s, md)
             orc.lib().orc_copy_boundaries(ctypes.byref(oc), orc.P(full_old), orc.P(full_new), orc.P(bd), used, s, md, 0)
-            sel = mine & cases.ghost_write_mask(bd, used, n, p, md, s)
+            depth = np.array([int(x) >> 27 if x != 0xFFFFFFFF else -1 for x in pos[:used]])
+            active = np.repeat(np.array([d >= 0 and (s & ((1 << (md - d)) - 1)) == 0 for d in depth]), t ** 3)
+            sel = mine & (cases.ghost_write_mask(bd, used, n, p, md, s) | active)
             assert np.array_equal(lo[sel].view(np.uint32), full_old[sel].view(np.uint32)), f"rank {rank} substep {s}"
             assert np.array_equal(ln[sel].view(np.uint32), full_new[sel].view(np.uint32)), f"rank {rank} substep {s}"
         dist.barrier()
@@ -151,5 +159,43 @@ def _rank_main(rank: int, world: int, port: int, n: int, p: int, tree: str):
 
 @pytest.mark.parametrize("world,n,p,tree", [(2, 16, 3, "bssn"), (3, 28, 2, "uneven")])
 def test_exchange_over_gloo(orc, world, n, p, tree):
+    """Each substep's two exchanges (children before the restriction, source boxes before the
+    ghost fill) over torch.distributed with gloo: every rank's own domains end as in the unsharded
+    substep."""
     import torch.multiprocessing as mp
     mp.spawn(_rank_main, args=(world, _free_port(), n, p, tree), nprocs=world, join=True)
+
+
+@pytest.mark.parametrize("n,p", [(16, 3), (28, 2)])
+@pytest.mark.parametrize("tree", ["bssn", "uneven", "uniform2"])
+@pytest.mark.parametrize("ranks", [2, 3, 5])
+def test_restriction_plan_brings_every_child(am, orc, n, p, tree, ranks):
+    """With only its own domains valid (the rest NaN), a rank that receives its restriction plan's
+    boxes restricts every active domain it owns exactly as the unsharded restriction does."""
+    from adaptivemesh_gb300 import sharding
+    hg = np.load(os.path.join(GOLDEN, "host_golden.npz"))
+    pos, _bd, used, md = _tree(tree)
+    ch = hg[f"tree/{tree}/children"]
+    t = n + 2 * p
+    cfg, oc = am.Config(n, p, OUTER), orc.cfg(n, p, OUTER)
+    f_old, f_new = _fields(pos, used, n, p)
+    owner = sharding.partition_morton(pos, used, ranks)
+    depth = np.array([int(x) >> 27 if x != 0xFFFFFFFF else -1 for x in pos[:used]])
+    received = 0
+    for s in range(1 << md):
+        full_old = f_old.copy()
+        orc.lib().orc_copy_new_to_old(ctypes.byref(oc), orc.P(full_old), orc.P(f_new), orc.P(pos), orc.P(ch), used, s, md)
+        for r in range(ranks):
+            boxes = sharding.restriction_plan(cfg, pos, ch, owner, used, s, md, r)
+            received += len(boxes)
+            assert all(owner[b[0]] == b[1] != r for b in boxes)
+            mine = _owned_mask(owner, r, t)
+            lo = np.where(mine, f_old, np.nan).astype(np.float32)
+            ln = np.where(mine, f_new, np.nan).astype(np.float32)
+            _unpack_host(ln, boxes, t, _pack_host(f_new, boxes, t))
+            orc.lib().orc_copy_new_to_old(ctypes.byref(oc), orc.P(lo), orc.P(ln), orc.P(pos), orc.P(ch), used, s, md)
+            active = np.array([d >= 0 and (s & ((1 << (md - d)) - 1)) == 0 for d in depth])
+            sel = np.repeat((owner == r) & active, t ** 3)
+            assert np.array_equal(lo[sel].view(np.uint32), full_old[sel].view(np.uint32)), f"substep {s} rank {r}"
+    if ranks > 1 and tree != "uniform2":
+        assert received > 0
