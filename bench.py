@@ -205,6 +205,15 @@ def reference_arm(args) -> None:
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
                              "sample": vals[0]["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    # For comparison only (not this arm's value): the reference's own CUDA plugin on this GPU, its
+    # headers compiled for sm_103a into the checker library, on the same workload
+    try:
+        import torch
+        if torch.cuda.is_available():
+            from oracle import time_reference_gpu
+            line["reference_gpu"] = time_reference_gpu.measure(N, P, args.depth, steps=10, warmup=2)
+    except Exception as e:  # no checker library for this size, or no reference headers staged
+        line["reference_gpu"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
     print(json.dumps(line))
 
 

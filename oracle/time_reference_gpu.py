@@ -30,20 +30,13 @@ import cases  # noqa: E402
 from oracle import reflib  # noqa: E402
 
 
-def main() -> None:
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--size", type=int, default=16)
-    ap.add_argument("--padding", type=int, default=3)
-    ap.add_argument("--depth", type=int, default=3)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
-    args = ap.parse_args()
+def measure(n: int, p: int, depth: int, steps: int, warmup: int) -> dict:
+    """zone-cycles/s of the reference's BSSN plugin on the uniform octree of `depth` (see above)."""
     import torch
-    n, p = args.size, args.padding
     lib = reflib.load(f"n{n}p{p}")
     k = reflib.constants(lib)
     assert (k["size_domain"], k["padding_domain"]) == (n, p), k
-    slots = sum(8 ** d for d in range(args.depth + 1))
+    slots = sum(8 ** d for d in range(depth + 1))
     h = lib.refd_bssn_create(slots)
 
     class _Tree:
@@ -53,7 +46,7 @@ def main() -> None:
         def state(self):
             return reflib.octree_state(lib.refd_bssn_octree_state, h, slots)
     tree = _Tree()
-    cases.tree_uniform(tree, args.depth)
+    cases.tree_uniform(tree, depth)
     st = tree.state()
     used, t = st["used_slots"], n + 2 * p
     xyz = cases.cell_coordinates(st["positions"], used, n, p, 100.0)
@@ -69,22 +62,33 @@ def main() -> None:
             dst = torch.as_tensor(_Dev(lib.refd_bssn_field(h, which, c), used * t ** 3), device="cuda")
             dst.copy_(torch.from_numpy(metric[c]).cuda())
     torch.cuda.synchronize()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         assert lib.refd_bssn_timestep(h) == 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         assert lib.refd_bssn_timestep(h) == 0
     torch.cuda.synchronize()
     sec = time.perf_counter() - t0
-    leaves = 8 ** args.depth
+    leaves = 8 ** depth
     zones = leaves * n ** 3
     lib.refd_bssn_destroy(h)
-    print(json.dumps({"metric": "BSSN zone-cycles/s", "value": zones * args.steps / sec, "unit": "zone-cycles/s",
-                      "ms_per_step": sec * 1e3 / args.steps, "steps": args.steps, "warmup": args.warmup,
-                      "impl": "reference CUDA plugin (BSSN_AMR_data::timestep), sm_103a",
-                      "workload": f"uniform depth-{args.depth} octree: {leaves} leaf + {used - leaves} parent "
-                                  f"domains of {n}^3, padding {p}"}))
+    return {"metric": "BSSN zone-cycles/s", "value": zones * steps / sec, "unit": "zone-cycles/s",
+            "ms_per_step": sec * 1e3 / steps, "steps": steps, "warmup": warmup,
+            "impl": "reference CUDA plugin (BSSN_AMR_data::timestep), sm_103a",
+            "workload": f"uniform depth-{depth} octree: {leaves} leaf + {used - leaves} parent domains of {n}^3, "
+                        f"padding {p}"}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--size", type=int, default=16)
+    ap.add_argument("--padding", type=int, default=3)
+    ap.add_argument("--depth", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    args = ap.parse_args()
+    print(json.dumps(measure(args.size, args.padding, args.depth, args.steps, args.warmup)))
 
 
 if __name__ == "__main__":
