@@ -509,3 +509,82 @@ def test_field_norms(am, cuda, cfgname, tree):
     d_f[s * t ** 3 + (p * t + p) * t + p + 1] = float("nan")
     assert np.isnan(am.ops.field_norms(cfg, d_f, d_pos, d_ch, used)["max_abs"])
     o.close()
+
+
+def assert_same_nan(a, b, what):
+    """assert_same, except that a NaN matches any NaN: the device returns one canonical NaN, the
+    host's arithmetic other payloads."""
+    a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    na, nb = np.isnan(a), np.isnan(b)
+    assert np.array_equal(na, nb), f"{what}: NaN at {np.count_nonzero(na != nb)} places of one side only"
+    assert_same(np.where(na, 0, a).astype(np.float32), np.where(nb, 0, b).astype(np.float32), what)
+
+
+@pytest.mark.parametrize("kind", ["zeros", "nonfinite", "huge"])
+def test_ghost_fill_special_values(am, cuda, orc, kind):
+    """Ghost fills with special values planted in the sources, bit for bit against the oracle
+    (NaN matching any NaN): the operator entry point (staged, both copy_only_new settings) and a
+    BSSN timestep (fill in place), on a uniform tree, where sources are at the same depth and the
+    interpolation offsets are 0 or 1: signed zeros ('zeros'), NaN and infinities ('nonfinite'),
+    and magnitudes from 2^125 up, whose interpolation overflows ('huge').  Subnormal inputs are
+    left out: the device flushes them (as the reference's fast-math build does) and the oracle
+    models the flush only in the codec."""
+    import torch
+    n, p = 16, 3
+    t = n + 2 * p
+    cfg, oc = am.Config(n, p, OUTER), orc.cfg(n, p, OUTER)
+    pool = {"zeros": [0.0, -0.0],
+            "nonfinite": [np.nan, np.inf, -np.inf],
+            "huge": [2.0 ** 125, -2.0 ** 125, 3e38, -1.5 * 2.0 ** 126]}[kind]
+    pool = np.array(pool, np.float32)
+    rng = np.random.default_rng(17)
+
+    def plant(a):
+        a = a.copy()
+        k = rng.choice(a.size, size=a.size // 400, replace=False)
+        a[k] = pool[rng.integers(0, pool.size, k.size)]
+        return a
+
+    o = am.Octree(80)
+    cases.tree_uniform(o, 2)
+    st = o.state()
+    used, md = st["used_slots"], st["max_depth"]
+    xyz = cases.cell_coordinates(st["positions"], used, n, p, OUTER)
+    f_old, f_new = plant(cases.smooth_field(xyz, OUTER, 1, 11)), plant(cases.smooth_field(xyz, OUTER, 1, 12))
+    bd = torch.from_numpy(st["boundaries"][: used * 6].view(np.int64)).cuda()
+    for s in range(1 << md):
+        for only_new in (1, 0):
+            go, gn = torch.from_numpy(f_old.copy()).cuda(), torch.from_numpy(f_new.copy()).cuda()
+            am.ops.copy_boundaries(cfg, go, gn, bd, used, s, md, copy_only_new=bool(only_new))
+            o_old, o_new = f_old.copy(), f_new.copy()
+            orc.lib().orc_copy_boundaries(ctypes.byref(oc), orc.P(o_old), orc.P(o_new), orc.P(st["boundaries"]),
+                                          used, s, md, only_new)
+            assert_same_nan(host(go), o_old, f"{kind} substep {s} copy_only_new {only_new}: old")
+            assert_same_nan(host(gn), o_new, f"{kind} substep {s} copy_only_new {only_new}: new")
+    o.close()
+    # a BSSN timestep, whose fill runs in place, with the specials in every component
+    sim = am.Sim(cfg, am.SIM_BSSN, slots=80, mode=am.MODE_BATCHED)
+    cases.tree_uniform(sim, 2)
+    sim.synchronize()
+    metric = [plant(m) for m in cases.metric_fields(xyz, OUTER, 300)]
+    for which in (am.Sim.OLD, am.Sim.NEW):
+        for k in range(6):
+            sim.tensor(which, k)[: used * t ** 3].copy_(torch.from_numpy(metric[k]).cuda())
+    torch.cuda.synchronize()
+    seed0 = sim.rng
+    sim.timestep()
+    sim.synchronize()
+    old6, new6 = [m.copy() for m in metric], [m.copy() for m in metric]
+    inner = used * n ** 3
+    dm = [np.zeros(inner, np.uint32) for _ in range(6)]
+    chr6 = [np.zeros(inner, np.uint32) for _ in range(6)]
+    ri = [np.zeros(inner, np.float32) for _ in range(6)]
+    timer, gen = ctypes.c_uint32(0), ctypes.c_int32(seed0)
+    orc.lib().orc_bssn_timestep(ctypes.byref(oc), orc.P(orc.ptrs(old6)), orc.P(orc.ptrs(new6)), orc.P(orc.ptrs(dm)),
+                                orc.P(orc.ptrs(chr6)), orc.P(orc.ptrs(ri)), orc.P(st["positions"]),
+                                orc.P(st["children"]), orc.P(st["boundaries"]), used, md, ctypes.byref(timer),
+                                ctypes.byref(gen), 0, used)
+    for k in range(6):
+        assert_same_nan(host(sim.tensor(am.Sim.OLD, k)[: used * t ** 3]), old6[k], f"{kind} timestep old{k}")
+        assert_same_nan(host(sim.tensor(am.Sim.NEW, k)[: used * t ** 3]), new6[k], f"{kind} timestep new{k}")
+    sim.close()
