@@ -518,3 +518,39 @@ def test_set_octree_refuses_bad_arrays(am, cuda):
             sim.set_octree(st)
     _assert_states_equal(sim.state(), good, "after refused uploads")
     sim.close()
+
+
+def test_checkpoint_between_phases(am, cuda, tmp_path):
+    """A checkpoint taken between the phases of a timestep (amr_sim_phase) resumes in another
+    simulation to the same state as the uninterrupted run, counter and generator included."""
+    import torch
+    cfg = am.Config(16, 3, 100.0)
+    phases = (am.PHASE_COPY_BACK, am.PHASE_MODIFY_NODES, am.PHASE_PREDICTOR, am.PHASE_COPY_BOUNDS,
+              am.PHASE_CORRECTOR, am.PHASE_INCREMENT_TIMER)
+    sim, _st, _ = _bssn_sim(am, cfg, "uneven", am.MODE_BATCHED)
+    sim.timestep()
+    for _ in range(3):             # three substeps of the next timestep ...
+        for ph in phases:
+            sim.phase(ph)
+    sim.phase(am.PHASE_COPY_BACK)  # ... and the first phase of the fourth
+    sim.synchronize()
+    assert sim.state()["timer"] == 3
+    sim.save_checkpoint(str(tmp_path))
+
+    def finish(s):
+        for ph in phases[1:]:
+            s.phase(ph)
+        while s.state()["timer"] != 0:
+            for ph in phases:
+                s.phase(ph)
+        s.timestep()
+        s.synchronize()
+    finish(sim)
+    want = _full_state(am, sim, am.SIM_BSSN)
+    sim.close()
+    resumed = am.Sim(cfg, am.SIM_BSSN, slots=128, mode=am.MODE_GRAPH)
+    resumed.load_checkpoint(str(tmp_path))
+    assert resumed.state()["timer"] == 3
+    finish(resumed)
+    _assert_states_equal(_full_state(am, resumed, am.SIM_BSSN), want, "resumed between phases")
+    resumed.close()
