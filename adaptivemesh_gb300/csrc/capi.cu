@@ -69,7 +69,11 @@ uint32_t stencil_grid(const amr_config& c, int kind, uint32_t n_items) {
     per_sm = per_sm < 2048u / threads ? per_sm : 2048u / threads;
     if (per_sm < 1) per_sm = 1;
     const uint32_t cap = per_sm * (uint32_t)sms;
-    return n_items < cap ? n_items : cap;
+    // few items: wider grids than one CTA per item.  The fused kind splits its planes evenly over
+    // the CTAs (at least 4 interior planes each); the others cut items into z-ranges.
+    const uint64_t want = kind == SK_BSSN ? ((uint64_t)n_items * c.size_domain + 3u) / 4u
+                                          : (uint64_t)n_items * (c.size_domain / 2u);
+    return want < cap ? (uint32_t)want : cap;
 }
 
 // Error flag of the current device, shared by the operator entry points and the simulations on

@@ -50,6 +50,9 @@ struct StencilArgs {
     const uint32_t* positions;    // octree_abs_pos per slot
     const uint32_t* items;        // domains to process (nullptr: item i is slot i)
     uint32_t n_items;
+    // single-operator kinds: with zsplit > 1 (a divisor of N), every item is cut into zsplit
+    // z-ranges, one work unit each (few items: spread over the grid); 0 or 1: whole items
+    uint32_t zsplit;
     uint32_t substep, max_depth;
     Geo geo;
     int* err;                     // set to 1 if a bounded wait gave up

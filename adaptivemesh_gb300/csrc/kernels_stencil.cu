@@ -290,12 +290,14 @@ __global__ void __launch_bounds__(N * N, N * N <= 256 ? 2 : 1) k_stencil(const _
     // cut into Q z-ranges of N/Q interior planes so that it spreads over every CTA.  A unit streams
     // its nz + 2P padded planes through the ring; thread 0 keeps the ring R planes ahead of the
     // plane being computed, across unit boundaries.
-    constexpr uint32_t Q = S::Q, NZQ = N / Q;
+    // With a.zsplit > 1 every item is cut that way instead (few items, launched on a wider grid).
     const uint32_t G = gridDim.x;
     const uint32_t rem = a.n_items % G;
-    const bool split = rem != 0u && Q * rem <= (Q - 1u) * G;
-    const uint32_t n_whole = split ? a.n_items - rem : a.n_items;
-    const uint32_t n_units = n_whole + (split ? rem * Q : 0u);
+    const bool all_split = a.zsplit > 1u;
+    const uint32_t Q = all_split ? a.zsplit : S::Q, NZQ = N / Q;
+    const bool split = all_split || (rem != 0u && Q * rem <= (Q - 1u) * G);
+    const uint32_t n_whole = all_split ? 0u : split ? a.n_items - rem : a.n_items;
+    const uint32_t n_units = n_whole + (all_split ? a.n_items * Q : split ? rem * Q : 0u);
     auto unit_of = [&](uint32_t u, uint32_t& item, uint32_t& z0, uint32_t& nz) {
         if (u < n_whole) { item = u; z0 = 0; nz = N; }
         else { const uint32_t v = u - n_whole; item = n_whole + v / Q; z0 = (v % Q) * NZQ; nz = NZQ; }
@@ -665,6 +667,19 @@ cudaError_t launch_stencil_t(const StencilArgs& a, uint32_t grid, cudaStream_t s
     const cudaError_t e = ensure_smem_limit(kernel, S::SMEM, configured);
     if (e != cudaSuccess) return e;
     if (grid == 0) return cudaSuccess;
+    if constexpr (KIND != SK_BSSN) {
+        // a grid wider than the items (few domains): cut each into the most z-ranges of at
+        // least two planes that the grid holds
+        if (a.n_items > 0u && grid > a.n_items) {
+            uint32_t q = 1;
+            for (uint32_t d = 2; d <= (uint32_t)N / 2u; d++)
+                if (N % d == 0 && (uint64_t)d * a.n_items <= grid) q = d;
+            StencilArgs b = a;
+            b.zsplit = q;
+            kernel<<<a.n_items * q, S::THREADS, S::SMEM, st>>>(b);
+            return cudaGetLastError();
+        }
+    }
     kernel<<<grid, S::THREADS, S::SMEM, st>>>(a);
     return cudaGetLastError();
 }

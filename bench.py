@@ -56,11 +56,11 @@ def build_tree(o, depth: int = DEPTH):
     cases.tree_uniform(o, depth)
 
 
-def leaf_zones(st) -> int:
+def leaf_zones(st, n: int | None = None) -> int:
     used = st["used_slots"]
     ch = st["children"][: used * 8].reshape(used, 8)
     leaves = sum(1 for i in range(used) if st["positions"][i] != 0xFFFFFFFF and (ch[i] == -1).all())
-    return leaves * N ** 3
+    return leaves * (n or N) ** 3
 
 
 class ClockSampler:
@@ -217,6 +217,45 @@ def reference_arm(args) -> None:
     print(json.dumps(line))
 
 
+def wave_line(args) -> None:
+    """SimpleWave (wave_AMR_data::timestep with its regridding) at 28^3, padding 2, from root + 8
+    children and a smooth seeded blob: each timestep timed alone between device synchronisations
+    (the plugin reads its criterion back to the host every substep), its leaf zones counted after
+    it.  The reference plugin's figure on the same run comes from its own headers built for this
+    GPU (the timing script beside the checker library)."""
+    import numpy as np
+    import torch
+    import adaptivemesh_gb300 as am
+    import cases
+    n, p = 28, 2
+    t = n + 2 * p
+    sim = am.Sim(am.Config(n, p, OUTER), am.SIM_WAVE, slots=128, mode=am.MODE_BATCHED)
+    xyz = cases.cell_coordinates(np.array([0], np.uint32), 1, n, p, OUTER)
+    f0 = cases.smooth_field(xyz, OUTER, 0, 77, noise=0.0) * np.float32(0.5)
+    for which in (am.Sim.OLD, am.Sim.NEW):
+        sim.tensor(which)[: t ** 3].copy_(torch.from_numpy(f0).cuda())
+    torch.cuda.synchronize()
+    for c in range(8):
+        sim.add_node(0, c)
+    sim.copy_bounds()
+    sec, zones = 0.0, 0
+    for i in range(args.warmup + args.steps):
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.timestep()
+        sim.synchronize()
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            sec += dt
+            zones += leaf_zones(sim.state(), n)
+    sim.close()
+    print(json.dumps({"metric": "SimpleWave zone-cycles/s", "value": zones / sec, "unit": UNIT, "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps,
+                      "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "SimpleWave with regridding from root + 8 children, 28^3 domains, "
+                                             "padding 2", "mode": "batched"}}))
+
+
 def main() -> None:
     global N, P
     ap = argparse.ArgumentParser()
@@ -230,8 +269,13 @@ def main() -> None:
     ap.add_argument("--depth", type=int, default=DEPTH, help="uniform octree depth (3 = the benchmark workload)")
     ap.add_argument("--size", type=int, default=N, help="size_domain (16 = the benchmark workload; 8, 16, 28, 32)")
     ap.add_argument("--padding", type=int, default=P, help="padding_domain (3 = the benchmark workload)")
+    ap.add_argument("--plugin", default="bssn", choices=["bssn", "wave"],
+                    help="wave: time the SimpleWave plugin instead (an extra line, not the benchmark)")
     args = ap.parse_args()
     N, P = args.size, args.padding
+    if args.plugin == "wave":
+        wave_line(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
         return
