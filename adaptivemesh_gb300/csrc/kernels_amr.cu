@@ -21,7 +21,7 @@ inline uint32_t blocks_for(uint64_t n) { return (uint32_t)((n + kBlock - 1) / kB
 // without children is a straight copy of its range (16-byte aligned: 128-bit loads and stores,
 // several in flight per thread); otherwise every cell covered by a child becomes the mean of the
 // child's 2x2x2 cells and the rest is copied.
-constexpr uint32_t kSlabs = 4;          // slabs per domain of a launch over all active domains
+constexpr uint32_t kSlabs = 4;          // slabs per domain of a launch over all active domains (at least)
 constexpr uint32_t kParentSlabs = 16;   // ... of a launch over domains with children only (gathers)
 template <int N, int P>
 __global__ void __launch_bounds__(kBlock) k_copy_new_to_old(const __grid_constant__ FieldSet f, const uint32_t* __restrict__ positions,
@@ -451,7 +451,14 @@ cudaError_t launch_copy_new_to_old(Dims d, const FieldSet& f, const uint32_t* po
                                    const uint32_t* items, uint32_t n_items, uint32_t substep, uint32_t max_depth,
                                    cudaStream_t st, bool parents_only) {
     if (n_items == 0 || f.ncomp == 0) return cudaSuccess;
-    const dim3 grid(n_items, (uint32_t)f.ncomp, parents_only ? kParentSlabs : kSlabs);
+    // few domains: more slabs per domain, up to about two CTAs per SM in all
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    uint32_t slabs = parents_only ? kParentSlabs : kSlabs;
+    const uint64_t per_slab = (uint64_t)n_items * (uint32_t)f.ncomp;
+    while (slabs < 64u && per_slab * slabs * 2u <= 2u * (uint64_t)(sms > 0 ? sms : 1)) slabs *= 2u;
+    const dim3 grid(n_items, (uint32_t)f.ncomp, slabs);
 #define AMR_RESTRICT(N, P) \
     if (d.n == N && d.p == P) { k_copy_new_to_old<N, P><<<grid, kBlock, 0, st>>>(f, positions, children, items, substep, max_depth); return cudaGetLastError(); }
     AMR_FOR_EACH_CONFIG(AMR_RESTRICT)
