@@ -157,16 +157,21 @@ __global__ void k_criterion_columns(Dims d, float outer_dx, const uint32_t* __re
     }
     crit[o] = cr;
 }
+// One warp per octant (8 per block of 256).  The reference takes the maximum of the octant's q x h
+// column values in order, starting from NaN (SimpleWave.h:117-139); the values are non-negative
+// or NaN and fmaxf skips NaN, so the maximum does not depend on the order: the lanes take strided
+// parts and combine them in a tree.
 __global__ void k_criterion_octants(Dims d, float* __restrict__ crit, uint32_t used) {
     const uint32_t n = d.n, h = n >> 1, q = n >> 2;
-    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= used * 8u) return;
+    const uint32_t idx = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31u;
+    if (idx >= used * 8u) return;   // uniform in the warp
     const uint32_t x = idx & 1u, y = (idx >> 1) & 1u, z = (idx >> 2) & 1u, node = idx >> 3;
     const uint64_t base = (uint64_t)node * n * n + z * (n * n >> 1) + y * (n * n >> 2) + x * h;
     float cr = __int_as_float(0x7fc00000);
-    for (uint32_t yy = 0; yy < q; yy++)
-        for (uint32_t xx = 0; xx < h; xx++) cr = fmaxf(cr, crit[base + xx + (uint64_t)yy * n]);
-    crit[base] = cr;
+    for (uint32_t e = lane; e < q * h; e += 32u) cr = fmaxf(cr, crit[base + e % h + (uint64_t)(e / h) * n]);
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) cr = fmaxf(cr, __shfl_xor_sync(0xFFFFFFFFu, cr, s));
+    if (lane == 0) crit[base] = cr;
 }
 
 
@@ -266,7 +271,7 @@ cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const ui
     k_criterion_columns<<<blocks_for(n), kBlock, 0, st>>>(d, g.outer_dx, der, hess, crit, positions, used, substep, max_depth);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_criterion_octants<<<blocks_for((uint64_t)used * 8u), kBlock, 0, st>>>(d, crit, used);
+    k_criterion_octants<<<(uint32_t)(((uint64_t)used * 8u + kBlock / 32u - 1u) / (kBlock / 32u)), kBlock, 0, st>>>(d, crit, used);
     return cudaGetLastError();
 }
 
