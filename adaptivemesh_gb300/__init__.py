@@ -103,6 +103,8 @@ EXPORTS = {
     "amr_sim_copy_to_host_side": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, VP, U64]),
     "amr_sim_stage_to_device": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, VP, U64]),
     "amr_sim_snapshot_to_host": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, VP, U64]),
+    "amr_sim_stage_many": (ctypes.c_int, [VP, U32, VP, VP, VP, VP]),
+    "amr_sim_snapshot_many": (ctypes.c_int, [VP, U32, VP, VP, VP, VP]),
     "amr_sim_event_record": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_event_elapsed": (ctypes.c_int, [VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "amr_sim_save": (ctypes.c_int, [VP, ctypes.c_char_p]),

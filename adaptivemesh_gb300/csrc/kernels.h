@@ -93,6 +93,17 @@ cudaError_t launch_rasterise(Dims d, const float* data, const int32_t* children,
 cudaError_t launch_store_words(int32_t* dst, const int32_t* words, uint32_t n, cudaStream_t st, uint32_t* launched);
 // Device-to-device copy of n 4-byte words (128-bit accesses where both addresses allow), one launch.
 cudaError_t launch_copy_words(void* dst, const void* src, uint64_t n, cudaStream_t st);
+// Up to kMax device-to-device copies of n 4-byte words in one launch (16-byte aligned buffers).
+struct CopyList {
+    static constexpr uint32_t kMax = 36;
+    struct Item {
+        void* dst;
+        const void* src;
+        uint64_t n;
+    } item[kMax];
+    uint32_t n = 0;
+};
+cudaError_t launch_copy_many(const CopyList& l, cudaStream_t st);
 cudaError_t launch_criterion(Dims d, const Geo& g, const uint32_t* der, const uint32_t* hess, float* crit,
                              const uint32_t* positions, uint32_t used, uint32_t substep, uint32_t max_depth,
                              cudaStream_t st);

@@ -353,4 +353,40 @@ cudaError_t launch_copy_words(void* dst, const void* src, uint64_t n, cudaStream
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- many copies in one launch
+namespace {
+// blockIdx.y: the copy; its CTAs stride over its 16-byte vectors, then its last n % 4 words
+__global__ void __launch_bounds__(kBlock) k_copy_many(const __grid_constant__ CopyList l) {
+    const CopyList::Item& it = l.item[blockIdx.y];
+    const uint64_t n4 = it.n / 4u;
+    const float4* __restrict__ s4 = static_cast<const float4*>(it.src);
+    float4* __restrict__ d4 = static_cast<float4*>(it.dst);
+    for (uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x; i < n4; i += (uint64_t)gridDim.x * kBlock)
+        __stcs(d4 + i, __ldcs(s4 + i));
+    if (blockIdx.x == 0 && threadIdx.x < (uint32_t)(it.n % 4u))
+        static_cast<float*>(it.dst)[n4 * 4u + threadIdx.x] = static_cast<const float*>(it.src)[n4 * 4u + threadIdx.x];
+}
+}  // namespace
+
+cudaError_t launch_copy_many(const CopyList& l, cudaStream_t st) {
+    if (l.n == 0) return cudaSuccess;
+    if (l.n > CopyList::kMax) return cudaErrorInvalidValue;
+    uint64_t most = 0;
+    for (uint32_t i = 0; i < l.n; i++) {
+        if ((reinterpret_cast<uintptr_t>(l.item[i].dst) | reinterpret_cast<uintptr_t>(l.item[i].src)) % 16u != 0u)
+            return cudaErrorInvalidValue;   // the callers' buffers are allocations: 256-byte aligned
+        most = l.item[i].n > most ? l.item[i].n : most;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+    // about 8 CTAs per SM in all, and no more per copy than its largest member's vectors need
+    uint64_t per = ((uint64_t)sms * 8u + l.n - 1u) / l.n;
+    const uint64_t need = (most / 4u + 4u * kBlock - 1u) / (4u * kBlock);
+    per = per < need ? per : need;
+    k_copy_many<<<dim3((uint32_t)(per < 1u ? 1u : per), l.n), kBlock, 0, st>>>(l);
+    return cudaGetLastError();
+}
+
 }  // namespace amr

@@ -908,6 +908,91 @@ AMR_API int amr_sim_snapshot_to_host(amr_sim* s, int which, int comp, void* host
     d.pending = true;
     return AMR_OK;
 }
+// The batched forms: the same transfers for up to 36 distinct buffers, with one copy launch on the
+// simulation's stream for all of them (host transfers stay one per buffer).
+static int check_many(SimBase* b, uint32_t n, const int* which, const int* comp, const void* const* host,
+                      const uint64_t* count, void** dev) {
+    if (n > CopyList::kMax || (n && (!which || !comp || !host || !count))) return AMR_ERR_INVALID;
+    for (uint32_t i = 0; i < n; i++) {
+        if (which[i] < 0 || which[i] >= 6 || comp[i] < 0 || comp[i] >= 6 || !host[i]) return AMR_ERR_INVALID;
+        for (uint32_t j = 0; j < i; j++)
+            if (which[j] == which[i] && comp[j] == comp[i]) return AMR_ERR_INVALID;   // one staging copy each
+        uint64_t cap = 0;
+        const int st = b->buffer(which[i], comp[i], &dev[i], &cap);
+        if (st) return st;
+        if (count[i] > cap) return AMR_ERR_INVALID;
+    }
+    return b->ensure_transfer_streams();
+}
+AMR_API int amr_sim_stage_many(amr_sim* s, uint32_t n, const int* which, const int* comp, const void* const* host,
+                               const uint64_t* count) {
+    if (!s) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    void* dev[CopyList::kMax];
+    int st = check_many(b, n, which, comp, host, count, dev);
+    if (st) return st;
+    CopyList list;
+    SimBase::Staging* last = nullptr;
+    cudaError_t e = cudaSuccess;
+    for (uint32_t i = 0; i < n && e == cudaSuccess; i++) {
+        if (count[i] == 0) continue;
+        SimBase::Staging& u = b->up[which[i]][comp[i]];
+        uint64_t cap = 0;
+        void* unused = nullptr;
+        if ((st = b->buffer(which[i], comp[i], &unused, &cap)) || (st = u.ensure(cap))) return st;
+        e = cudaStreamWaitEvent(b->up_stream, u.copied, 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(u.buf, host[i], count[i] * 4u, cudaMemcpyHostToDevice, b->up_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(u.moved, b->up_stream);
+        if ((st = b->wait_side(which[i], comp[i]))) return st;
+        list.item[list.n++] = {dev[i], u.buf, count[i]};
+        last = &u;
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+    if (!last) return AMR_OK;
+    // the upload stream runs in order: its last transfer done means all are
+    e = cudaStreamWaitEvent(b->stream, last->moved, 0);
+    if (e == cudaSuccess) e = launch_copy_many(list, b->stream);
+    b->launches++;
+    for (uint32_t i = 0; i < n && e == cudaSuccess; i++)
+        if (count[i]) e = cudaEventRecord(b->up[which[i]][comp[i]].copied, b->stream);
+    return cuda_status(e);
+}
+AMR_API int amr_sim_snapshot_many(amr_sim* s, uint32_t n, const int* which, const int* comp, void* const* host,
+                                  const uint64_t* count) {
+    if (!s) return AMR_ERR_INVALID;
+    SimBase* b = s->impl;
+    void* dev[CopyList::kMax];
+    int st = check_many(b, n, which, comp, const_cast<const void* const*>(host), count, dev);
+    if (st) return st;
+    CopyList list;
+    SimBase::Staging* first = nullptr;
+    cudaError_t e = cudaSuccess;
+    for (uint32_t i = 0; i < n && e == cudaSuccess; i++) {
+        if (count[i] == 0) continue;
+        SimBase::Staging& d = b->down[which[i]][comp[i]];
+        uint64_t cap = 0;
+        void* unused = nullptr;
+        if ((st = b->buffer(which[i], comp[i], &unused, &cap)) || (st = d.ensure(cap))) return st;
+        if (d.pending) e = cudaStreamWaitEvent(b->stream, d.moved, 0);   // the previous snapshot has left
+        list.item[list.n++] = {d.buf, dev[i], count[i]};
+        if (!first) first = &d;
+    }
+    if (e != cudaSuccess) return cuda_status(e);
+    if (!first) return AMR_OK;
+    e = launch_copy_many(list, b->stream);
+    b->launches++;
+    for (uint32_t i = 0; i < n && e == cudaSuccess; i++)
+        if (count[i]) e = cudaEventRecord(b->down[which[i]][comp[i]].copied, b->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->down_stream, first->copied, 0);
+    for (uint32_t i = 0; i < n && e == cudaSuccess; i++) {
+        if (count[i] == 0) continue;
+        SimBase::Staging& d = b->down[which[i]][comp[i]];
+        e = cudaMemcpyAsync(host[i], d.buf, count[i] * 4u, cudaMemcpyDeviceToHost, b->down_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(d.moved, b->down_stream);
+        if (e == cudaSuccess) d.pending = true;
+    }
+    return cuda_status(e);
+}
 AMR_API int amr_sim_copy_to_device(amr_sim* s, int which, int comp, const void* host, uint64_t count) {
     return sim_copy(s, which, comp, const_cast<void*>(host), count, true);
 }

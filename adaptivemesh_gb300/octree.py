@@ -171,6 +171,31 @@ class Sim:
         addr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
         check(load().amr_sim_snapshot_to_host(self.h, which, comp, addr, n), "amr_sim_snapshot_to_host")
 
+    @staticmethod
+    def _many(items):
+        n = len(items)
+        which = np.array([it[0] for it in items], np.int32)
+        comp = np.array([it[1] for it in items], np.int32)
+        addr = (ctypes.c_void_p * max(n, 1))(*[it[2].data_ptr() if hasattr(it[2], "data_ptr") else it[2].ctypes.data
+                                                for it in items])
+        count = np.array([it[3] if len(it) > 3 else (it[2].numel() if hasattr(it[2], "numel") else it[2].size)
+                          for it in items], np.uint64)
+        return n, which, comp, addr, count
+
+    def stage_many(self, items) -> None:
+        """stage_to_device for several distinct buffers, [(which, comp, host[, count])], with one
+        copy launch for all (amr_sim_stage_many)."""
+        n, which, comp, addr, count = self._many(items)
+        check(load().amr_sim_stage_many(self.h, n, which.ctypes.data, comp.ctypes.data, ctypes.addressof(addr),
+                                        count.ctypes.data), "amr_sim_stage_many")
+
+    def snapshot_many(self, items) -> None:
+        """snapshot_to_host for several distinct buffers, [(which, comp, host[, count])], with one
+        copy launch for all (amr_sim_snapshot_many)."""
+        n, which, comp, addr, count = self._many(items)
+        check(load().amr_sim_snapshot_many(self.h, n, which.ctypes.data, comp.ctypes.data, ctypes.addressof(addr),
+                                           count.ctypes.data), "amr_sim_snapshot_many")
+
     def event_record(self, slot: int) -> None:
         check(load().amr_sim_event_record(self.h, slot), "amr_sim_event_record")
 

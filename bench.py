@@ -321,15 +321,14 @@ def main() -> None:
     d2h = sum(t.numel() * 4 for t in h_out)
 
     def upload():
-        # host -> staging at once (overlapping the work enqueued so far), staging -> buffer on the
-        # simulation's stream after that work
-        for (w, k), h in zip(ins, h_in):
-            sim.stage_to_device(w, k, h)
+        # host -> staging at once (overlapping the work enqueued so far), staging -> buffers on the
+        # simulation's stream after that work, one copy launch for all
+        sim.stage_many([(w, k, h) for (w, k), h in zip(ins, h_in)])
 
     def download():
-        # buffer -> staging on the simulation's stream, staging -> host overlapping later work
-        for (w, k, n), h in zip(outs, h_out):
-            sim.snapshot_to_host(w, k, h)
+        # buffers -> staging on the simulation's stream (one launch), staging -> host overlapping
+        # later work
+        sim.snapshot_many([(w, k, h) for (w, k, n), h in zip(outs, h_out)])
 
     upload()
     sim.synchronize()

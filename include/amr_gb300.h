@@ -247,6 +247,13 @@ int amr_sim_copy_to_host_side(amr_sim* sim, int which, int comp, void* host, uin
  * completed. */
 int amr_sim_stage_to_device(amr_sim* sim, int which, int comp, const void* host, uint64_t count);
 int amr_sim_snapshot_to_host(amr_sim* sim, int which, int comp, void* host, uint64_t count);
+/* The same transfers for n (at most 36) distinct buffers at once: arrays of (which, comp, host,
+ * count).  The device-to-device copies of all of them are one launch on the simulation's stream;
+ * the host transfers are one per buffer on the transfer stream.  Results equal n single calls. */
+int amr_sim_stage_many(amr_sim* sim, uint32_t n, const int* which, const int* comp, const void* const* host,
+                       const uint64_t* count);
+int amr_sim_snapshot_many(amr_sim* sim, uint32_t n, const int* which, const int* comp, void* const* host,
+                          const uint64_t* count);
 /* Checkpoint of a simulation into the existing directory `dir`: the octree arrays
  * (positions.bin, parent.bin, children.bin, boundaries.bin, lifetime.bin), every field buffer
  * amr_sim_buffer names (field_<which>_<comp>.bin), each the raw little-endian bytes of the whole

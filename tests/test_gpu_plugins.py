@@ -395,6 +395,23 @@ def test_staged_transfers_match_plain_copies(am, cuda):
             for k in range(6):
                 _same(got[i][o][k].numpy(), want[i][o][k].numpy(), f"step {i} buffer {w} comp {k}: staged vs plain")
     _same(part[1:n_in - 2].numpy(), want[-1][2][5][:n_in - 3].numpy(), "partial snapshot")
+    # the batched forms: one copy launch per direction and step
+    batched, _, _ = _bssn_sim(am, cfg, "uneven", am.MODE_GRAPH)
+    got2 = [[[torch.empty(n, dtype=dt, pin_memory=True) for _ in range(6)] for (_, n, dt) in outs] for _ in range(steps)]
+    batched.stage_many([(am.Sim.NEW, k, inputs[0][k]) for k in range(6)])
+    for i in range(steps):
+        batched.timestep()
+        batched.snapshot_many([(w, k, got2[i][o][k]) for o, (w, _, _) in enumerate(outs) for k in range(6)])
+        if i + 1 < steps:
+            batched.stage_many([(am.Sim.NEW, k, inputs[i + 1][k]) for k in range(6)])
+    batched.synchronize()
+    for i in range(steps):
+        for o, (w, _, _) in enumerate(outs):
+            for k in range(6):
+                _same(got2[i][o][k].numpy(), want[i][o][k].numpy(), f"step {i} buffer {w} comp {k}: batched vs plain")
+    with pytest.raises(am.AmrError):   # one staging copy per buffer: no buffer twice in a batch
+        batched.snapshot_many([(am.Sim.CHR, 0, got2[0][2][0]), (am.Sim.CHR, 0, got2[0][2][1])])
+    batched.close()
     assert int(part[0]) == 0 and int(part[n_in - 2]) == 0 and int(part[n_in]) == 0, "snapshot wrote outside its count"
     plain.close()
     staged.close()
