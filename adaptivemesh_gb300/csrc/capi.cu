@@ -1,5 +1,6 @@
 // capi.cu -- extern "C" operator entry points and octree bindings (include/amr_gb300.h).
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -70,8 +71,12 @@ uint32_t stencil_grid(const amr_config& c, int kind, uint32_t n_items) {
     if (per_sm < 1) per_sm = 1;
     const uint32_t cap = per_sm * (uint32_t)sms;
     // few items: wider grids than one CTA per item.  The fused kind splits its planes evenly over
-    // the CTAs (at least 4 interior planes each); the others cut items into z-ranges.
-    const uint64_t want = kind == SK_BSSN ? ((uint64_t)n_items * c.size_domain + 3u) / 4u
+    // the CTAs: at least 4 interior planes each (each CTA also streams 2p halo planes), unless
+    // that leaves SMs idle, then one CTA per SM down to one plane each.  The others cut items
+    // into z-ranges.
+    const uint64_t planes = (uint64_t)n_items * c.size_domain;
+    const uint64_t one_per_sm = planes < (uint64_t)sms ? planes : (uint64_t)sms;
+    const uint64_t want = kind == SK_BSSN ? std::max((planes + 3u) / 4u, one_per_sm)
                                           : (uint64_t)n_items * (c.size_domain / 2u);
     return want < cap ? (uint32_t)want : cap;
 }
