@@ -22,7 +22,7 @@ from . import build as _build
 LIB_PATH = _build.LIB
 
 OK = 0
-ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_DEVICE, ERR_CAPACITY = 1, 2, 3, 4, 5
+ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_DEVICE, ERR_CAPACITY, ERR_TIMEOUT = 1, 2, 3, 4, 5, 6
 SIM_BSSN, SIM_WAVE = 1, 2
 DTYPE_UINT32, DTYPE_INT32, DTYPE_FLOAT32 = 0, 1, 2
 MODE_PLAIN, MODE_BATCHED, MODE_GRAPH = 0, 1, 2
@@ -61,6 +61,7 @@ EXPORTS = {
     "amr_config_supported": (ctypes.c_int, [CP]),
     "amr_last_cuda_error": (ctypes.c_int, []),
     "amr_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "amr_device_status": (ctypes.c_int, [VP]),
     "amr_cf3_encode": (ctypes.c_int, [VP, VP, U64, VP, VP]),
     "amr_cf3_decode": (ctypes.c_int, [VP, U64, VP, VP]),
     "amr_differentiate": (ctypes.c_int, [CP, VP, VP, VP, VP, U32, U32, U32, I32, VP]),
@@ -118,6 +119,8 @@ EXPORTS = {
     "amr_sim_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
     "amr_sim_synchronize": (ctypes.c_int, [VP]),
     "amr_sim_kernel_launches": (U64, [VP]),
+    "amr_sim_set_stencil_ctas": (ctypes.c_int, [VP, U32]),
+    "amr_sim_set_fault_injection": (ctypes.c_int, [VP, U32, U32]),
     "amr_sim_enable_kernel_timing": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_kernel_timing": (ctypes.c_int, [VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(U64)]),
     "amr_inclusive_scan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP]),

@@ -99,6 +99,17 @@ int* device_error_flag() {
     return flag[dev];
 }
 
+// Read the device error flag and clear it (the caller has synchronised the work that may set
+// it): AMR_ERR_TIMEOUT if a bounded wait gave up since the last read.
+int take_device_error(int* flag) {
+    if (!flag) return AMR_ERR_CUDA;
+    int h = 0;
+    cudaError_t e = cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && h) e = cudaMemset(flag, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_status(e);
+    return h ? AMR_ERR_TIMEOUT : AMR_OK;
+}
+
 }  // namespace amr
 
 using namespace amr;
@@ -120,8 +131,15 @@ AMR_API const char* amr_status_string(int s) {
         case AMR_ERR_CUDA: return "CUDA runtime error";
         case AMR_ERR_NO_DEVICE: return "no CUDA device";
         case AMR_ERR_CAPACITY: return "capacity exceeded";
+        case AMR_ERR_TIMEOUT: return "a kernel's bounded wait gave up (its results are invalid)";
         default: return "unknown status";
     }
+}
+
+AMR_API int amr_device_status(void* stream) {
+    const cudaError_t e = cudaStreamSynchronize(S(stream));
+    if (e != cudaSuccess) return cuda_status(e);
+    return take_device_error(device_error_flag());
 }
 
 AMR_API int amr_cf3_encode(const float* xyz, const int32_t* seeds, uint64_t n, uint32_t* out, void* stream) {

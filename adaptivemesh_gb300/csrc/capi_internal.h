@@ -16,6 +16,7 @@ bool bssn_fused_supported(const amr_config* c);
 cudaError_t launch_stencil(const amr_config& c, int kind, const StencilArgs& a, uint32_t grid, cudaStream_t st);
 uint32_t stencil_grid(const amr_config& c, int kind, uint32_t n_items);
 int* device_error_flag();
+int take_device_error(int* flag);
 int octree_state_impl(const Octree& t, uint32_t* positions, int32_t* parent, int32_t* children, uint64_t* boundaries,
                       uint32_t* lifetime, uint32_t* scalars);
 

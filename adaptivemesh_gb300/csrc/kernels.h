@@ -61,6 +61,12 @@ struct StencilArgs {
     // AMR.h:961-996), while a domain with children reads field[k] (restricted beforehand).
     const float* leaf_src[6];
     const int32_t* children;
+    // Failure-path test hooks of the fused pass (SK_BSSN), host-set, off when 0: spin_limit
+    // replaces the polls a data wait may take before it gives up (kMaxSpins); with withhold = q + 1
+    // the producer of every CTA skips its q-th plane request, so the waits on that plane run out.
+    // Waits for copies already issued (the drain before a CTA leaves) always use kMaxSpins.
+    uint32_t spin_limit;
+    uint32_t withhold;
 };
 
 template <int N, int P, int KIND>

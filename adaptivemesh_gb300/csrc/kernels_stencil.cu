@@ -544,6 +544,7 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, StencilS
         return leaf;
     };
 
+    const uint32_t spins = a.spin_limit ? a.spin_limit : kMaxSpins;
     if (warp == CW) {   // ---------------- producer warp: one thread requests every plane
         if (lane != 0) return;
         uint32_t q = 0;   // planes requested
@@ -558,8 +559,9 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, StencilS
             for (uint32_t j = 0; j < nz + 2u * P; j++, q++) {
                 const uint32_t s = q % R;
                 // the slot's previous plane (q - R) must have been released by every compute warp
-                if (q >= (uint32_t)R && !mbar_wait(&empty[s], ((q / R) - 1u) & 1u)) { ok = false; break; }
+                if (q >= (uint32_t)R && !mbar_wait(&empty[s], ((q / R) - 1u) & 1u, spins)) { ok = false; break; }
                 if (s_abort) { ok = false; break; }
+                if (q + 1u == a.withhold) continue;   // failure-path test: this plane never arrives
                 mbar_arrive_expect_tx(&full[s], NC * S::TILE_BYTES);
 #pragma unroll
                 for (int k = 0; k < NC; k++)
@@ -567,11 +569,15 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, StencilS
                              S::TILE_BYTES, &full[s]);
             }
         }
-        if (!ok) {   // abort: let the copies in flight land before the CTA's shared memory goes
+        if (!ok) {
             s_abort = 1;
             atomicExch(a.err, 1);
-            for (uint32_t p = q > (uint32_t)R ? q - R : 0u; p < q; p++) mbar_wait(&full[p % R], (p / R) & 1u);
         }
+        // The CTA's shared memory must outlive every copy issued into it: wait for the last R
+        // requests to land (the earlier ones were consumed before their slots were reused).  In a
+        // normal run they land anyway; after an abort, compute warps may have left without them.
+        for (uint32_t p = q > (uint32_t)R ? q - R : 0u; p < q; p++)
+            if (p + 1u != a.withhold) mbar_wait(&full[p % R], (p / R) & 1u);
         return;
     }
 
@@ -609,7 +615,7 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, StencilS
             bool ok = true;
             for (int j = zl == 0 ? 0 : 2 * P; j <= 2 * P; j++) {   // a unit's first window needs all
                 const uint32_t sq = g + j;
-                ok &= mbar_wait(&full[sq % R], (sq / R) & 1u);
+                ok &= mbar_wait(&full[sq % R], (sq / R) & 1u, spins);
             }
             if (!ok) s_abort = 1;
             if (s_abort) { bulk_wait(); return; }

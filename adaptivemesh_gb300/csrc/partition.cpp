@@ -84,7 +84,9 @@ int amr_ghost_exchange_plan(const amr_config* cfg, const uint64_t* boundaries, c
             const int32_t target = (int32_t)((nd & 16777215u) | ((nd & (1u << 23)) ? 4278190080u : 0u));
             const int cd = (nd >> 28) == 15u ? -1 : (int)(nd >> 28);
             const uint32_t dd = (nd >> 24) & 15u;
-            if (target == -1 || cd <= 0 || (substep & ((1u << (max_depth - (uint32_t)cd)) - 1u)) != 0u) continue;
+            if (target == -1 || cd <= 0) continue;
+            if (cd > (int)max_depth) return AMR_ERR_INVALID;   // a record deeper than the tree
+            if ((substep & ((1u << (max_depth - (uint32_t)cd)) - 1u)) != 0u) continue;
             if ((uint32_t)target >= used_slots) return AMR_ERR_INVALID;
             const int32_t src_rank = owner[target];
             if (src_rank == (int32_t)rank) continue;

@@ -333,6 +333,19 @@ public:
     }
     double timed_ms = 0.0;
     uint64_t timed_launches = 0;
+
+    // CTAs of the fused BSSN pass: fixed by amr_sim_set_stencil_ctas (0: automatic), else the
+    // autotuned choice for this domain count, else the library's rule (stencil_grid).
+    uint32_t stencil_ctas = 0;
+    // failure-path test hooks of the fused pass (amr_sim_set_fault_injection; StencilArgs)
+    uint32_t fault_spin_limit = 0, fault_withhold = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> tuned_ctas;   // (active domains, CTAs)
+    uint32_t fused_grid(uint32_t n_items) const {
+        if (stencil_ctas) return stencil_ctas;
+        for (const auto& t : tuned_ctas)
+            if (t.first == n_items) return t.second;
+        return stencil_grid(cfg, SK_BSSN, n_items);
+    }
 };
 
 // ============================================================================ BSSN
@@ -510,8 +523,10 @@ private:
             a.children = d_children;
             for (int k = 0; k < 6; k++) a.leaf_src[k] = new6[k];
         }
+        a.spin_limit = fault_spin_limit;
+        a.withhold = fault_withhold;
         time_begin();
-        st = check(launch_stencil(cfg, SK_BSSN, a, stencil_grid(cfg, SK_BSSN, a.n_items), stream));
+        st = check(launch_stencil(cfg, SK_BSSN, a, fused_grid(a.n_items), stream));
         time_end();
         return st;
     }
@@ -931,19 +946,25 @@ AMR_API int amr_sim_stage_many(amr_sim* s, uint32_t n, const int* which, const i
     void* dev[CopyList::kMax];
     int st = check_many(b, n, which, comp, host, count, dev);
     if (st) return st;
+    // every staging allocation and every wait on a side read first: an error return then means
+    // that nothing was queued
+    for (uint32_t i = 0; i < n; i++) {
+        if (count[i] == 0) continue;
+        uint64_t cap = 0;
+        void* unused = nullptr;
+        if ((st = b->buffer(which[i], comp[i], &unused, &cap)) || (st = b->up[which[i]][comp[i]].ensure(cap)) ||
+            (st = b->wait_side(which[i], comp[i])))
+            return st;
+    }
     CopyList list;
     SimBase::Staging* last = nullptr;
     cudaError_t e = cudaSuccess;
     for (uint32_t i = 0; i < n && e == cudaSuccess; i++) {
         if (count[i] == 0) continue;
         SimBase::Staging& u = b->up[which[i]][comp[i]];
-        uint64_t cap = 0;
-        void* unused = nullptr;
-        if ((st = b->buffer(which[i], comp[i], &unused, &cap)) || (st = u.ensure(cap))) return st;
         e = cudaStreamWaitEvent(b->up_stream, u.copied, 0);
         if (e == cudaSuccess) e = cudaMemcpyAsync(u.buf, host[i], count[i] * 4u, cudaMemcpyHostToDevice, b->up_stream);
         if (e == cudaSuccess) e = cudaEventRecord(u.moved, b->up_stream);
-        if ((st = b->wait_side(which[i], comp[i]))) return st;
         list.item[list.n++] = {dev[i], u.buf, count[i]};
         last = &u;
     }
@@ -964,15 +985,18 @@ AMR_API int amr_sim_snapshot_many(amr_sim* s, uint32_t n, const int* which, cons
     void* dev[CopyList::kMax];
     int st = check_many(b, n, which, comp, const_cast<const void* const*>(host), count, dev);
     if (st) return st;
+    for (uint32_t i = 0; i < n; i++) {   // staging allocations first: an error then queues nothing
+        if (count[i] == 0) continue;
+        uint64_t cap = 0;
+        void* unused = nullptr;
+        if ((st = b->buffer(which[i], comp[i], &unused, &cap)) || (st = b->down[which[i]][comp[i]].ensure(cap))) return st;
+    }
     CopyList list;
     SimBase::Staging* first = nullptr;
     cudaError_t e = cudaSuccess;
     for (uint32_t i = 0; i < n && e == cudaSuccess; i++) {
         if (count[i] == 0) continue;
         SimBase::Staging& d = b->down[which[i]][comp[i]];
-        uint64_t cap = 0;
-        void* unused = nullptr;
-        if ((st = b->buffer(which[i], comp[i], &unused, &cap)) || (st = d.ensure(cap))) return st;
         if (d.pending) e = cudaStreamWaitEvent(b->stream, d.moved, 0);   // the previous snapshot has left
         list.item[list.n++] = {d.buf, dev[i], count[i]};
         if (!first) first = &d;
@@ -1080,18 +1104,31 @@ AMR_API int amr_sim_save(amr_sim* s, const char* dir) {
     return AMR_OK;
 }
 
-// The device kernels index with these arrays: parents, children and boundary targets must name
-// slots, and positions must be free or no deeper than the depth limit.
-static bool octree_arrays_valid(uint32_t slots, const uint32_t* pos, const int32_t* par, const int32_t* ch,
-                                const uint64_t* bd) {
-    for (uint32_t i = 0; i < slots; i++)
-        if (pos_depth_host(pos[i]) > (int)kDepthLimit || par[i] < -1 || par[i] >= (int32_t)slots) return false;
+// The device kernels index with these arrays and shift by (max_depth - depth): parents, children
+// and boundary targets must name slots, the counter must lie in 0 .. 2^max_depth - 1, and every
+// live node, and every boundary record of a live node, must be no deeper than max_depth (itself at
+// most the depth limit).
+static bool octree_state_valid(uint32_t slots, const uint32_t* pos, const int32_t* par, const int32_t* ch,
+                               const uint64_t* bd, uint32_t timer, uint32_t max_depth, uint32_t first_free,
+                               uint32_t used) {
+    if (max_depth > kDepthLimit || timer >= (1u << max_depth) || first_free > slots || used == 0u || used > slots)
+        return false;
+    for (uint32_t i = 0; i < slots; i++) {
+        const int d = pos_depth_host(pos[i]);
+        if (d > (int)max_depth || par[i] < -1 || par[i] >= (int32_t)slots) return false;
+    }
     for (size_t i = 0; i < (size_t)slots * 8u; i++)
         if (ch[i] < -1 || ch[i] >= (int32_t)slots) return false;
     for (size_t i = 0; i < (size_t)slots * 6u; i++) {
         const uint32_t nd = (uint32_t)bd[i];
         const int32_t target = (int32_t)((nd & 16777215u) | ((nd & (1u << 23)) ? 4278190080u : 0u));
         if (target < -1 || target >= (int32_t)slots) return false;
+        // a record in use (a live node's, with a target) carries the node's depth in bits 28..31
+        // and the depth difference to its target in bits 24..27
+        if (target != -1 && pos_depth_host(pos[i / 6u]) != -1) {
+            const uint32_t depth = nd >> 28, diff = (nd >> 24) & 15u;
+            if (depth > max_depth || diff > depth) return false;
+        }
     }
     return true;
 }
@@ -1102,8 +1139,8 @@ AMR_API int amr_sim_set_octree(amr_sim* s, const uint32_t* positions, const int3
     SimBase* b = s->impl;
     const uint32_t slots = b->tree.max_slots();
     const uint32_t timer = scalars5[0], max_depth = scalars5[1], first_free = scalars5[2], used = scalars5[3];
-    if (scalars5[4] != slots || max_depth > kDepthLimit || timer >= (1u << max_depth) || first_free > slots ||
-        used == 0u || used > slots || !octree_arrays_valid(slots, positions, parent, children, boundaries))
+    if (scalars5[4] != slots ||
+        !octree_state_valid(slots, positions, parent, children, boundaries, timer, max_depth, first_free, used))
         return AMR_ERR_INVALID;
     int st = b->wait_side(-1, 0);   // side reads of the old tree's domains finish first
     if (st) return st;
@@ -1153,19 +1190,27 @@ AMR_API int amr_sim_load(amr_sim* s, const char* dir) {
         !read_file(d + "/boundaries.bin", bd.data(), (size_t)slots * 48u) ||
         !read_file(d + "/lifetime.bin", life.data(), slots * 4u))
         return AMR_ERR_INVALID;
-    if (!octree_arrays_valid(slots, pos.data(), par.data(), ch.data(), bd.data())) return AMR_ERR_INVALID;
-    std::vector<uint8_t> host;
+    if (!octree_state_valid(slots, pos.data(), par.data(), ch.data(), bd.data(), words[7], words[8], words[9],
+                            words[10] + 1u))
+        return AMR_ERR_INVALID;
+    // every field file is read and size-checked before anything is uploaded, so that a missing or
+    // truncated file leaves the simulation as it was
+    std::vector<std::vector<uint8_t>> fields;
+    std::vector<void*> targets;
     for (int which = 0; which < 6; which++)
         for (int comp = 0; comp < 6; comp++) {
             void* ptr = nullptr;
             uint64_t count = 0;
             if (b->buffer(which, comp, &ptr, &count) != AMR_OK) continue;
-            host.resize(count * 4u);
-            if (!read_file(d + "/field_" + std::to_string(which) + "_" + std::to_string(comp) + ".bin", host.data(),
-                           host.size()))
+            fields.emplace_back(count * 4u);
+            if (!read_file(d + "/field_" + std::to_string(which) + "_" + std::to_string(comp) + ".bin",
+                           fields.back().data(), fields.back().size()))
                 return AMR_ERR_INVALID;
-            if ((st = cuda_status(cudaMemcpy(ptr, host.data(), count * 4u, cudaMemcpyHostToDevice)))) return st;
+            targets.push_back(ptr);
         }
+    for (size_t i = 0; i < fields.size(); i++)
+        if ((st = cuda_status(cudaMemcpy(targets[i], fields[i].data(), fields[i].size(), cudaMemcpyHostToDevice))))
+            return st;
     b->tree.restore(pos.data(), par.data(), ch.data(), bd.data(), life.data(), words[7], (int)words[8], words[9],
                     words[10]);
     b->rng = (int32_t)words[11];
@@ -1204,11 +1249,22 @@ AMR_API int amr_sim_synchronize(amr_sim* s) {
     if (st) return st;
     st = cuda_status(cudaStreamSynchronize(s->impl->stream));
     if (st) return st;
-    int h = 0;
-    if (cudaMemcpy(&h, s->impl->err_flag, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return AMR_ERR_CUDA;
-    return h ? AMR_ERR_CUDA : AMR_OK;
+    return take_device_error(s->impl->err_flag);
+}
+AMR_API int amr_sim_set_fault_injection(amr_sim* s, uint32_t spin_limit, uint32_t withhold_plane) {
+    if (!s) return AMR_ERR_INVALID;
+    s->impl->fault_spin_limit = spin_limit;
+    s->impl->fault_withhold = withhold_plane;
+    s->impl->graph_valid = false;
+    return AMR_OK;
 }
 AMR_API uint64_t amr_sim_kernel_launches(const amr_sim* s) { return s ? s->impl->launches : 0u; }
+AMR_API int amr_sim_set_stencil_ctas(amr_sim* s, uint32_t ctas) {
+    if (!s || ctas > (1u << 20)) return AMR_ERR_INVALID;
+    s->impl->stencil_ctas = ctas;
+    s->impl->graph_valid = false;
+    return AMR_OK;
+}
 AMR_API int amr_sim_enable_kernel_timing(amr_sim* s, int enable) {
     if (!s) return AMR_ERR_INVALID;
     if (enable && s->impl->mode == AMR_MODE_GRAPH) return AMR_ERR_INVALID;

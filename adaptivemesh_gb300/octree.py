@@ -241,6 +241,14 @@ class Sim:
     def kernel_launches(self) -> int:
         return int(load().amr_sim_kernel_launches(self.h))
 
+    def set_stencil_ctas(self, ctas: int) -> None:
+        """CTAs of the fused BSSN derivative pass (0: the library's choice)."""
+        check(load().amr_sim_set_stencil_ctas(self.h, ctas), "amr_sim_set_stencil_ctas")
+
+    def set_fault_injection(self, spin_limit: int = 0, withhold_plane: int = 0) -> None:
+        """Failure-path test hook of the fused pass (amr_sim_set_fault_injection); (0, 0) is off."""
+        check(load().amr_sim_set_fault_injection(self.h, spin_limit, withhold_plane), "amr_sim_set_fault_injection")
+
     def enable_kernel_timing(self, enable: bool = True) -> None:
         check(load().amr_sim_enable_kernel_timing(self.h, 1 if enable else 0), "amr_sim_enable_kernel_timing")
 

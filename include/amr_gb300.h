@@ -33,6 +33,7 @@ extern "C" {
 #define AMR_ERR_CUDA 3              /* a CUDA runtime call failed; see amr_last_cuda_error() */
 #define AMR_ERR_NO_DEVICE 4         /* no CUDA device is visible */
 #define AMR_ERR_CAPACITY 5          /* node slots exhausted or a fixed-size buffer is too small */
+#define AMR_ERR_TIMEOUT 6           /* a kernel's bounded wait gave up; that work's results are invalid */
 
 /* Domain configuration: the reference's compile-time constants (AMR.h:9-20) as run-time values. */
 typedef struct amr_config {
@@ -54,6 +55,12 @@ int amr_config_supported(const amr_config* cfg);
 int amr_last_cuda_error(void);
 /* Human-readable text for a status code. */
 const char* amr_status_string(int status);
+/* Synchronise `stream`, then report whether a kernel of this library on the current device gave
+ * up a bounded wait (a data copy that never arrived) since the last report: AMR_ERR_TIMEOUT once,
+ * and the device's flag is cleared.  The operator entry points are asynchronous, so this is how
+ * their callers learn of such a failure.  No counterpart in the reference, whose kernels do not
+ * wait on one another. */
+int amr_device_status(void* stream);
 
 /* ---------------------------------------------------------------- compressed_float3 codec
  * 3 x (sign + 8-bit mantissa) with a 5-bit shared exponent, bit-exact with the reference's
@@ -296,10 +303,21 @@ int amr_sim_set_octree(amr_sim* s, const uint32_t* positions, const int32_t* par
 int amr_sim_rng(const amr_sim* s, int32_t* seed);
 int amr_sim_set_rng(amr_sim* s, int32_t seed);
 int amr_sim_stream(amr_sim* s, void** stream);
+/* Wait for the simulation's work; AMR_ERR_TIMEOUT (once) if a kernel gave up a bounded wait. */
 int amr_sim_synchronize(amr_sim* s);
 /* Kernel launches the library issued for this simulation since creation (graph replays count
  * the kernels in the graph). */
 uint64_t amr_sim_kernel_launches(const amr_sim* s);
+/* Test hook of the failure path (no counterpart in the reference): with spin_limit != 0 the fused
+ * BSSN pass's data waits give up after that many polls, and with withhold_plane = q + 1 each CTA's
+ * producer skips its q-th plane request, so the waits on it run out.  The pass then leaves with
+ * invalid results and amr_sim_synchronize returns AMR_ERR_TIMEOUT (once).  (0, 0) turns it off. */
+int amr_sim_set_fault_injection(amr_sim* s, uint32_t spin_limit, uint32_t withhold_plane);
+/* Number of CTAs of the fused BSSN derivative pass (AMR_MODE_BATCHED / AMR_MODE_GRAPH), in place
+ * of the library's choice; 0 restores it.  Results do not depend on it (every CTA takes an equal
+ * contiguous range of the active domains' planes).  The reference sizes its launches from the
+ * domain constants instead (AMR.h:1119-1142). */
+int amr_sim_set_stencil_ctas(amr_sim* s, uint32_t ctas);
 /* Optional timing of the dominant kernel (the derivative stencil) with CUDA events on the
  * simulation's stream.  amr_sim_kernel_timing returns the summed milliseconds and launch count
  * since the last reset. */

@@ -112,6 +112,14 @@ void orc_bssn_timestep(const orc_cfg* c, float* const* old6, float* const* new6,
                        const uint64_t* boundaries, uint32_t used, uint32_t max_depth, uint32_t* timer, int32_t* rng,
                        uint32_t slot_begin, uint32_t slot_end);
 
+/* ---- the same timestep in double precision with no quantisation (oracle/fp64_path.c): the FP64
+ * host oracle for error reports and the FP64 CPU stencil path.  old6/new6 padded doubles;
+ * grad6[k], chr6[k]: 3 doubles per inner cell; ric6[k]: 1 double per inner cell.  Every slot. */
+void orc_bssn_timestep_f64(const orc_cfg* c, double* const* old6, double* const* new6, double* const* grad6,
+                           double* const* chr6, double* const* ric6, const uint32_t* positions,
+                           const int32_t* children, const uint64_t* boundaries, uint32_t used, uint32_t max_depth,
+                           uint32_t* timer);
+
 /* parallel.h:10-82, 215-251, 385-421 -- the reference's scan and reductions over `n` elements of
  * `ncomp` values; dtype 0 uint32, 1 int32, 2 float32 (flushing subnormals as the device build).
  * The array ends as the reference leaves it; orc_extreme writes the result to `result`. */

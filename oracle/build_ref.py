@@ -16,6 +16,10 @@ Two steps:
               also works where the checkout is absent, as long as a previous
               stage() left the headers in oracle/_ref/src/.
 
+The reference checkout's AdaptiveMesh/ folder is taken from the AMR_REFERENCE_DIR environment
+variable, or from the `--ref DIR` argument when run as a script; its default is the checkout's
+location in the build container, /root/reference/AdaptiveMesh.
+
 Configurations: "n28p2" is the reference as shipped (size_domain 28, padding 2);
 "n16p3" is size_domain 16 with padding 3 (the workload size of the benchmarks).
 """
@@ -29,7 +33,8 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference/AdaptiveMesh"
+DEFAULT_REF_ROOT = "/root/reference/AdaptiveMesh"
+REF_ROOT = os.environ.get("AMR_REFERENCE_DIR", DEFAULT_REF_ROOT)
 OUT = os.path.join(HERE, "_ref")
 HEADERS = ["helper_math.h", "tensors.h", "AMR.h", "BSSN.h", "SimpleWave.h", "CUDA_memory.h", "image_process.h",
            "parallel.h"]
@@ -37,15 +42,16 @@ CONFIGS = {"n28p2": (28, 2), "n16p3": (16, 3)}
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 
 
-def stage() -> bool:
+def stage(ref_root: str | None = None) -> bool:
     """Copy reference headers into oracle/_ref/src/<cfg>; returns False if no checkout."""
-    if not os.path.isdir(REF_ROOT):
+    ref_root = ref_root or REF_ROOT
+    if not os.path.isdir(ref_root):
         return False
     for cfg, (n, p) in CONFIGS.items():
         dst = os.path.join(OUT, "src", cfg)
         os.makedirs(dst, exist_ok=True)
         for h in HEADERS:
-            src = os.path.join(REF_ROOT, h)
+            src = os.path.join(ref_root, h)
             with open(src, "rb") as f:
                 data = f.read()
             if h == "AMR.h" and cfg != "n28p2":
@@ -79,9 +85,9 @@ def _build_one(cfg: str) -> str:
     return lib
 
 
-def build(configs=None) -> list[str]:
+def build(configs=None, ref_root: str | None = None) -> list[str]:
     """Build every configuration whose staged headers exist; returns the library paths."""
-    stage()
+    stage(ref_root)
     configs = configs or list(CONFIGS)
     todo = [c for c in configs if os.path.isdir(os.path.join(OUT, "src", c))]
     with ThreadPoolExecutor(max_workers=len(todo) or 1) as ex:
@@ -93,4 +99,9 @@ def lib_path(cfg: str) -> str:
 
 
 if __name__ == "__main__":
-    print("\n".join(build(sys.argv[1:] or None)))
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--ref", default=None, help="the reference checkout's AdaptiveMesh/ folder")
+    ap.add_argument("configs", nargs="*", help=f"configurations to build (default: all of {list(CONFIGS)})")
+    args = ap.parse_args()
+    print("\n".join(build(args.configs or None, args.ref)))

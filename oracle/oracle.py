@@ -13,7 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liborc.so")
-SRC = [os.path.join(HERE, "amr_oracle.c"), os.path.join(HERE, "amr_oracle.h")]
+SRC = [os.path.join(HERE, "amr_oracle.c"), os.path.join(HERE, "fp64_path.c"), os.path.join(HERE, "amr_oracle.h")]
 
 FUSED_NOISE = 1
 FTZ = 2
@@ -64,6 +64,7 @@ _SIGS = {
     "orc_extreme": (None, [ctypes.c_int, ctypes.c_int, ctypes.c_int, VP, U32, VP]),
     "orc_differentiate_f64": (None, [VP, VP, VP, VP, VP, VP, U32]),
     "orc_bssn_timestep": (None, [VP, VP, VP, VP, VP, VP, VP, VP, VP, U32, U32, VP, VP, U32, U32]),
+    "orc_bssn_timestep_f64": (None, [VP, VP, VP, VP, VP, VP, VP, VP, VP, U32, U32, VP]),
     "orc_num_threads": (ctypes.c_int, []),
     "orc_set_num_threads": (None, [ctypes.c_int]),
 }
@@ -77,7 +78,7 @@ def build() -> str:
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
-           "-o", LIB + ".tmp", SRC[0], "-lm"]
+           "-o", LIB + ".tmp", SRC[0], SRC[1], "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(LIB + ".tmp", LIB)
     return LIB

@@ -199,3 +199,18 @@ def test_restriction_plan_brings_every_child(am, orc, n, p, tree, ranks):
             assert np.array_equal(lo[sel].view(np.uint32), full_old[sel].view(np.uint32)), f"substep {s} rank {r}"
     if ranks > 1 and tree != "uniform2":
         assert received > 0
+
+
+def test_plan_refuses_records_deeper_than_the_tree(am):
+    """A boundary record whose depth exceeds max_depth (a bad upload or checkpoint) would make the
+    plan shift by a negative count: refused with AMR_ERR_INVALID."""
+    from adaptivemesh_gb300 import sharding
+    pos, bd, used, md = _tree("bssn")
+    owner = sharding.partition_morton(pos, used, 2)
+    bd = bd.copy()
+    slot = next(s for s in range(used) if int(bd[s * 6]) & 0xFFFFFF not in (0xFFFFFF,) and owner[s] == 1)
+    word = int(bd[slot * 6])
+    bd[slot * 6] = (word & ~(0xF << 28)) | ((md + 1) << 28)
+    with pytest.raises(am.AmrError) as info:
+        sharding.exchange_plan(am.Config(16, 3, OUTER), bd, owner, used, 0, md, 1)
+    assert info.value.status == am.ERR_INVALID
