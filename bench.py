@@ -16,9 +16,15 @@ Metric: zone-cycles/s = 512 * 16^3 leaf zones x steps / seconds (covered parents
          (amr_sim_stage_to_device / amr_sim_snapshot_to_host): the next step's input is uploaded
          and this step's output downloaded while the next step computes.
 
+  parity        the last end-to-end step recomputed on the host cores by the oracle from the same
+                input and generator state: "ok" when every downloaded word equals it (the traces
+                within 1e-4 of their scale: the device divides with the hardware reciprocal)
+  cpu_baseline  the same stencils in FP64 without quantisation on all host cores (one whole
+                timestep over every domain); cpu_fp32_port is the oracle's FP32 restatement
+
 `--impl reference` times the reference path on the CPU: the reference has no CPU solver, so
-this is the oracle's restatement of BSSN_AMR_data::timestep (OpenMP over domains), on a bounded
-sample of the same workload each step.
+this is the oracle's restatement of BSSN_AMR_data::timestep (bit-identical to the reference's
+device build, OpenMP over planes), whole timesteps over every domain of the same workload.
 """
 from __future__ import annotations
 
@@ -131,80 +137,106 @@ def fused_restriction_bytes_per_leaf() -> int:
     return 6 * 4 * (N + 2 * P) ** 3
 
 
-class CpuPort:
-    """The oracle's restatement of BSSN_AMR_data::timestep on the host cores (OpenMP over
-    domains), run on a bounded sample of the workload's leaf domains."""
+def golden_tree(depth: int) -> dict:
+    """The uniform octree's arrays as the reference's own host code (AMR<T>, AMR.h:118-294) builds
+    them, from the committed fixture (tests/golden/gen_host_golden.py), so that the CPU legs need
+    neither this library nor the checker library to lay out their work."""
+    import numpy as np
+    hg = np.load(os.path.join(ROOT, "tests", "golden", "host_golden.npz"))
+    key = f"tree/uniform{depth}"
+    if f"{key}/positions" not in hg.files:
+        raise ValueError(f"no fixture of the uniform depth-{depth} tree")
+    sc = hg[f"{key}/scalars"]
+    return {"positions": hg[f"{key}/positions"], "children": hg[f"{key}/children"],
+            "boundaries": hg[f"{key}/boundaries"], "used_slots": int(sc[3]), "max_depth": int(sc[1])}
 
-    def __init__(self, threads: int | None = None):
+
+class CpuTimestep:
+    """One whole BSSN_AMR_data::timestep (8 substeps, every slot: 512 leaves and 73 parents) on the
+    host cores through the oracle (OpenMP over planes): `fp32` is the restatement that is
+    bit-identical to the reference's device build, `fp64` the same stencils in double precision
+    without quantisation (oracle/fp64_path.c)."""
+
+    def __init__(self, depth: int, threads: int | None = None):
         import numpy as np
-        import adaptivemesh_gb300 as am
         from oracle import oracle as orc
         import cases
-
-        o = am.Octree(600)
-        build_tree(o)
-        self.st = st = o.state()
-        self.used = used = st["used_slots"]
-        xyz = cases.cell_coordinates(st["positions"], used, N, P, OUTER)
-        metric = cases.metric_fields(xyz, OUTER, 500)
-        self.orc, self.c, self.L = orc, orc.cfg(N, P, OUTER), orc.lib()
+        self.np, self.orc, self.L = np, orc, orc.lib()
         if threads:
             self.L.orc_set_num_threads(threads)
         self.cores = int(self.L.orc_num_threads())
-        inner = used * N ** 3
-        self.arrays = ([m.copy() for m in metric], [m.copy() for m in metric],
-                       [np.zeros(inner, np.uint32) for _ in range(6)], [np.zeros(inner, np.uint32) for _ in range(6)],
-                       [np.zeros(inner, np.float32) for _ in range(6)])
-        self.pp = [orc.ptrs(x) for x in self.arrays]
-        self.first_leaf = used - 512          # leaves are the last 512 slots of the breadth-first tree
-        self.n_leaf = 8
+        self.st = st = golden_tree(depth)
+        self.used = used = st["used_slots"]
+        self.zones = 8 ** depth * N ** 3
+        xyz = cases.cell_coordinates(st["positions"], used, N, P, OUTER)
+        self.metric = cases.metric_fields(xyz, OUTER, 500)
+        self.c = orc.cfg(N, P, OUTER)
 
-    def run(self, n_leaf: int) -> float:
-        st, orc, pp = self.st, self.orc, self.pp
-        timer, rng = ctypes.c_uint32(0), ctypes.c_int32(12894712)
+    def fp32(self, new6=None, seed: int = 12894712) -> tuple[float, dict]:
+        np, orc, st = self.np, self.orc, self.st
+        inner = self.used * N ** 3
+        src = new6 if new6 is not None else self.metric
+        arrays = {"old": [m.copy() for m in src], "new": [m.copy() for m in src],
+                  "dmet": [np.zeros(inner, np.uint32) for _ in range(6)],
+                  "chr": [np.zeros(inner, np.uint32) for _ in range(6)],
+                  "ricci": [np.zeros(inner, np.float32) for _ in range(6)]}
+        pp = {k: orc.ptrs(v) for k, v in arrays.items()}
+        timer, rng = ctypes.c_uint32(0), ctypes.c_int32(seed)
         t0 = time.perf_counter()
-        self.L.orc_bssn_timestep(ctypes.byref(self.c), pp[0], pp[1], pp[2], pp[3], pp[4],
+        self.L.orc_bssn_timestep(ctypes.byref(self.c), pp["old"], pp["new"], pp["dmet"], pp["chr"], pp["ricci"],
                                  orc.P(st["positions"]), orc.P(st["children"]), orc.P(st["boundaries"]), self.used,
-                                 st["max_depth"], ctypes.byref(timer), ctypes.byref(rng), self.first_leaf,
-                                 self.first_leaf + n_leaf)
+                                 st["max_depth"], ctypes.byref(timer), ctypes.byref(rng), 0, self.used)
+        return time.perf_counter() - t0, arrays
+
+    def fp64(self) -> float:
+        np, orc, st = self.np, self.orc, self.st
+        inner = self.used * N ** 3
+        arrays = [[m.astype(np.float64) for m in self.metric], [m.astype(np.float64) for m in self.metric],
+                  [np.zeros(inner * 3) for _ in range(6)], [np.zeros(inner * 3) for _ in range(6)],
+                  [np.zeros(inner) for _ in range(6)]]
+        pp = [orc.ptrs(a) for a in arrays]
+        timer = ctypes.c_uint32(0)
+        t0 = time.perf_counter()
+        self.L.orc_bssn_timestep_f64(ctypes.byref(self.c), *pp, orc.P(st["positions"]), orc.P(st["children"]),
+                                     orc.P(st["boundaries"]), self.used, st["max_depth"], ctypes.byref(timer))
         return time.perf_counter() - t0
 
-    def calibrate(self, seconds: float) -> None:
-        t = self.run(8)
-        self.n_leaf = int(max(8, min(512, 8 * seconds / max(t, 1e-3))))
 
-    def sample(self) -> dict:
-        t = self.run(self.n_leaf)
-        return {"value": self.n_leaf * N ** 3 / t, "unit": UNIT, "cores": self.cores, "kind": "port",
-                "sample": f"{self.n_leaf} of 512 leaf domains, one full timestep (8 substeps), {t:.2f} s"}
-
-
-def cpu_sample(seconds_target: float, threads: int | None = None) -> dict:
-    port = CpuPort(threads)
-    port.calibrate(seconds_target)
-    return port.sample()
+def config_dict(depth: int, world: int) -> dict:
+    """The workload description both arms print (identical keys and values at the same N)."""
+    return {"workload": workload(depth), "leaf_domains": 8 ** depth * world, "zones_per_domain": N ** 3,
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "state 299 MB > L2 129 MB, no flush" if (depth, N, P) == (3, 16, 3) else "no flush"}
 
 
 def reference_arm(args) -> None:
+    """The reference's path on the host cores: the oracle's restatement of BSSN_AMR_data::timestep,
+    bit-identical to the reference's device build (the reference has no CPU solver of its own),
+    whole timesteps over every domain on all host threads.  Steps that would not finish within
+    about three minutes are not run, and `steps` reports the steps timed."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    port = CpuPort()
-    # each step is a bounded sample, sized so that the whole run stays within a few minutes
-    port.calibrate(max(0.2, min(args.cpu_seconds, 150.0 / (args.steps + args.warmup))))
-    for _ in range(args.warmup):
-        port.sample()
-    vals = [port.sample() for _ in range(args.steps)]
-    v = statistics.median(x["value"] for x in vals)
-    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 8 ** args.depth * N ** 3 / v * 1e3, "higher_is_better": True,
+    port = CpuTimestep(args.depth)
+    t_first, _ = port.fp32()                      # also the first warm-up step
+    budget = 180.0
+    warm = max(0, min(args.warmup - 1, int(budget * 0.2 / t_first)))
+    for _ in range(warm):
+        port.fp32()
+    steps = max(1, min(args.steps, int((budget - (warm + 1) * t_first) / t_first)))
+    times = [port.fp32()[0] for _ in range(steps)]
+    total = sum(times)
+    v = port.zones * steps / total
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+            "warmup": warm + 1, "ms_per_step": total / steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload(args.depth), "leaf_domains": 8 ** args.depth, "zones_per_domain": N ** 3,
-                       "parallelism": "replicas"},
-            "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"]},
+            "config": config_dict(args.depth, args.gpus), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": port.cores, "kind": "port",
+                             "sample": f"{steps} whole timesteps (8 substeps each) over all {port.used} domains "
+                                       f"({port.zones // N ** 3} leaves), FP32 restatement"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if steps < args.steps:
+        line["steps_requested"] = args.steps
     # For comparison only (not this arm's value): the reference's own CUDA plugin on this GPU, its
     # headers compiled for sm_103a into the checker library, on the same workload
     try:
@@ -264,7 +296,6 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="graph", choices=["plain", "batched", "graph"])
-    ap.add_argument("--cpu-seconds", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--depth", type=int, default=DEPTH, help="uniform octree depth (3 = the benchmark workload)")
     ap.add_argument("--size", type=int, default=N, help="size_domain (16 = the benchmark workload; 8, 16, 28, 32)")
@@ -306,7 +337,6 @@ def main() -> None:
     metric = cases.metric_fields(xyz, OUTER, 500)
     T3 = cfg.total ** 3
     padded, inner = used * T3, used * N ** 3
-    state_mb = 12 * padded * 4 / 1e6   # old and new, six components each
     # host buffers (page-locked) of the state and of the step's outputs; every copy goes through
     # the C ABI on the simulation's stream
     # A timestep's inputs are the six `new` fields: its first phase (restriction at substep 0, when
@@ -362,9 +392,12 @@ def main() -> None:
     progress("e2e")
     # ---- end to end through the C ABI with host buffers (e2e)
 
+    last_seed = [0]
+
     def e2e_steps(k):
         upload()                  # the first step's input
         for i in range(k):
+            last_seed[0] = sim.rng   # the host generator as this step starts (checked below)
             sim.timestep()
             download()            # this step's output ...
             if i + 1 < k:
@@ -428,16 +461,37 @@ def main() -> None:
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload(args.depth), "leaf_domains": zones // N ** 3 * world,
-                       "zones_per_domain": N ** 3, "parallelism": "replicas" if world > 1 else "single",
-                       "mode": args.mode, "l2": f"state {state_mb:.0f} MB > L2 129 MB, no flush"},
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args.depth, world),
+            "mode": args.mode,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": ms_e2e / args.steps},
             "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clocks.summary()}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        progress("cpu baseline")
-        line["cpu_baseline"] = cpu_sample(args.cpu_seconds)
+        progress("cpu baseline and parity of the last timed step")
+        try:
+            cpu = CpuTimestep(args.depth)
+            # the last end-to-end step's input (the uploaded metric) and generator, on the host
+            # cores: its outputs must equal what that step downloaded
+            t32, ref = cpu.fp32([h.numpy() for h in h_in], last_seed[0])
+            bad = []
+            for i, (w, k, _n) in enumerate(outs):
+                got = h_out[i].numpy()
+                want = {am.Sim.NEW: ref["new"], am.Sim.DMET: ref["dmet"], am.Sim.CHR: ref["chr"],
+                        am.Sim.RICCI: ref["ricci"]}[w][k]
+                if w == am.Sim.RICCI:   # hardware reciprocal on the device, exact division here
+                    if not np.all(np.abs(got - want) <= 1e-4 * (float(np.abs(want).max()) + 1e-30)):
+                        bad.append(f"trace {k}")
+                elif np.count_nonzero(got.view(np.uint32) != want.view(np.uint32)):
+                    bad.append(f"buffer {w}/{k}")
+            line["parity"] = "ok" if not bad else "mismatch: " + ", ".join(bad)
+            t64 = cpu.fp64()
+            line["cpu_baseline"] = {"value": cpu.zones / t64, "unit": UNIT, "cores": cpu.cores, "kind": "port",
+                                    "sample": f"one whole timestep (8 substeps, all {cpu.used} domains) of the same "
+                                              f"stencils in FP64 without quantisation, {t64:.2f} s"}
+            line["cpu_fp32_port"] = {"value": cpu.zones / t32, "unit": UNIT, "cores": cpu.cores,
+                                     "sample": f"the last timed step recomputed by the FP32 restatement, {t32:.2f} s"}
+        except ValueError as e:   # no fixture of this tree depth
+            line["parity"] = f"unchecked: {e}"
     if rank == 0:
         print(json.dumps(line), flush=True)
     # release every torch object that refers to the simulation's memory or stream first

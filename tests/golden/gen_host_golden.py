@@ -12,7 +12,8 @@ run the reference's __host__ code, are called).  Writes <out>/host_golden.npz wi
   boundary/*   domain_boundary words between every pair of nodes of the 'bssn' and 'uneven' trees
   inverse/*    float3x3_sym::inverse on random symmetric positive-definite matrices
   tree/<name>/*  the octree arrays (AMR.h:118-294) after building each tree of cases.TREES and
-               cases.EDGE_TREES (depth limit, full slot array), a uniform depth-2 tree and a random script of add / remove / timer / find
+               cases.EDGE_TREES (depth limit, full slot array), uniform depth-2 and depth-3 trees and a random
+               script of add / remove / timer / find
                operations; for the script also the state digest after every operation
 
 The committed copy is tests/golden/host_golden.npz, checked on the CPU by
@@ -155,6 +156,11 @@ def main(out_dir: str):
     o = reflib.RefOctree(lib, 80)
     cases.tree_uniform(o, 2)
     put_state(out, "tree/uniform2", o.state())
+    o.close()
+    # the benchmark's octree (uniform depth 3: 585 slots), also read by the benchmark's CPU legs
+    o = reflib.RefOctree(lib, 585)
+    cases.tree_uniform(o, 3)
+    put_state(out, "tree/uniform3", o.state())
     o.close()
     script = octree_script(2024, 400)
     o = reflib.RefOctree(lib, SLOTS)

@@ -84,13 +84,14 @@ def test_inverse_within_contraction_noise(orc, hg):
     assert np.all(np.abs(out - ref) <= 2e-6 * scale)
 
 
-@pytest.mark.parametrize("tree", ["wave", "bssn", "uneven", "uniform2", "root", "deep", "full"])
+@pytest.mark.parametrize("tree", ["wave", "bssn", "uneven", "uniform2", "uniform3", "root", "deep", "full"])
 def test_octree_matches_reference(am, hg, tree):
     """The octree arrays after building each tree equal the reference octree's, including the
-    depth limit ('deep') and a full slot array ('full')."""
-    o = am.Octree(80 if tree == "uniform2" else cases.EDGE_SLOTS.get(tree, hgen.SLOTS))
-    if tree == "uniform2":
-        cases.tree_uniform(o, 2)
+    depth limit ('deep'), a full slot array ('full') and the benchmark's tree ('uniform3')."""
+    uniform = {"uniform2": (2, 80), "uniform3": (3, 585)}
+    o = am.Octree(uniform[tree][1] if tree in uniform else cases.EDGE_SLOTS.get(tree, hgen.SLOTS))
+    if tree in uniform:
+        cases.tree_uniform(o, uniform[tree][0])
     else:
         cases.ALL_TREES[tree](o)
     st = o.state()
