@@ -23,7 +23,11 @@ LIB_PATH = _build.LIB
 
 OK = 0
 ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_DEVICE, ERR_CAPACITY, ERR_TIMEOUT = 1, 2, 3, 4, 5, 6
-SIM_BSSN, SIM_WAVE = 1, 2
+SIM_BSSN, SIM_WAVE, SIM_BSSN_EVOLVE, SIM_WAVE_RK4 = 1, 2, 3, 4
+SLICING_1PLUSLOG, SLICING_HARMONIC = 0, 1
+ID_FLAT, ID_GAUGE_WAVE, ID_BRILL_LINDQUIST, ID_GAUSSIAN_PULSE = 0, 1, 2, 3
+# BSSN evolution fields (amr_sim_buffer components)
+F_CHI, F_GXX, F_K, F_AXX, F_GAMX, F_ALPHA, F_BETAX, F_BX = 0, 1, 7, 8, 14, 17, 18, 21
 DTYPE_UINT32, DTYPE_INT32, DTYPE_FLOAT32 = 0, 1, 2
 MODE_PLAIN, MODE_BATCHED, MODE_GRAPH = 0, 1, 2
 # the plugin interface's phases, in the order of the reference's timestep loop (AMR.h:324-333)
@@ -55,6 +59,31 @@ class Config(ctypes.Structure):
 
 
 CP = ctypes.POINTER(Config)
+
+
+class Evolution(ctypes.Structure):
+    """amr_evolution: physics and gauge of an evolution simulation."""
+    _fields_ = [("slicing", ctypes.c_int), ("shift", ctypes.c_int), ("eta", ctypes.c_float),
+                ("ko_sigma", ctypes.c_float), ("cfl", ctypes.c_float), ("periodic", ctypes.c_int)]
+
+    def __init__(self, slicing=0, shift=0, eta=2.0, ko_sigma=0.1, cfl=0.25, periodic=0):
+        super().__init__(slicing, shift, eta, ko_sigma, cfl, periodic)
+
+
+class InitialData(ctypes.Structure):
+    """amr_initial_data: analytic initial data of an evolution simulation."""
+    _fields_ = [("kind", ctypes.c_int), ("amplitude", ctypes.c_float), ("wavelength", ctypes.c_float),
+                ("n_punctures", ctypes.c_int), ("mass", ctypes.c_float * 4), ("position", (ctypes.c_float * 3) * 4),
+                ("width", ctypes.c_float)]
+
+    def __init__(self, kind=0, amplitude=0.0, wavelength=1.0, punctures=(), width=0.1):
+        super().__init__()
+        self.kind, self.amplitude, self.wavelength, self.width = kind, amplitude, wavelength, width
+        self.n_punctures = len(punctures)
+        for i, (m, pos) in enumerate(punctures):
+            self.mass[i] = m
+            for k in range(3):
+                self.position[i][k] = pos[k]
 
 EXPORTS = {
     "amr_version": (ctypes.c_char_p, []),
@@ -121,6 +150,10 @@ EXPORTS = {
     "amr_sim_kernel_launches": (U64, [VP]),
     "amr_sim_set_stencil_ctas": (ctypes.c_int, [VP, U32]),
     "amr_sim_set_fault_injection": (ctypes.c_int, [VP, U32, U32]),
+    "amr_sim_set_evolution": (ctypes.c_int, [VP, VP]),
+    "amr_sim_initial_data": (ctypes.c_int, [VP, VP]),
+    "amr_sim_constraint_norms": (ctypes.c_int, [VP, ctypes.c_float, VP]),
+    "amr_octree_set_periodic": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_enable_kernel_timing": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_kernel_timing": (ctypes.c_int, [VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(U64)]),
     "amr_inclusive_scan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP]),
@@ -185,4 +218,5 @@ def _ptr_array(ts) -> ctypes.Array:
 from . import ops  # noqa: E402
 from .octree import Octree, Sim  # noqa: E402
 
-__all__ = ["Config", "Octree", "Sim", "ops", "load", "check", "AmrError", "LIB_PATH", "EXPORTS"]
+__all__ = ["Config", "Evolution", "InitialData", "Octree", "Sim", "ops", "load", "check", "AmrError", "LIB_PATH",
+           "EXPORTS"]

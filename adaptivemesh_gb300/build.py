@@ -6,8 +6,9 @@ Incremental: a unit is rebuilt when it or any header under csrc/ or include/ is 
 its object.
 
 Device code is compiled with -fmad=false (the kernels spell out every fused multiply-add) and
--ftz=true (subnormals flush to zero, as in the reference's fast-math build); host code with
--ffp-contract=off, so host float arithmetic rounds the same on x86-64 and aarch64.
+-ftz=true (subnormals flush to zero, as in the reference's fast-math build), except the units listed
+in CONTRACTED; host code with -ffp-contract=off, so host float arithmetic rounds the same on x86-64
+and aarch64.
 """
 from __future__ import annotations
 
@@ -37,6 +38,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-fmad=false", "-ftz=true", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
               "-I", INCLUDE, "-I", CSRC]
+# Units without a reference build to reproduce bit for bit (the evolutions, held to an FP64 oracle
+# within stated tolerances) let the compiler contract products and sums into fused multiply-adds.
+CONTRACTED = {"kernels_evolve.cu"}
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
@@ -50,7 +54,10 @@ def _compile(src: str, newest_header: float) -> str:
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), newest_header):
         return obj
     if src.endswith(".cu"):
-        cmd = [_nvcc(), *NVCC_FLAGS, "-c", src, "-o", obj + ".tmp"]
+        flags = NVCC_FLAGS
+        if os.path.basename(src) in CONTRACTED:
+            flags = [("-fmad=true" if f == "-fmad=false" else f) for f in NVCC_FLAGS]
+        cmd = [_nvcc(), *flags, "-c", src, "-o", obj + ".tmp"]
     else:
         cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, "-I", os.path.join(os.path.dirname(_nvcc()), "..", "include"),
                "-c", src, "-o", obj + ".tmp"]

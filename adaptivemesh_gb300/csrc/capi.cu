@@ -333,6 +333,11 @@ AMR_API int amr_octree_remove_nodes(amr_octree* o, const int32_t* nodes, uint32_
     o->tree.end_batch();
     return AMR_OK;
 }
+AMR_API int amr_octree_set_periodic(amr_octree* o, int periodic) {
+    AMR_REQUIRE(o);
+    o->tree.set_periodic(periodic != 0);
+    return AMR_OK;
+}
 AMR_API int amr_octree_increment_timer(amr_octree* o) {
     AMR_REQUIRE(o);
     o->tree.increment_timer();

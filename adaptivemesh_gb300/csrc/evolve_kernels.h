@@ -1,0 +1,79 @@
+// evolve_kernels.h -- launch interfaces of the evolution kernels (kernels_evolve.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "evolve.h"
+
+namespace amr {
+
+// Analytic initial data on every cell of the first `used` slots, into three buffer sets (the root's
+// ghost layer, the outer boundary, is never refilled, so every state buffer holds it).
+struct EvoInitArgs {
+    float* out1[kMaxFields];
+    float* out2[kMaxFields];
+    float* out3[kMaxFields];
+    const uint32_t* positions;
+    uint32_t used, n, t;
+    int nf, physics;
+    float outer_size;
+    InitData id;
+};
+
+// Ghost fill of X (the state being filled) for the faces normal to `axis` of the listed slots.
+struct EvoGhostArgs {
+    float* X[kMaxFields];
+    const float* old_f[kMaxFields];
+    const float* new_f[kMaxFields];
+    const uint64_t* boundaries;
+    const uint8_t* evolved;       // per slot: 1 if the slot is evolved (not covered by eight children)
+    const uint32_t* items;
+    uint32_t n_items;
+    uint32_t n, p, t;
+    uint32_t substep, max_depth;
+    int axis;
+    int nf;
+    float c_stage;                // time of the state being filled, as a fraction of the target's step
+};
+
+// Device addresses of the four constraint buffers (H, M_x, M_y, M_z; inner layout).
+struct ConsPtrs {
+    float* c[4];
+};
+
+// Restriction of the listed slots: old <- new, child-covered cells from the child (fourth order).
+struct EvoRestrictArgs {
+    float* old_f[kMaxFields];
+    const float* new_f[kMaxFields];
+    const int32_t* children;
+    const uint32_t* items;
+    uint32_t n_items;
+    uint32_t n, p, t;
+    int nf;
+};
+
+bool evo_config_supported(uint32_t n, uint32_t p);
+cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st);
+cudaError_t launch_evo_init(const EvoInitArgs& a, cudaStream_t st);
+cudaError_t launch_evo_derivs(const EvoArgs& a, cudaStream_t st);
+cudaError_t launch_evo_rhs(const EvoArgs& a, cudaStream_t st);
+cudaError_t launch_evo_ghost(const EvoGhostArgs& g, cudaStream_t st);
+cudaError_t launch_evo_constraints(const EvoArgs& a, const ConsPtrs& cons, cudaStream_t st);
+// FP64 norms of the constraints over the composite grid of the listed slots (interior cells no child
+// covers), leaving out cells within the excision radius of a puncture: out[0] rms H, [1] max |H|,
+// [2] rms |M|, [3] max |M|, [4] cells.  `part` holds 5 doubles per slot.
+struct EvoNormArgs {
+    ConsPtrs cons;
+    const uint32_t* items;
+    uint32_t n_items, n;
+    const uint32_t* positions;
+    const int32_t* children;
+    float outer_size;
+    float excision2;
+    int n_punctures;
+    float pos[4][3];
+};
+cudaError_t launch_evo_norms(const EvoNormArgs& g, double* part, double* out, cudaStream_t st);
+
+}  // namespace amr

@@ -1,0 +1,405 @@
+// evolve_sim.cu -- simulations of the evolution kinds (AMR_SIM_BSSN_EVOLVE, AMR_SIM_WAVE_RK4) on the
+// amr_sim object: the reference's timestep loop (AMR.h:324-333) with RK4 substeps (evolve.h).
+//
+// Phases of one substep (the plugin interface's names):
+//   copy_back     restriction of every active domain: old <- new, child-covered cells <- the child's
+//                 new field at the cell's centre, fourth order (the reference's copy_new_to_old,
+//                 AMR.h:961-996, averages the 2x2x2 cells: second order)
+//   modify_nodes  nothing (regridding is driven from outside, amr_sim_add_nodes / remove_nodes)
+//   predictor     the four RK4 stages over the active evolved domains, each a derivative pass and a
+//                 pointwise update, with the ghost cells of stages 2-4 filled in between
+//   copy_bounds   ghost fill of the final state (so that the next restriction copies valid ghosts)
+//   corrector     nothing (RK4 has no separate corrector stage)
+// Buffers per field: old (state at the start of a step), new (final state; also the stage-3 input),
+// stage (stages 2 and 4), all padded; the RK accumulator (inner layout).
+#include <algorithm>
+
+#include "evolve_kernels.h"
+#include "sim_base.h"
+
+namespace amr {
+
+class EvolveSim : public SimBase {
+public:
+    EvolveSim(const amr_config& c, int kind, uint32_t slots, int mode) : SimBase(c, slots, mode), kind(kind) {
+        nf = kind == AMR_SIM_BSSN_EVOLVE ? BSSN_NF : WAVE_NF;
+        nd = kind == AMR_SIM_BSSN_EVOLVE ? BSSN_ND_CONSTRAINTS : WAVE_ND;
+        kind_id = kind;
+        prm.physics = kind == AMR_SIM_BSSN_EVOLVE ? 0 : 1;
+        prm.slicing = AMR_SLICING_1PLUSLOG;
+        prm.shift = 0;
+        prm.eta = 2.f;
+        prm.ko_sigma = .1f;
+        prm.cfl = .25f;
+        prm.chi_floor = 1e-6f;
+        prm.outer_size = c.outer_size;
+    }
+    ~EvolveSim() override {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        for (int f = 0; f < kMaxFields; f++) { cudaFree(old_f[f]); cudaFree(new_f[f]); cudaFree(stage_f[f]); cudaFree(acc[f]); }
+        for (float* c : cons.c) cudaFree(c);
+        cudaFree(deriv); cudaFree(d_evolved); cudaFree(d_lists); cudaFree(d_part); cudaFree(d_norms);
+    }
+    int init() override {
+        int st = SimBase::init();
+        if (st) return st;
+        const size_t s = tree.max_slots();
+        const size_t padded = s * dims.t * dims.t * dims.t, inner = s * dims.n * dims.n * dims.n;
+        cudaError_t e = cudaSuccess;
+        for (int f = 0; f < nf && e == cudaSuccess; f++) {
+            e = dev_alloc(&old_f[f], padded);
+            if (e == cudaSuccess) e = dev_alloc(&new_f[f], padded);
+            if (e == cudaSuccess) e = dev_alloc(&stage_f[f], padded);
+            if (e == cudaSuccess) e = dev_alloc(&acc[f], inner);
+        }
+        if (e == cudaSuccess) e = dev_alloc(&deriv, inner * (size_t)nd);
+        for (int k = 0; k < 4 && e == cudaSuccess && kind == AMR_SIM_BSSN_EVOLVE; k++) e = dev_alloc(&cons.c[k], inner);
+        if (e == cudaSuccess) e = dev_alloc(&d_evolved, s);
+        if (e == cudaSuccess) e = dev_alloc(&d_lists, s * 2u * ((size_t)1u << kDepthLimit) + 2u * s);
+        if (e == cudaSuccess) e = dev_alloc(&d_part, s * 5u);
+        if (e == cudaSuccess) e = dev_alloc(&d_norms, 8);
+        return cuda_status(e);
+    }
+
+    // ---- node constructors: prolongate both state buffers of every field (AMR.h:1053-1115)
+    void node_ctor(int32_t node) override {
+        const uint32_t off = (uint32_t)pos_final_offset(tree.positions()[node]);
+        const int32_t parent = tree.parents()[node];
+        for (int f = 0; f < nf; f++) {
+            check(launch_copy_to_child(dims, old_f[f], off, node, parent, stream));
+            check(launch_copy_to_child(dims, new_f[f], off, node, parent, stream));
+        }
+        graph_valid = false;
+        lists_valid = false;
+    }
+    void node_ctor_groups(const NodeCtor* items, const uint32_t* group_end, uint32_t groups) override {
+        float* bufs[2 * kMaxFields];
+        for (int f = 0; f < nf; f++) { bufs[f] = old_f[f]; bufs[nf + f] = new_f[f]; }
+        // the prolongation launch takes up to 12 buffers: run every group once per chunk of buffers
+        for (int b0 = 0; b0 < 2 * nf; b0 += 12)
+            prolongate_groups(items, group_end, groups, bufs + b0, std::min(12, 2 * nf - b0));
+        graph_valid = false;
+        lists_valid = false;
+    }
+    void node_dtor(int32_t) override { lists_valid = false; }
+
+    int buffer(int which, int comp, void** ptr, uint64_t* count) override {
+        const uint64_t s = tree.max_slots();
+        const uint64_t padded = s * dims.t * dims.t * dims.t, inner = s * dims.n * dims.n * dims.n;
+        if (comp < 0) return AMR_ERR_INVALID;
+        switch (which) {
+            case 0: if (comp >= nf) return AMR_ERR_INVALID; *ptr = old_f[comp]; *count = padded; return AMR_OK;
+            case 1: if (comp >= nf) return AMR_ERR_INVALID; *ptr = new_f[comp]; *count = padded; return AMR_OK;
+            case 2: if (comp >= nf) return AMR_ERR_INVALID; *ptr = stage_f[comp]; *count = padded; return AMR_OK;
+            case 3: if (comp >= nf) return AMR_ERR_INVALID; *ptr = acc[comp]; *count = inner; return AMR_OK;
+            case 4: if (comp >= 4 || !cons.c[comp]) return AMR_ERR_INVALID; *ptr = cons.c[comp]; *count = inner; return AMR_OK;
+            case 5: if (comp >= nd) return AMR_ERR_INVALID; *ptr = deriv + (size_t)comp * inner; *count = inner; return AMR_OK;
+            default: return AMR_ERR_INVALID;
+        }
+    }
+
+    // ---- lists per substep: active domains (restriction) and active evolved domains
+    int build_lists() {
+        if (lists_valid) return AMR_OK;
+        const uint32_t md = (uint32_t)tree.read_max_depth(), used = tree.curr_used_slots();
+        const uint32_t nsub = 1u << md;
+        std::vector<uint8_t> evolved(tree.max_slots(), 0);
+        leaves.clear();
+        // Every live domain is evolved, covered parents included: a leaf beside a covered parent of
+        // its own depth takes its ghost values from it at every stage (and the parent's values are
+        // replaced by its children's at each restriction).
+        for (uint32_t i = 0; i < used; i++) {
+            if (pos_depth_host(tree.positions()[i]) == -1) continue;
+            int nchild = 0;
+            for (int c = 0; c < 8; c++) nchild += tree.children()[(size_t)i * 8u + c] != -1;
+            evolved[i] = 1;
+            if (nchild == 0) leaves.push_back(i);
+        }
+        std::vector<uint32_t> all;
+        act_off.assign(nsub, 0); act_cnt.assign(nsub, 0); evo_off.assign(nsub, 0); evo_cnt.assign(nsub, 0);
+        for (uint32_t s = 0; s < nsub; s++) {
+            act_off[s] = (uint32_t)all.size();
+            for (uint32_t i = 0; i < used; i++) {
+                const int d = pos_depth_host(tree.positions()[i]);
+                if (d != -1 && (s & ((1u << (md - (uint32_t)d)) - 1u)) == 0u) all.push_back(i);
+            }
+            act_cnt[s] = (uint32_t)all.size() - act_off[s];
+            evo_off[s] = (uint32_t)all.size();
+            for (uint32_t k = act_off[s]; k < act_off[s] + act_cnt[s]; k++)
+                if (evolved[all[k]]) all.push_back(all[k]);
+            evo_cnt[s] = (uint32_t)all.size() - evo_off[s];
+        }
+        all_evolved_off = (uint32_t)all.size();
+        for (uint32_t i = 0; i < used; i++)
+            if (evolved[i]) all.push_back(i);
+        all_evolved_cnt = (uint32_t)all.size() - all_evolved_off;
+        leaves_off = (uint32_t)all.size();
+        all.insert(all.end(), leaves.begin(), leaves.end());
+        const size_t cap = (size_t)tree.max_slots() * 2u * ((size_t)1u << kDepthLimit) + 2u * tree.max_slots();
+        if (all.size() > cap) return AMR_ERR_CAPACITY;
+        cudaError_t e = cudaMemcpyAsync(d_lists, all.data(), all.size() * 4u, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_evolved, evolved.data(), evolved.size(), cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        lists_valid = true;
+        return AMR_OK;
+    }
+    int prepare() {
+        int st = sync_octree();
+        if (st) return st;
+        if (!items_valid) { lists_valid = false; items_valid = true; }
+        return build_lists();
+    }
+
+    // ---- phases
+    int copy_back() override {
+        int st = prepare();
+        if (st) return st;
+        const uint32_t s = tree.timer(), md = (uint32_t)tree.read_max_depth();
+        if (act_cnt[s] == 0) return AMR_OK;
+        EvoRestrictArgs g;
+        std::memset(&g, 0, sizeof(g));
+        for (int f = 0; f < nf; f++) { g.old_f[f] = old_f[f]; g.new_f[f] = new_f[f]; }
+        g.children = d_children;
+        g.items = d_lists + act_off[s];
+        g.n_items = act_cnt[s];
+        g.n = dims.n; g.p = dims.p; g.t = dims.t;
+        g.nf = nf;
+        (void)md;
+        return check(launch_evo_restrict(g, stream));
+    }
+    int modify_nodes() override { return AMR_OK; }
+    int predictor() override {
+        int st = prepare();
+        if (st) return st;
+        const uint32_t s = tree.timer();
+        if (evo_cnt[s] == 0) return AMR_OK;
+        float* const* in[4] = {old_f, stage_f, new_f, stage_f};
+        float* const* out[4] = {stage_f, new_f, stage_f, new_f};
+        const float c_next[3] = {.5f, .5f, 1.f};
+        for (int stage = 1; stage <= 4; stage++) {
+            EvoArgs a = args(s, in[stage - 1], out[stage - 1], stage, 0);
+            if ((st = check(launch_evo_derivs(a, stream)))) return st;
+            time_begin();
+            if ((st = check(launch_evo_rhs(a, stream)))) return st;
+            time_end();
+            if (stage < 4 && (st = fill(s, out[stage - 1], c_next[stage - 1]))) return st;
+        }
+        return AMR_OK;
+    }
+    int copy_bounds() override {
+        int st = prepare();
+        if (st) return st;
+        return fill(tree.timer(), new_f, 1.f);
+    }
+    int corrector() override { return AMR_OK; }
+
+    int timestep() override {
+        if (mode != AMR_MODE_GRAPH) return SimBase::timestep();
+        int st = prepare();
+        if (st) return st;
+        if (tree.timer() != 0u) return SimBase::timestep();
+        const uint32_t nsub = 1u << tree.read_max_depth();
+        if (!graph_valid) {
+            if (graph_exec) { cudaGraphExecDestroy(graph_exec); graph_exec = nullptr; }
+            cudaGraph_t graph;
+            cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_status(e);
+            capturing = true;
+            const uint64_t before = launches;
+            st = SimBase::timestep();
+            capturing = false;
+            e = cudaStreamEndCapture(stream, &graph);
+            if (st) { if (e == cudaSuccess) cudaGraphDestroy(graph); return st; }
+            if (e != cudaSuccess) return cuda_status(e);
+            e = cudaGraphInstantiate(&graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_status(e);
+            graph_launches = launches - before;
+            launches = before;
+            graph_valid = true;
+            // the capture ran the host loop (counter and lifetimes) without device work: replay it
+            const cudaError_t e2 = cudaGraphLaunch(graph_exec, stream);
+            if (e2 != cudaSuccess) return cuda_status(e2);
+            launches += graph_launches;
+            return AMR_OK;
+        }
+        const cudaError_t e = cudaGraphLaunch(graph_exec, stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        launches += graph_launches;
+        for (uint32_t s = 0; s < nsub; s++) tree.increment_timer();
+        return AMR_OK;
+    }
+
+    // ---- evolution interface
+    int set_evolution(const amr_evolution& e) {
+        if (!(e.cfl > 0.f) || e.cfl > 1.f || e.ko_sigma < 0.f || e.eta < 0.f) return AMR_ERR_INVALID;
+        if (e.slicing != AMR_SLICING_1PLUSLOG && e.slicing != AMR_SLICING_HARMONIC) return AMR_ERR_INVALID;
+        prm.slicing = e.slicing;
+        prm.shift = e.shift ? 1 : 0;
+        prm.eta = e.eta;
+        prm.ko_sigma = e.ko_sigma;
+        prm.cfl = e.cfl;
+        tree.set_periodic(e.periodic != 0);
+        graph_valid = false;
+        return AMR_OK;
+    }
+    int initial_data(const amr_initial_data& d) {
+        int st = sync_octree();
+        if (st) return st;
+        EvoInitArgs a;
+        std::memset(&a, 0, sizeof(a));
+        for (int f = 0; f < nf; f++) { a.out1[f] = old_f[f]; a.out2[f] = new_f[f]; a.out3[f] = stage_f[f]; }
+        a.positions = d_positions;
+        a.used = tree.curr_used_slots();
+        a.n = dims.n;
+        a.t = dims.t;
+        a.nf = nf;
+        a.physics = prm.physics;
+        a.outer_size = cfg.outer_size;
+        a.id.kind = d.kind;
+        a.id.amplitude = d.amplitude;
+        a.id.wavelength = d.wavelength;
+        a.id.n_punctures = std::min(d.n_punctures, 4);
+        for (int i = 0; i < 4; i++) {
+            a.id.mass[i] = d.mass[i];
+            for (int k = 0; k < 3; k++) a.id.pos[i][k] = d.position[i][k];
+        }
+        a.id.width = d.width;
+        id_used = a.id;
+        tree.set_timer(0u);
+        return check(launch_evo_init(a, stream));
+    }
+    int constraint_norms(float excision, double* out) {
+        if (kind != AMR_SIM_BSSN_EVOLVE) return AMR_ERR_INVALID;
+        int st = prepare();
+        if (st) return st;
+        // derivatives of the current state (new) on every evolved domain, then the constraints
+        EvoArgs a = args(0, new_f, new_f, 0, 1);
+        a.items = d_lists + all_evolved_off;
+        a.n_items = all_evolved_cnt;
+        if ((st = check(launch_evo_derivs(a, stream)))) return st;
+        if ((st = check(launch_evo_constraints(a, cons, stream)))) return st;
+        EvoNormArgs g;
+        std::memset(&g, 0, sizeof(g));
+        g.cons = cons;
+        g.items = a.items;
+        g.n_items = a.n_items;
+        g.n = dims.n;
+        g.positions = d_positions;
+        g.children = d_children;
+        g.outer_size = cfg.outer_size;
+        g.excision2 = excision * excision;
+        g.n_punctures = excision > 0.f ? id_used.n_punctures : 0;
+        for (int i = 0; i < 4; i++)
+            for (int k = 0; k < 3; k++) g.pos[i][k] = id_used.pos[i][k];
+        if ((st = check(launch_evo_norms(g, d_part, d_norms, stream)))) return st;
+        cudaError_t e = cudaMemcpyAsync(out, d_norms, 5 * sizeof(double), cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        return cuda_status(e);
+    }
+
+private:
+    EvoArgs args(uint32_t s, float* const* in, float* const* out, int stage, int constraints) {
+        EvoArgs a;
+        std::memset(&a, 0, sizeof(a));
+        for (int f = 0; f < nf; f++) {
+            a.fields[f] = in[f];
+            a.out[f] = out[f];
+            a.old_f[f] = old_f[f];
+            a.acc[f] = acc[f];
+        }
+        a.deriv = deriv;
+        a.deriv_stride = (uint64_t)tree.max_slots() * dims.n * dims.n * dims.n;
+        a.positions = d_positions;
+        a.items = d_lists + (evo_off.empty() ? 0u : evo_off[s]);
+        a.n_items = evo_cnt.empty() ? 0u : evo_cnt[s];
+        a.n = dims.n;
+        a.p = dims.p;
+        a.t = dims.t;
+        a.dt0 = prm.cfl * cfg.outer_size / (float)dims.n;
+        a.stage = stage;
+        a.constraints = constraints;
+        a.prm = prm;
+        a.err = err_flag;
+        return a;
+    }
+    // ghost fill of `x` (the state at c_stage of the active domains' step), three axis passes
+    int fill(uint32_t s, float* const* x, float c_stage) {
+        if (evo_cnt[s] == 0) return AMR_OK;
+        EvoGhostArgs g;
+        std::memset(&g, 0, sizeof(g));
+        for (int f = 0; f < nf; f++) { g.X[f] = x[f]; g.old_f[f] = old_f[f]; g.new_f[f] = new_f[f]; }
+        g.boundaries = d_boundaries;
+        g.evolved = d_evolved;
+        g.items = d_lists + evo_off[s];
+        g.n_items = evo_cnt[s];
+        g.n = dims.n; g.p = dims.p; g.t = dims.t;
+        g.substep = s;
+        g.max_depth = (uint32_t)tree.read_max_depth();
+        g.nf = nf;
+        g.c_stage = c_stage;
+        for (int axis = 0; axis < 3; axis++) {
+            g.axis = axis;
+            const int st = check(launch_evo_ghost(g, stream));
+            if (st) return st;
+        }
+        return AMR_OK;
+    }
+
+    int kind, nf, nd;
+    EvoParams prm;
+    InitData id_used = {};     // the last initial data (puncture positions for the excision)
+    float* old_f[kMaxFields] = {};
+    float* new_f[kMaxFields] = {};
+    float* stage_f[kMaxFields] = {};
+    float* acc[kMaxFields] = {};
+    float* deriv = nullptr;
+    ConsPtrs cons = {};
+    uint8_t* d_evolved = nullptr;
+    uint32_t* d_lists = nullptr;
+    double* d_part = nullptr;
+    double* d_norms = nullptr;
+    bool lists_valid = false;
+    std::vector<uint32_t> act_off, act_cnt, evo_off, evo_cnt, leaves;
+    uint32_t all_evolved_off = 0, all_evolved_cnt = 0, leaves_off = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_launches = 0;
+};
+
+SimBase* make_evolve_sim(const amr_config& c, int kind, uint32_t slots, int mode) {
+    return new (std::nothrow) EvolveSim(c, kind, slots, mode);
+}
+bool is_evolve_sim(const SimBase* s) { return dynamic_cast<const EvolveSim*>(s) != nullptr; }
+
+}  // namespace amr
+
+using namespace amr;
+
+#define AMR_API extern "C" __attribute__((visibility("default")))
+
+AMR_API int amr_sim_set_evolution(amr_sim* s, const amr_evolution* e) {
+    if (!s || !e) return AMR_ERR_INVALID;
+    EvolveSim* v = dynamic_cast<EvolveSim*>(s->impl);
+    if (!v) return AMR_ERR_INVALID;
+    return v->set_evolution(*e);
+}
+AMR_API int amr_sim_initial_data(amr_sim* s, const amr_initial_data* d) {
+    if (!s || !d) return AMR_ERR_INVALID;
+    EvolveSim* v = dynamic_cast<EvolveSim*>(s->impl);
+    if (!v) return AMR_ERR_INVALID;
+    if (d->kind < AMR_ID_FLAT || d->kind > AMR_ID_GAUSSIAN_PULSE || d->n_punctures < 0 || d->n_punctures > 4)
+        return AMR_ERR_INVALID;
+    if (d->kind == AMR_ID_GAUGE_WAVE && !(d->wavelength > 0.f)) return AMR_ERR_INVALID;
+    if (d->kind == AMR_ID_GAUSSIAN_PULSE && !(d->width > 0.f)) return AMR_ERR_INVALID;
+    const int st = s->impl->wait_side(-1, 0);
+    return st ? st : v->initial_data(*d);
+}
+AMR_API int amr_sim_constraint_norms(amr_sim* s, float excision_radius, double* out5) {
+    if (!s || !out5 || !(excision_radius >= 0.f)) return AMR_ERR_INVALID;
+    EvolveSim* v = dynamic_cast<EvolveSim*>(s->impl);
+    if (!v) return AMR_ERR_INVALID;
+    const int st = s->impl->wait_side(-1, 0);
+    return st ? st : v->constraint_norms(excision_radius, out5);
+}

@@ -1,0 +1,609 @@
+// kernels_evolve.cu -- kernels of the BSSN evolution and of the scalar wave u_tt = Δu (evolve.h).
+//
+// Compiled with contraction on (-fmad=true): unlike the reference-semantics kernels, these have no
+// reference device build to reproduce bit for bit; they are held to the FP64 oracle
+// (oracle/bssn_evolve.c) within stated tolerances.
+//
+//   k_evo_init      analytic initial data on every cell (ghosts included) of every live slot
+//   k_evo_derivs    derivative pass: a CTA per (domain, z-slab); each field's padded slab moves into
+//                   shared memory with one 1-D bulk copy (two buffers, the next field in flight),
+//                   then first / second / mixed derivatives, advection and Kreiss-Oliger terms
+//   k_evo_rhs_*     pointwise right-hand side and RK4 stage update
+//   k_evo_ghost     ghost fill of a stage's state, one face-normal axis per launch
+//   k_evo_constraints, k_evo_norms_*   Hamiltonian and momentum constraints, FP64 norms
+#include <cmath>
+
+#include "amr_device.cuh"
+#include "evolve.h"
+#include "evolve_kernels.h"
+#include "evolve_physics.cuh"
+#include "kernels.h"
+#include "tma.cuh"
+
+namespace amr {
+
+namespace {
+
+// Centre of a slot's domain in units of the root edge (the root spans [-1/2, 1/2]).
+__device__ __forceinline__ void slot_centre(uint32_t pos, float c[3]) {
+    const int depth = pos_depth(pos);
+    c[0] = c[1] = c[2] = 0.f;
+    uint32_t path = pos & kPathMask;
+    float step = .25f;
+    for (int i = 0; i < depth; i++, path >>= 3, step *= .5f)
+        for (int a = 0; a < 3; a++) c[a] += (path & (1u << a)) ? step : -step;
+}
+
+// ------------------------------------------------------------------ initial data
+__global__ void k_evo_init(EvoInitArgs a) {
+    const uint32_t t = a.t, cells = t * t * t;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)a.used * cells) return;
+    const uint32_t slot = (uint32_t)(gid / cells), c = (uint32_t)(gid % cells);
+    const uint32_t pos = a.positions[slot];
+    const int depth = pos_depth(pos);
+    if (depth == -1) return;
+    float ctr[3];
+    slot_centre(pos, ctr);
+    const float h = a.outer_size / ((float)a.n * (float)(1u << depth));
+    const uint32_t idx[3] = {c % t, (c / t) % t, c / (t * t)};
+    float x[3];
+    for (int k = 0; k < 3; k++) x[k] = ctr[k] * a.outer_size + ((float)idx[k] + .5f - .5f * (float)t) * h;
+    float u[kMaxFields];
+    evo_initial_values(a.id, a.physics, x, u);
+    for (int f = 0; f < a.nf; f++) {
+        a.out1[f][gid] = u[f];
+        a.out2[f][gid] = u[f];
+        a.out3[f][gid] = u[f];
+    }
+}
+
+// ------------------------------------------------------------------ derivative pass
+// z-slab planes per unit: the slab's padded planes (ZS + 6) of one field fit twice in shared memory
+template <int N>
+struct DerivShape {
+    static constexpr int P = 3, T = N + 2 * P;
+    static constexpr int ZS = N >= 32 ? 2 : 4;
+    static constexpr int THREADS = 256;
+    static constexpr int CELLS = N * N * ZS;
+    static constexpr int CPT = CELLS / THREADS;          // cells per thread
+    static constexpr uint32_t SLAB = (uint32_t)((ZS + 6) * T * T);   // floats
+    static constexpr uint32_t SLAB_BYTES = SLAB * 4u;
+    static constexpr size_t SMEM = 2u * SLAB_BYTES + 64u;
+    static_assert(CELLS % THREADS == 0 && N % ZS == 0, "whole cells per thread and planes per slab");
+    static_assert(SLAB_BYTES % 16u == 0u && (T * T * 4) % 16 == 0, "slabs are aligned bulk copies");
+};
+
+// The order in which the derivative pass visits the fields: the shift first, so that the advection
+// terms of the others can use it.
+__device__ __forceinline__ int deriv_field_order(int physics, int i) {
+    if (physics != 0) return i;
+    return i < 3 ? F_BETAX + i : (i < 21 ? i - 3 : i);
+}
+
+template <int N>
+__global__ void __launch_bounds__(DerivShape<N>::THREADS) k_evo_derivs(const __grid_constant__ EvoArgs a) {
+    using S = DerivShape<N>;
+    constexpr int T = S::T, ZS = S::ZS, CPT = S::CPT;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* buf = reinterpret_cast<float*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + 2u * S::SLAB_BYTES);
+    __shared__ int s_abort;
+
+    const uint32_t tid = threadIdx.x;
+    const uint32_t slabs = N / ZS;
+    const uint32_t item = blockIdx.x / slabs, slab = blockIdx.x % slabs;
+    if (item >= a.n_items) return;
+    const uint32_t slot = a.items[item];
+    const int depth = pos_depth(a.positions[slot]);
+    const int nf = a.prm.physics == 0 ? BSSN_NF : WAVE_NF;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+        s_abort = 0;
+    }
+    __syncthreads();
+    const size_t src_off = (size_t)slot * T * T * T + (size_t)slab * ZS * T * T;   // padded plane slab*ZS (p = 3)
+    auto issue = [&](int i) {   // field of visit i into buffer i % 2
+        const int f = deriv_field_order(a.prm.physics, i);
+        mbar_arrive_expect_tx(&bar[i & 1], S::SLAB_BYTES);
+        bulk_g2s(buf + (size_t)(i & 1) * S::SLAB, a.fields[f] + src_off, S::SLAB_BYTES, &bar[i & 1]);
+    };
+    if (tid == 0) {
+        issue(0);
+        if (nf > 1) issue(1);
+    }
+    const float h = a.prm.outer_size / ((float)N * (float)(1u << depth));
+    const float i12h = 1.f / (12.f * h), i12h2 = 1.f / (12.f * h * h), i144h2 = 1.f / (144.f * h * h);
+    const float ko = a.prm.ko_sigma / (64.f * h);
+    const bool bssn = a.prm.physics == 0;
+    const bool shift_on = bssn && a.prm.shift != 0;
+    // the shift at each of this thread's cells, for the advection terms of every field
+    float beta[CPT][3];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+        const uint32_t cell = tid + (uint32_t)c * S::THREADS;
+        const uint32_t x = cell % N, y = (cell / N) % N, z = slab * ZS + cell / (N * N);
+        const size_t pi = (size_t)slot * T * T * T + ((size_t)(z + 3) * T + (y + 3)) * T + (x + 3);
+#pragma unroll
+        for (int k = 0; k < 3; k++) beta[c][k] = bssn ? a.fields[F_BETAX + k][pi] : 0.f;
+    }
+    float* D = a.deriv;
+    const uint64_t ds = a.deriv_stride;
+
+    int stopped = nf;   // the visit at which a wait gave up
+    for (int i = 0; i < nf; i++) {
+        const int f = deriv_field_order(a.prm.physics, i);
+        const bool ok = mbar_wait(&bar[i & 1], (uint32_t)(i >> 1) & 1u);
+        if (!ok) s_abort = 1;
+        __syncthreads();
+        if (s_abort) { stopped = i; break; }
+        const float* tile = buf + (size_t)(i & 1) * S::SLAB;
+#pragma unroll
+        for (int c = 0; c < CPT; c++) {
+            const uint32_t cell = tid + (uint32_t)c * S::THREADS;
+            const uint32_t x = cell % N, y = (cell / N) % N, zl = cell / (N * N);
+            const uint32_t z = slab * ZS + zl;
+            const float* q = tile + ((zl + 3) * T + (y + 3)) * T + (x + 3);
+            const uint64_t o = ((uint64_t)slot * N + z) * N * N + (uint64_t)y * N + x;
+            constexpr int st[3] = {1, T, T * T};
+            float d1[3], ko_sum = 0.f;
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+                const int s = st[ax];
+                d1[ax] = ((q[-2 * s] - q[2 * s]) + 8.f * (q[s] - q[-s])) * i12h;
+                ko_sum += (q[-3 * s] + q[3 * s]) - 6.f * (q[-2 * s] + q[2 * s]) + 15.f * (q[-s] + q[s]) - 20.f * q[0];
+            }
+            // which derivatives this field keeps (evolve.h): first, second (with mixed)
+            int first = -1, second = -1;
+            if (bssn) {
+                if (f == F_CHI) { first = D_CHI1; second = D_CHI2; }
+                else if (f >= F_GXX && f <= F_GZZ) { first = D_G1 + 3 * (f - F_GXX); second = D_G2 + 6 * (f - F_GXX); }
+                else if (f == F_K) first = D_K1;
+                else if (f >= F_AXX && f <= F_AZZ) { if (a.constraints) first = D_AT1 + 3 * (f - F_AXX); }
+                else if (f >= F_GAMX && f <= F_GAMZ) first = D_GAM1 + 3 * (f - F_GAMX);
+                else if (f == F_ALPHA) { first = D_AL1; second = D_AL2; }
+                else if (f >= F_BETAX && f <= F_BETAZ) { first = D_BE1 + 3 * (f - F_BETAX); second = D_BE2 + 6 * (f - F_BETAX); }
+            }
+            if (first >= 0)
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) D[(uint64_t)(first + ax) * ds + o] = d1[ax];
+            if (second >= 0 || !bssn) {
+                float dd[3];
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                    const int s = st[ax];
+                    dd[ax] = (16.f * (q[-s] + q[s]) - (q[-2 * s] + q[2 * s]) - 30.f * q[0]) * i12h2;
+                }
+                if (!bssn) {
+                    if (f == W_U) D[(uint64_t)WD_LAP * ds + o] = dd[0] + dd[1] + dd[2];
+                } else {
+#pragma unroll
+                    for (int ax = 0; ax < 3; ax++) D[(uint64_t)(second + ax) * ds + o] = dd[ax];
+                    constexpr int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+                    constexpr float w[4] = {1.f, -8.f, 8.f, -1.f};
+                    constexpr int off[4] = {-2, -1, 1, 2};
+#pragma unroll
+                    for (int m = 0; m < 3; m++) {
+                        const int sa = st[pa[m]], sb = st[pb[m]];
+                        float acc = 0.f;
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            float row = 0.f;
+#pragma unroll
+                            for (int v = 0; v < 4; v++) row = fmaf(w[v], q[off[u] * sa + off[v] * sb], row);
+                            acc = fmaf(w[u], row, acc);
+                        }
+                        D[(uint64_t)(second + 3 + m) * ds + o] = acc * i144h2;
+                    }
+                }
+            }
+            // advection along the shift and dissipation (a frozen shift and its driver have neither)
+            float extra = ko * ko_sum;
+            if (bssn) {
+                extra = fmaf(beta[c][0], d1[0], fmaf(beta[c][1], d1[1], fmaf(beta[c][2], d1[2], extra)));
+                if (!shift_on && f >= F_BETAX) extra = 0.f;
+            }
+            D[(uint64_t)((bssn ? D_EXTRA : WD_EXTRA) + f) * ds + o] = extra;
+        }
+        __syncthreads();   // every thread is done with buffer i % 2
+        if (tid == 0 && i + 2 < nf) issue(i + 2);
+    }
+    // Every copy issued was waited for, except after a wait gave up at visit `stopped`: the copies
+    // of visits stopped and stopped + 1 may still be in flight, and the CTA's shared memory must
+    // outlive them (bounded waits).
+    if (stopped < nf && tid == 0) {
+        atomicExch(a.err, 1);
+        for (int i = stopped; i < nf && i <= stopped + 1; i++) mbar_wait(&bar[i & 1], (uint32_t)(i >> 1) & 1u);
+    }
+}
+
+// ------------------------------------------------------------------ right-hand sides and stage update
+// RK4: stage 1: acc = old + dt/6 k1, out = old + dt/2 k1; stage 2: acc += dt/3 k2, out = old + dt/2 k2;
+// stage 3: acc += dt/3 k3, out = old + dt k3; stage 4: out = acc + dt/6 k4.
+__device__ __forceinline__ void rk_update(const EvoArgs& a, int f, uint64_t pi, uint64_t ii, float u_old, float r,
+                                          float dt) {
+    switch (a.stage) {
+        case 1:
+            a.acc[f][ii] = fmaf(dt * (1.f / 6.f), r, u_old);
+            a.out[f][pi] = fmaf(dt * .5f, r, u_old);
+            break;
+        case 2:
+            a.acc[f][ii] = fmaf(dt * (1.f / 3.f), r, a.acc[f][ii]);
+            a.out[f][pi] = fmaf(dt * .5f, r, u_old);
+            break;
+        case 3:
+            a.acc[f][ii] = fmaf(dt * (1.f / 3.f), r, a.acc[f][ii]);
+            a.out[f][pi] = fmaf(dt, r, u_old);
+            break;
+        default:
+            a.out[f][pi] = fmaf(dt * (1.f / 6.f), r, a.acc[f][ii]);
+            break;
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) k_evo_rhs_bssn(const __grid_constant__ EvoArgs a) {
+    constexpr int P = 3, T = N + 2 * P;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)a.n_items * N * N * N) return;
+    const uint32_t item = (uint32_t)(gid / (N * N * N)), cell = (uint32_t)(gid % (N * N * N));
+    const uint32_t slot = a.items[item];
+    const uint32_t x = cell % N, y = (cell / N) % N, z = cell / (N * N);
+    const int depth = pos_depth(a.positions[slot]);
+    const float dt = a.dt0 / (float)(1u << depth);
+    const uint64_t pi = (uint64_t)slot * T * T * T + ((uint64_t)(z + P) * T + (y + P)) * T + (x + P);
+    const uint64_t ii = (uint64_t)slot * N * N * N + cell;
+    float u[BSSN_NF];
+#pragma unroll
+    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi];
+    const float* D = a.deriv;
+    const uint64_t ds = a.deriv_stride;
+    auto dv = [&](int k) { return D[(uint64_t)k * ds + ii]; };
+    float rhs[BSSN_NF];
+    bssn_rhs(u, dv, a.prm, rhs);
+#pragma unroll 1
+    for (int f = 0; f < BSSN_NF; f++) {
+        const float r = rhs[f] + dv(D_EXTRA + f);
+        const float uo = a.stage == 1 ? u[f] : a.old_f[f][pi];
+        rk_update(a, f, pi, ii, uo, r, dt);
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_evo_rhs_wave(const __grid_constant__ EvoArgs a) {
+    constexpr int P = 3, T = N + 2 * P;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)a.n_items * N * N * N) return;
+    const uint32_t item = (uint32_t)(gid / (N * N * N)), cell = (uint32_t)(gid % (N * N * N));
+    const uint32_t slot = a.items[item];
+    const uint32_t x = cell % N, y = (cell / N) % N, z = cell / (N * N);
+    const int depth = pos_depth(a.positions[slot]);
+    const float dt = a.dt0 / (float)(1u << depth);
+    const uint64_t pi = (uint64_t)slot * T * T * T + ((uint64_t)(z + P) * T + (y + P)) * T + (x + P);
+    const uint64_t ii = (uint64_t)slot * N * N * N + cell;
+    const float* D = a.deriv;
+    const uint64_t ds = a.deriv_stride;
+    const float uu = a.fields[W_U][pi], vv = a.fields[W_V][pi];
+    const float r_u = vv + D[(uint64_t)(WD_EXTRA + W_U) * ds + ii];
+    const float r_v = D[(uint64_t)WD_LAP * ds + ii] + D[(uint64_t)(WD_EXTRA + W_V) * ds + ii];
+    rk_update(a, W_U, pi, ii, a.stage == 1 ? uu : a.old_f[W_U][pi], r_u, dt);
+    rk_update(a, W_V, pi, ii, a.stage == 1 ? vv : a.old_f[W_V][pi], r_v, dt);
+}
+
+// ------------------------------------------------------------------ ghost fill
+__global__ void __launch_bounds__(256) k_evo_ghost(const __grid_constant__ EvoGhostArgs g) {
+    const uint32_t item = blockIdx.x >> 1, side = blockIdx.x & 1u;   // side 0: + face, 1: - face
+    if (item >= g.n_items) return;
+    const uint32_t slot = g.items[item];
+    const uint32_t n = g.n, p = g.p, t = g.t, d = (uint32_t)g.axis;
+    const uint32_t face = d + 3u * side;
+    const uint64_t bd = g.boundaries[(size_t)slot * 6u + face];
+    const int32_t src = bd_target(bd);
+    const int cd = bd_curr_depth(bd);
+    if (src == -1 || cd <= 0) return;
+    const uint32_t dd = bd_depth_diff(bd);
+    const int sd = cd - (int)dd;
+    const bool root_src = src == 0;
+    const bool src_evolved = g.evolved[src] != 0;
+    const bool src_active = active_depth(g.substep, (uint32_t)sd, g.max_depth);
+    // the source's state at the time of the value being filled (evolve.h)
+    int mode;      // 0: old only, 1: X only, 2: old..X, 3: old..new
+    float frac = 0.f;
+    if (!src_evolved) mode = 0;
+    else if (src_active) {
+        mode = dd == 0u ? 1 : 2;
+        frac = 1.f / (float)(1u << dd);
+    } else {
+        mode = 3;
+        const uint32_t kp = (g.substep >> (g.max_depth - (uint32_t)cd)) & ((1u << dd) - 1u);
+        frac = ((float)kp + g.c_stage) / (float)(1u << dd);
+    }
+    const float3 relp = cf3_decode((uint32_t)(bd >> 32));
+    const float rel[3] = {relp.x, relp.y, relp.z};
+    const float rel_scale = 1.f / (float)(1u << dd);
+    // extents of the fill: axes before d over the whole padded range (their ghosts are filled),
+    // axes after d over the interior
+    uint32_t lo[3], ext[3];
+    for (uint32_t a2 = 0; a2 < 3; a2++) {
+        if (a2 == d) { lo[a2] = side == 0 ? p + n : 0; ext[a2] = p; }
+        else if (a2 < d) { lo[a2] = 0; ext[a2] = t; }
+        else { lo[a2] = p; ext[a2] = n; }
+    }
+    const uint32_t count = ext[0] * ext[1] * ext[2];
+    const uint64_t cells = (uint64_t)t * t * t;
+    for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) {
+        const uint32_t w[3] = {lo[0] + k % ext[0], lo[1] + (k / ext[0]) % ext[1], lo[2] + k / (ext[0] * ext[1])};
+        const uint64_t dst = (uint64_t)slot * cells + ((uint64_t)w[2] * t + w[1]) * t + w[0];
+        // source cell (same depth: the cell itself) or the base cell b of a tricubic stencil b-1 .. b+2
+        // kept inside the cells that are valid: the interior along the normal axis and the later
+        // axes, the whole padded range along the earlier axes (filled by earlier passes) and
+        // everywhere in the root (its frozen ghost layer is the outer boundary)
+        int idx[3];
+        float wgt[3][4];
+        const bool exact = dd == 0u;
+        for (uint32_t a2 = 0; a2 < 3; a2++) {
+            float rp = ((float)w[a2] - (float)p + .5f) / (float)n - .5f;
+            rp = rp * rel_scale + rel[a2];
+            const float ri = (rp + .5f) * (float)n + (float)p - .5f;
+            if (exact) {
+                idx[a2] = __float2int_rn(ri);
+                continue;
+            }
+            const int lo_c = root_src || a2 < d ? 1 : (int)p + 1;
+            const int hi_c = root_src || a2 < d ? (int)t - 3 : (int)(t - p) - 3;
+            int b = __float2int_rd(ri);
+            b = b < lo_c ? lo_c : (b > hi_c ? hi_c : b);
+            const float x = ri - (float)b;
+            idx[a2] = b;
+            wgt[a2][0] = -x * (x - 1.f) * (x - 2.f) * (1.f / 6.f);
+            wgt[a2][1] = (x + 1.f) * (x - 1.f) * (x - 2.f) * .5f;
+            wgt[a2][2] = -(x + 1.f) * x * (x - 2.f) * .5f;
+            wgt[a2][3] = (x + 1.f) * x * (x - 1.f) * (1.f / 6.f);
+        }
+        const int64_t si = (int64_t)src * (int64_t)cells + ((int64_t)idx[2] * t + idx[1]) * t + idx[0];
+        for (int f = 0; f < g.nf; f++) {
+            const float* A0 = g.old_f[f];
+            const float* A1 = mode == 3 ? g.new_f[f] : g.X[f];
+            float va = 0.f, vb = 0.f;
+            if (exact) {
+                va = A0[si];
+                vb = A1[si];
+            } else {
+#pragma unroll
+                for (int k2 = 0; k2 < 4; k2++)
+#pragma unroll
+                    for (int k1 = 0; k1 < 4; k1++) {
+                        const float w12 = wgt[1][k1] * wgt[2][k2];
+                        const int64_t row = si + ((int64_t)(k2 - 1) * t + (k1 - 1)) * t - 1;
+#pragma unroll
+                        for (int k0 = 0; k0 < 4; k0++) {
+                            const float wk = wgt[0][k0] * w12;
+                            va = fmaf(wk, A0[row + k0], va);
+                            if (mode != 0) vb = fmaf(wk, A1[row + k0], vb);
+                        }
+                    }
+            }
+            float v;
+            if (mode == 0) v = va;
+            else if (mode == 1) v = vb;
+            else v = fmaf(frac, vb, (1.f - frac) * va);
+            g.X[f][dst] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ restriction
+// old <- new for every listed slot; a cell covered by a child <- the child's new field at the cell's
+// centre (the corner shared by 2x2x2 child cells), by the 4-point midpoint rule (-1, 9, 9, -1)/16 along
+// each axis (child cells 2c-1 .. 2c+2, the child's ghost layer at its faces included).  The reference
+// averages the 2x2x2 block (AMR.h:961-996), a second-order rule.
+__global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ EvoRestrictArgs g) {
+    const uint32_t t = g.t, p = g.p, n = g.n, hn = n / 2;
+    const uint32_t item = blockIdx.x / t, z = blockIdx.x % t;
+    if (item >= g.n_items) return;
+    const uint32_t slot = g.items[item];
+    const uint64_t cells = (uint64_t)t * t * t;
+    constexpr float w4[4] = {-1.f / 16.f, 9.f / 16.f, 9.f / 16.f, -1.f / 16.f};
+    for (uint32_t k = threadIdx.x; k < t * t; k += blockDim.x) {
+        const uint32_t x = k % t, y = k / t;
+        const uint32_t tx = (x - p) / hn, ty = (y - p) / hn, tz = (z - p) / hn;   // unsigned wrap for ghosts
+        const int32_t ch = (tx < 2u && ty < 2u && tz < 2u) ? g.children[tx + ty * 2u + tz * 4u + slot * 8u] : -1;
+        const uint64_t o = slot * cells + ((uint64_t)z * t + y) * t + x;
+        if (ch == -1) {
+            for (int f = 0; f < g.nf; f++) g.old_f[f][o] = g.new_f[f][o];
+            continue;
+        }
+        const uint32_t cx = ((x - p) * 2u) % n + p, cy = ((y - p) * 2u) % n + p, cz = ((z - p) * 2u) % n + p;
+        const uint64_t base = (uint64_t)ch * cells + ((uint64_t)(cz - 1) * t + (cy - 1)) * t + (cx - 1);
+        for (int f = 0; f < g.nf; f++) {
+            const float* v = g.new_f[f];
+            float acc = 0.f;
+#pragma unroll
+            for (int k2 = 0; k2 < 4; k2++)
+#pragma unroll
+                for (int k1 = 0; k1 < 4; k1++) {
+                    float row = 0.f;
+#pragma unroll
+                    for (int k0 = 0; k0 < 4; k0++) row = fmaf(w4[k0], v[base + ((uint64_t)k2 * t + k1) * t + k0], row);
+                    acc = fmaf(w4[k1] * w4[k2], row, acc);
+                }
+            g.old_f[f][o] = acc;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ constraints and FP64 norms
+template <int N>
+__global__ void __launch_bounds__(128) k_evo_constraints(const __grid_constant__ EvoArgs a, const ConsPtrs cons) {
+    constexpr int P = 3, T = N + 2 * P;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (uint64_t)a.n_items * N * N * N) return;
+    const uint32_t item = (uint32_t)(gid / (N * N * N)), cell = (uint32_t)(gid % (N * N * N));
+    const uint32_t slot = a.items[item];
+    const uint32_t x = cell % N, y = (cell / N) % N, z = cell / (N * N);
+    const uint64_t pi = (uint64_t)slot * T * T * T + ((uint64_t)(z + P) * T + (y + P)) * T + (x + P);
+    const uint64_t ii = (uint64_t)slot * N * N * N + cell;
+    float u[BSSN_NF];
+#pragma unroll
+    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi];
+    const float* D = a.deriv;
+    const uint64_t ds = a.deriv_stride;
+    auto dv = [&](int k) { return D[(uint64_t)k * ds + ii]; };
+    float hm[4];
+    bssn_constraints(u, dv, a.prm, hm);
+    for (int k = 0; k < 4; k++) cons.c[k][ii] = hm[k];
+}
+
+// One CTA per live slot: sum of H^2, max |H|, sum of |M|^2, max |M| and the cell count over its
+// interior cells that no child covers and that lie outside the excision radius of every puncture, in
+// double, with a fixed reduction order.
+__device__ __forceinline__ double nan_max(double a, double b) { return (a != a || b != b) ? (a + b) : fmax(a, b); }
+__global__ void __launch_bounds__(256) k_evo_norms_domain(const EvoNormArgs g, double* part) {
+    const uint32_t b = blockIdx.x;
+    if (b >= g.n_items) return;
+    const uint32_t slot = g.items[b], n = g.n, hn = n / 2;
+    const uint32_t cells = n * n * n;
+    const uint32_t pos = g.positions[slot];
+    const int depth = pos_depth(pos);
+    float ctr[3];
+    slot_centre(pos, ctr);
+    const float h = g.outer_size / ((float)n * (float)(1u << depth));
+    double s[5] = {0, 0, 0, 0, 0};
+    for (uint32_t c = threadIdx.x; c < cells; c += blockDim.x) {
+        const uint32_t x = c % n, y = (c / n) % n, z = c / (n * n);
+        const uint32_t oct = (x / hn) | ((y / hn) << 1) | ((z / hn) << 2);
+        if (g.children[slot * 8u + oct] != -1) continue;
+        bool excised = false;
+        for (int a = 0; a < g.n_punctures; a++) {
+            const float dx = ctr[0] * g.outer_size + ((float)x + .5f - .5f * (float)n) * h - g.pos[a][0];
+            const float dy = ctr[1] * g.outer_size + ((float)y + .5f - .5f * (float)n) * h - g.pos[a][1];
+            const float dz = ctr[2] * g.outer_size + ((float)z + .5f - .5f * (float)n) * h - g.pos[a][2];
+            excised |= dx * dx + dy * dy + dz * dz < g.excision2;
+        }
+        if (excised) continue;
+        const uint64_t i = (uint64_t)slot * cells + c;
+        const double hv = g.cons.c[0][i];
+        const double m2 = (double)g.cons.c[1][i] * g.cons.c[1][i] + (double)g.cons.c[2][i] * g.cons.c[2][i] +
+                          (double)g.cons.c[3][i] * g.cons.c[3][i];
+        s[0] += hv * hv;
+        s[1] = nan_max(s[1], fabs(hv));
+        s[2] += m2;
+        s[3] = nan_max(s[3], sqrt(m2));
+        s[4] += 1.0;
+    }
+    __shared__ double red[5][256];
+    for (int k = 0; k < 5; k++) red[k][threadIdx.x] = s[k];
+    __syncthreads();
+    for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[0][threadIdx.x] += red[0][threadIdx.x + w];
+            red[1][threadIdx.x] = nan_max(red[1][threadIdx.x], red[1][threadIdx.x + w]);
+            red[2][threadIdx.x] += red[2][threadIdx.x + w];
+            red[3][threadIdx.x] = nan_max(red[3][threadIdx.x], red[3][threadIdx.x + w]);
+            red[4][threadIdx.x] += red[4][threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 5; k++) part[(size_t)b * 5 + k] = red[k][0];
+}
+__global__ void k_evo_norms_total(const double* part, uint32_t n_items, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s[5] = {0, 0, 0, 0, 0};
+    for (uint32_t b = 0; b < n_items; b++) {
+        s[0] += part[(size_t)b * 5];
+        s[1] = nan_max(s[1], part[(size_t)b * 5 + 1]);
+        s[2] += part[(size_t)b * 5 + 2];
+        s[3] = nan_max(s[3], part[(size_t)b * 5 + 3]);
+        s[4] += part[(size_t)b * 5 + 4];
+    }
+    out[0] = s[4] > 0 ? sqrt(s[0] / s[4]) : 0.;
+    out[1] = s[1];
+    out[2] = s[4] > 0 ? sqrt(s[2] / s[4]) : 0.;
+    out[3] = s[3];
+    out[4] = s[4];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+bool evo_config_supported(uint32_t n, uint32_t p) { return p == 3u && (n == 8u || n == 16u || n == 32u); }
+
+cudaError_t launch_evo_init(const EvoInitArgs& a, cudaStream_t st) {
+    const uint64_t total = (uint64_t)a.used * a.t * a.t * a.t;
+    if (total == 0) return cudaSuccess;
+    k_evo_init<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t derivs_t(const EvoArgs& a, cudaStream_t st) {
+    using S = DerivShape<N>;
+    static std::atomic<uint64_t> configured{0};
+    cudaError_t e = ensure_smem_limit(k_evo_derivs<N>, S::SMEM, configured);
+    if (e != cudaSuccess || a.n_items == 0) return e;
+    k_evo_derivs<N><<<a.n_items * (N / S::ZS), S::THREADS, S::SMEM, st>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_evo_derivs(const EvoArgs& a, cudaStream_t st) {
+    switch (a.n) {
+        case 8: return derivs_t<8>(a, st);
+        case 16: return derivs_t<16>(a, st);
+        case 32: return derivs_t<32>(a, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int N>
+static cudaError_t rhs_t(const EvoArgs& a, cudaStream_t st) {
+    const uint64_t total = (uint64_t)a.n_items * N * N * N;
+    if (total == 0) return cudaSuccess;
+    if (a.prm.physics == 0) k_evo_rhs_bssn<N><<<(unsigned)((total + 127) / 128), 128, 0, st>>>(a);
+    else k_evo_rhs_wave<N><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_evo_rhs(const EvoArgs& a, cudaStream_t st) {
+    switch (a.n) {
+        case 8: return rhs_t<8>(a, st);
+        case 16: return rhs_t<16>(a, st);
+        case 32: return rhs_t<32>(a, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st) {
+    if (g.n_items == 0) return cudaSuccess;
+    k_evo_restrict<<<g.n_items * g.t, 256, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evo_ghost(const EvoGhostArgs& g, cudaStream_t st) {
+    if (g.n_items == 0) return cudaSuccess;
+    k_evo_ghost<<<g.n_items * 2u, 256, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t cons_t(const EvoArgs& a, const ConsPtrs& cons, cudaStream_t st) {
+    const uint64_t total = (uint64_t)a.n_items * N * N * N;
+    if (total == 0) return cudaSuccess;
+    k_evo_constraints<N><<<(unsigned)((total + 127) / 128), 128, 0, st>>>(a, cons);
+    return cudaGetLastError();
+}
+cudaError_t launch_evo_constraints(const EvoArgs& a, const ConsPtrs& cons, cudaStream_t st) {
+    switch (a.n) {
+        case 8: return cons_t<8>(a, cons, st);
+        case 16: return cons_t<16>(a, cons, st);
+        case 32: return cons_t<32>(a, cons, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+cudaError_t launch_evo_norms(const EvoNormArgs& g, double* part, double* out, cudaStream_t st) {
+    if (g.n_items) k_evo_norms_domain<<<g.n_items, 256, 0, st>>>(g, part);
+    k_evo_norms_total<<<1, 32, 0, st>>>(part, g.n_items, out);
+    return cudaGetLastError();
+}
+
+}  // namespace amr

@@ -61,6 +61,9 @@ uint32_t cf3_encode_host(float x, float y, float z) {
 }
 
 uint64_t make_boundary(uint32_t this_pos, uint32_t other_pos, int32_t other_idx) {
+    return make_boundary(this_pos, other_pos, other_idx, 0, 0.f);
+}
+uint64_t make_boundary(uint32_t this_pos, uint32_t other_pos, int32_t other_idx, int axis, float shift) {
     const int td = pos_depth_host(this_pos), od = pos_depth_host(other_pos);
     const uint32_t node_data = ((uint32_t)other_idx & 16777215u) | (((uint32_t)(td - od) & 15u) << 24) |
                                (((uint32_t)td & 15u) << 28);
@@ -73,6 +76,7 @@ uint64_t make_boundary(uint32_t this_pos, uint32_t other_pos, int32_t other_idx)
     s = other_pos & kPathMask;
     for (int i = 0; i < od; i++, s >>= 3)
         for (int a = 0; a < 3; a++) r[a] -= ((s & (1u << a)) ? mult : -mult) / (float)(1 << i);
+    r[axis] += shift;
     return (uint64_t)node_data | ((uint64_t)cf3_encode_host(r[0], r[1], r[2]) << 32);
 }
 
@@ -243,10 +247,26 @@ uint64_t Octree::yield_boundary(int32_t node, uint32_t face) const {
     // step one domain along the face normal at this depth, and reverse back.
     uint32_t p = reverse_bits32(positions_[node]) >> 5u;
     const uint32_t step = (kDirections[face % 3u] << ((9u - (uint32_t)depth) * 3u)) & kPathMask;
-    p = face < 3 ? morton_sum(p, step, true) : morton_diff(p, step, true);
-    uint32_t neighbour = find_node_idx(reverse_bits32(p) >> 5u, (uint32_t)depth);
-    if (p == ~0u) neighbour = 0;   // outside the root: the root's ghost layer is the source
+    const uint32_t q = face < 3 ? morton_sum(p, step, true) : morton_diff(p, step, true);
+    if (q == ~0u && periodic_) {
+        // across the root's boundary: the domain at the wrapped position, shifted by one root edge
+        // (2^depth of the neighbour's edges) to lie beside this one
+        const uint32_t w = face < 3 ? morton_sum(p, step, false) : morton_diff(p, step, false);
+        const uint32_t neighbour = find_node_idx(reverse_bits32(w) >> 5u, (uint32_t)depth);
+        const float root_edges = (float)(1u << (uint32_t)pos_depth_host(positions_[neighbour]));
+        return make_boundary(positions_[node], positions_[neighbour], (int32_t)neighbour, (int)(face % 3u),
+                             face < 3 ? -root_edges : root_edges);
+    }
+    uint32_t neighbour = find_node_idx(reverse_bits32(q) >> 5u, (uint32_t)depth);
+    if (q == ~0u) neighbour = 0;   // outside the root: the root's ghost layer is the source
     return make_boundary(positions_[node], positions_[neighbour], (int32_t)neighbour);
+}
+
+void Octree::set_periodic(bool periodic) {
+    if (periodic == periodic_) return;
+    periodic_ = periodic;
+    refresh_boundaries(1);
+    dirty_ = true;
 }
 
 }  // namespace amr

@@ -44,6 +44,9 @@ uint32_t reverse_bits32(uint32_t a);
 uint32_t morton_sum(uint32_t a, uint32_t b, bool overflow);        // yield_sum_coordinates, AMR.h:102-108
 uint32_t morton_diff(uint32_t a, uint32_t b, bool overflow);       // yield_diff_coordinates, AMR.h:109-115
 uint64_t make_boundary(uint32_t this_pos, uint32_t other_pos, int32_t other_idx);  // AMR.h:64-86
+// The same with `shift` other-domain edges added to the offset along `axis` (a periodic
+// neighbour across the root's boundary is described as if it lay next to this domain).
+uint64_t make_boundary(uint32_t this_pos, uint32_t other_pos, int32_t other_idx, int axis, float shift);
 constexpr uint64_t kNoBoundary = 0xFFFFFFFFull;                   // domain_boundary(), AMR.h:63
 // Host deterministic compressed_float3 encoder (tensors.h:374-393), for boundary offsets.
 uint32_t cf3_encode_host(float x, float y, float z);
@@ -71,6 +74,11 @@ public:
     void end_batch();
     uint32_t find_node_idx(uint32_t packed_pos, uint32_t max_depth = ~0u) const;   // AMR.h:255-263
     uint64_t yield_boundary(int32_t node, uint32_t face) const;                    // AMR.h:276-290
+    // Periodic root (no counterpart in the reference, whose outside neighbour is the root's frozen
+    // ghost layer): a face whose neighbour lies outside the root takes the domain on the opposite
+    // side, found as the reference finds any neighbour, and every boundary is recomputed.
+    void set_periodic(bool periodic);
+    bool periodic() const { return periodic_; }
 
     uint32_t curr_used_slots() const { return final_used_slot_ + 1u; }
     uint32_t read_first_free_slot() const { return first_free_slot_; }
@@ -116,6 +124,7 @@ private:
     uint32_t final_used_slot_ = 0;
     uint32_t timer_ = 0;
     bool dirty_ = true;
+    bool periodic_ = false;
     uint32_t depth_count_[32] = {};   // live nodes per depth (any depth a position word can hold)
     bool batching_ = false;
     int batch_min_depth_ = 32;        // shallowest change inside the current batch (32: none)

@@ -37,6 +37,10 @@ class Octree:
     def remove_node(self, node: int) -> None:
         check(load().amr_octree_remove_node(self.h, node), "amr_octree_remove_node")
 
+    def set_periodic(self, periodic: bool = True) -> None:
+        """Periodic root: faces leaving the root take the domain on the opposite side."""
+        check(load().amr_octree_set_periodic(self.h, 1 if periodic else 0), "amr_octree_set_periodic")
+
     def add_nodes(self, parents, offsets) -> None:
         """add_node for each (parent, offset) in order, as one batch (amr_octree_add_nodes)."""
         p, o = np.ascontiguousarray(parents, np.int32), np.ascontiguousarray(offsets, np.int32)
@@ -244,6 +248,24 @@ class Sim:
     def set_stencil_ctas(self, ctas: int) -> None:
         """CTAs of the fused BSSN derivative pass (0: the library's choice)."""
         check(load().amr_sim_set_stencil_ctas(self.h, ctas), "amr_sim_set_stencil_ctas")
+
+    # ---- evolution simulations (SIM_BSSN_EVOLVE, SIM_WAVE_RK4)
+    OLD_STATE, NEW_STATE, STAGE, ACC, CONSTRAINTS, DERIVS = 0, 1, 2, 3, 4, 5
+
+    def set_evolution(self, evolution) -> None:
+        """Physics and gauge (amr_sim_set_evolution; an Evolution structure)."""
+        check(load().amr_sim_set_evolution(self.h, ctypes.byref(evolution)), "amr_sim_set_evolution")
+
+    def initial_data(self, data) -> None:
+        """Analytic initial data on every live slot (amr_sim_initial_data; an InitialData structure)."""
+        check(load().amr_sim_initial_data(self.h, ctypes.byref(data)), "amr_sim_initial_data")
+
+    def constraint_norms(self, excision: float = 0.0) -> dict:
+        """FP64 norms of the Hamiltonian and momentum constraints over the composite grid, leaving out
+        cells within `excision` of a puncture."""
+        out = (ctypes.c_double * 5)()
+        check(load().amr_sim_constraint_norms(self.h, excision, out), "amr_sim_constraint_norms")
+        return {"H_l2": out[0], "H_max": out[1], "M_l2": out[2], "M_max": out[3], "cells": int(out[4])}
 
     def set_fault_injection(self, spin_limit: int = 0, withhold_plane: int = 0) -> None:
         """Failure-path test hook of the fused pass (amr_sim_set_fault_injection); (0, 0) is off."""

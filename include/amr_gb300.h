@@ -193,6 +193,10 @@ int amr_octree_remove_node(amr_octree* o, int32_t node);                       /
 int amr_octree_add_nodes(amr_octree* o, const int32_t* parents, const int32_t* offsets, uint32_t n);
 int amr_octree_remove_nodes(amr_octree* o, const int32_t* nodes, uint32_t n);
 int amr_octree_increment_timer(amr_octree* o);                                 /* AMR.h:180-188 */
+/* Periodic root (no counterpart in the reference, whose neighbour outside the root is the root's
+ * frozen ghost layer, AMR.h:276-290): a face leaving the root takes the domain on the opposite side,
+ * found as any neighbour is, with its offset given as if it lay beside this domain. */
+int amr_octree_set_periodic(amr_octree* o, int periodic);
 uint32_t amr_octree_find_node_idx(const amr_octree* o, uint32_t packed_pos, uint32_t max_depth); /* AMR.h:255-263 */
 /* scalars: timer_helper, max_depth, first_free_slot, curr_used_slots, max_slots.  Any output
  * pointer may be NULL; arrays hold node_slots (x8 children, x6 boundaries) entries. */
@@ -323,6 +327,53 @@ int amr_sim_set_stencil_ctas(amr_sim* s, uint32_t ctas);
  * since the last reset. */
 int amr_sim_enable_kernel_timing(amr_sim* s, int enable);
 int amr_sim_kernel_timing(amr_sim* s, double* ms, uint64_t* launches);
+
+/* ---------------------------------------------------------------- evolution
+ * The physics the reference's BSSN plugin stops short of (it recomputes metric derivatives and
+ * Christoffel symbols only, BSSN.h:143-159, and its one time integrator is SimpleWave's two-stage
+ * update, SimpleWave.h:7-46): the full BSSN system in moving-puncture form and the scalar wave
+ * u_tt = Δu, both with RK4 on the reference's octree, 2:1 subcycling driven by the same
+ * 0..2^max_depth-1 counter (AMR.h:180-188, 634-644), ghost cells filled from coarser-or-equal
+ * neighbours with space and time interpolation (AMR.h:701-762; edges and corners included here)
+ * and restriction of children into parents (AMR.h:961-996).  Simulations of these kinds use the
+ * amr_sim_* entry points above (create, add / remove nodes, timestep, buffers, save / load).
+ * Compiled for padding_domain 3 and size_domain 8, 16 or 32.  No counterpart in the reference. */
+#define AMR_SIM_BSSN_EVOLVE 3   /* 24 fields: chi, gt_ij (6), K, At_ij (6), Gt^i (3), alpha, beta^i (3), B^i (3) */
+#define AMR_SIM_WAVE_RK4 4      /* 2 fields: u, v = u_t */
+#define AMR_SLICING_1PLUSLOG 0  /* d_t alpha = beta.d alpha - 2 alpha K */
+#define AMR_SLICING_HARMONIC 1  /* d_t alpha = beta.d alpha - alpha^2 K */
+typedef struct amr_evolution {
+    int slicing;        /* AMR_SLICING_* */
+    int shift;          /* 0: shift frozen at its initial value (zero), 1: Gamma-driver */
+    float eta;          /* Gamma-driver damping (e.g. 2) */
+    float ko_sigma;     /* Kreiss-Oliger dissipation strength (e.g. 0.1; 0 turns it off) */
+    float cfl;          /* dt = cfl * dx at every depth (e.g. 0.25) */
+    int periodic;       /* 1: the root is periodic (opposite faces are neighbours) */
+} amr_evolution;
+#define AMR_ID_FLAT 0
+#define AMR_ID_GAUGE_WAVE 1       /* alpha^2 = gamma_xx = 1 - A sin(2 pi x / d) (Alcubierre et al. 2004) */
+#define AMR_ID_BRILL_LINDQUIST 2  /* psi = 1 + sum m_a / (2 r_a), chi = psi^-4, alpha = psi^-2 */
+#define AMR_ID_GAUSSIAN_PULSE 3   /* wave: u = exp(-|x|^2 / width^2), u_t = 0 */
+typedef struct amr_initial_data {
+    int kind;                 /* AMR_ID_* */
+    float amplitude;          /* gauge wave A */
+    float wavelength;         /* gauge wave d */
+    int n_punctures;          /* Brill-Lindquist: up to 4 */
+    float mass[4];
+    float position[4][3];     /* in the coordinates of the root, which spans [-outer_size/2, outer_size/2]^3 */
+    float width;              /* Gaussian pulse */
+} amr_initial_data;
+/* Set the physics and gauge of an AMR_SIM_BSSN_EVOLVE / AMR_SIM_WAVE_RK4 simulation. */
+int amr_sim_set_evolution(amr_sim* s, const amr_evolution* e);
+/* Write analytic initial data into every cell (ghosts included) of both state buffers of every live
+ * slot; the counter is reset to 0.  Build the octree first. */
+int amr_sim_initial_data(amr_sim* s, const amr_initial_data* d);
+/* Hamiltonian and momentum constraints of the current state over the composite grid (every interior
+ * cell that no child covers), leaving out cells closer than excision_radius to a puncture of the
+ * initial data (0: none), reduced in double precision with a fixed order:
+ * out5 = {rms H, max |H|, rms |M|, max |M|, cells} (|M| the Euclidean norm of M_i).  The constraint
+ * fields themselves are amr_sim_buffer(4, 0..3).  Synchronises the simulation's stream.  BSSN only. */
+int amr_sim_constraint_norms(amr_sim* s, float excision_radius, double* out5);
 
 /* ---------------------------------------------------------------- scan and reductions
  * The reference's general-purpose device algorithms (AdaptiveMesh/parallel.h) on a device array

@@ -120,6 +120,31 @@ void orc_bssn_timestep_f64(const orc_cfg* c, double* const* old6, double* const*
                            const int32_t* children, const uint64_t* boundaries, uint32_t used, uint32_t max_depth,
                            uint32_t* timer);
 
+/* ---- the evolution (oracle/bssn_evolve.c): the full BSSN system and the scalar wave, RK4 on the octree
+ * with 2:1 subcycling, in double precision -- the FP64 host oracle of the GPU evolutions.  No
+ * counterpart in the reference ("parity unpinned by the reference"). */
+typedef struct {
+    uint32_t n, p;          /* size_domain, padding_domain (3) */
+    float outer_size;       /* root edge */
+    int physics;            /* 0 BSSN, 1 scalar wave */
+    int slicing;            /* 0: 1+log, 1: harmonic */
+    int shift;              /* 0: frozen, 1: Gamma-driver */
+    float eta, ko_sigma, cfl, chi_floor;
+    int id_kind;            /* 0 flat, 1 gauge wave, 2 Brill-Lindquist, 3 Gaussian pulse */
+    float amplitude, wavelength;
+    int n_punctures;
+    float mass[4];
+    float pos[4][3];
+    float width;
+} orc_evo;
+void orc_evo_initial_data(const orc_evo* e, double* const* fields, const uint32_t* positions, uint32_t used);
+void orc_evo_timestep(const orc_evo* e, double* const* oldf, double* const* newf, double* const* stagef,
+                      double* const* acc, const uint32_t* positions, const int32_t* children,
+                      const uint64_t* boundaries, uint32_t used, uint32_t max_depth, uint32_t* timer);
+void orc_evo_constraints(const orc_evo* e, double* const* fields, const uint32_t* positions, const int32_t* children,
+                         uint32_t used, double excision, double* const* cons4, double* out5);
+void orc_periodic_boundaries(const uint32_t* positions, const int32_t* children, uint32_t used, uint64_t* out);
+
 /* parallel.h:10-82, 215-251, 385-421 -- the reference's scan and reductions over `n` elements of
  * `ncomp` values; dtype 0 uint32, 1 int32, 2 float32 (flushing subnormals as the device build).
  * The array ends as the reference leaves it; orc_extreme writes the result to `result`. */

@@ -13,7 +13,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liborc.so")
-SRC = [os.path.join(HERE, "amr_oracle.c"), os.path.join(HERE, "fp64_path.c"), os.path.join(HERE, "amr_oracle.h")]
+SRC = [os.path.join(HERE, "amr_oracle.c"), os.path.join(HERE, "fp64_path.c"), os.path.join(HERE, "bssn_evolve.c"),
+       os.path.join(HERE, "amr_oracle.h")]
 
 FUSED_NOISE = 1
 FTZ = 2
@@ -25,6 +26,16 @@ VP = ctypes.c_void_p
 U32 = ctypes.c_uint32
 I32 = ctypes.c_int32
 I64 = ctypes.c_int64
+
+
+class Evo(ctypes.Structure):
+    """orc_evo: physics, gauge and initial data of the evolution oracle."""
+    _fields_ = [("n", U32), ("p", U32), ("outer_size", ctypes.c_float), ("physics", ctypes.c_int),
+                ("slicing", ctypes.c_int), ("shift", ctypes.c_int), ("eta", ctypes.c_float),
+                ("ko_sigma", ctypes.c_float), ("cfl", ctypes.c_float), ("chi_floor", ctypes.c_float),
+                ("id_kind", ctypes.c_int), ("amplitude", ctypes.c_float), ("wavelength", ctypes.c_float),
+                ("n_punctures", ctypes.c_int), ("mass", ctypes.c_float * 4), ("pos", (ctypes.c_float * 3) * 4),
+                ("width", ctypes.c_float)]
 
 
 class Cfg(ctypes.Structure):
@@ -65,6 +76,10 @@ _SIGS = {
     "orc_differentiate_f64": (None, [VP, VP, VP, VP, VP, VP, U32]),
     "orc_bssn_timestep": (None, [VP, VP, VP, VP, VP, VP, VP, VP, VP, U32, U32, VP, VP, U32, U32]),
     "orc_bssn_timestep_f64": (None, [VP, VP, VP, VP, VP, VP, VP, VP, VP, U32, U32, VP]),
+    "orc_evo_initial_data": (None, [VP, VP, VP, U32]),
+    "orc_evo_timestep": (None, [VP, VP, VP, VP, VP, VP, VP, VP, U32, U32, VP]),
+    "orc_evo_constraints": (None, [VP, VP, VP, VP, U32, ctypes.c_double, VP, VP]),
+    "orc_periodic_boundaries": (None, [VP, VP, U32, VP]),
     "orc_num_threads": (ctypes.c_int, []),
     "orc_set_num_threads": (None, [ctypes.c_int]),
 }
@@ -78,7 +93,7 @@ def build() -> str:
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
-           "-o", LIB + ".tmp", SRC[0], SRC[1], "-lm"]
+           "-o", LIB + ".tmp", *SRC[:-1], "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(LIB + ".tmp", LIB)
     return LIB
