@@ -28,6 +28,8 @@ SLICING_1PLUSLOG, SLICING_HARMONIC = 0, 1
 ID_FLAT, ID_GAUGE_WAVE, ID_BRILL_LINDQUIST, ID_GAUSSIAN_PULSE = 0, 1, 2, 3
 # BSSN evolution fields (amr_sim_buffer components)
 F_CHI, F_GXX, F_K, F_AXX, F_GAMX, F_ALPHA, F_BETAX, F_BX = 0, 1, 7, 8, 14, 17, 18, 21
+# the BSSN evolution stores these fields less 1 (chi, gt_xx, gt_yy, gt_zz, alpha)
+BSSN_OFFSETS = tuple(1.0 if f in (0, 1, 4, 6, 17) else 0.0 for f in range(24))
 DTYPE_UINT32, DTYPE_INT32, DTYPE_FLOAT32 = 0, 1, 2
 MODE_PLAIN, MODE_BATCHED, MODE_GRAPH = 0, 1, 2
 # the plugin interface's phases, in the order of the reference's timestep loop (AMR.h:324-333)

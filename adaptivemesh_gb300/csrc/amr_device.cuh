@@ -41,10 +41,13 @@ __device__ __forceinline__ int32_t prng_next(int32_t& s) {
 // exactly 2^-32, so generate_float() is an exact power-of-two scaling of the converted integer
 // (nonzero results are at least 2^-32, far from the subnormal range) and the two products round
 // once: as the single product by 0.95f * 2^-32, which is exact as a float constant.
+constexpr float kNoiseScale = 0.95f * 0x1p-32f;
 __device__ __forceinline__ float prng_noise(int32_t& s) {
-    constexpr float kScale = 0.95f * 0x1p-32f;
-    return __fmul_rn(__int2float_rn(prng_next(s)), kScale);
+    return __fmul_rn(__int2float_rn(prng_next(s)), kNoiseScale);
 }
+// The draw itself as a float (generate_float() / 2^-32, exact): the stencil kernels' encoder adds
+// the noise with one fused multiply-add of it by 0.95f * 2^-32 (below).
+__device__ __forceinline__ float prng_noise_raw(int32_t& s) { return __int2float_rn(prng_next(s)); }
 // Per-cell generator of the stencil kernels, keyed by (launch seed, x, y, slot*N + z)
 // (AMR.h:1160-1162, BSSN.h:64-66):
 //   s = seed + x*2178614;  s ^= next(s) * y;  s ^= next(s) * zg
@@ -101,19 +104,28 @@ struct Cf3Quantised {
     float3 value;   // the decoded value of `word`
 };
 // word = E<<27 | s3<<26 | m3<<18 | s2<<17 | m2<<9 | s1<<8 | m1 ;  value_i = (1 - 2 s_i) m_i 2^(E-22)
-template <bool STOCHASTIC, bool WANT_VALUE>
+// The reference's device build adds the noise in two ways (pinned on a GB300 against its own
+// kernels): its standalone encoder rounds the noise product first (ROUNDED_NOISE, the codec entry
+// point), while the encodes inlined into its stencil and Christoffel kernels fuse the product into
+// the add, x * scale + draw * 0.95f as one fused multiply-add (the default).
+template <bool STOCHASTIC, bool WANT_VALUE, bool ROUNDED_NOISE = false>
 __device__ __forceinline__ Cf3Quantised cf3_encode_impl(float x, float y, float z, int32_t& rng) {
     const uint32_t E = min(max(max_exponent3(x, y, z), 112u) - 112u, 31u);
     const float scale = __uint_as_float((149u - E) << 23);          // 2^(22-E), exact
-    if (STOCHASTIC) {
-        // The noise product is rounded before it is added (not fused).  x * scale is exact (a
-        // power-of-two scaling), so one fused multiply-add gives the reference's rounded sum
-        // x * scale + noise, except where x * scale is subnormal: flushed first, it leaves the
-        // sum +0, while fused it can leave -0 (when the noise is 0); the field below reads |v| and
-        // (v < 0) only, the same for both zeros.
+    if (STOCHASTIC && ROUNDED_NOISE) {
+        // The noise product rounded before it is added.  x * scale is exact (a power-of-two
+        // scaling), so one fused multiply-add gives the reference's rounded sum x * scale + noise,
+        // except where x * scale is subnormal: flushed first, it leaves the sum +0, while fused it
+        // can leave -0 (when the noise is 0); the field below reads |v| and (v < 0) only, the same
+        // for both zeros.
         x = __fmaf_rn(x, scale, prng_noise(rng));
         y = __fmaf_rn(y, scale, prng_noise(rng));
         z = __fmaf_rn(z, scale, prng_noise(rng));
+    } else if (STOCHASTIC) {
+        // x * scale (exact, flushed if subnormal) + draw * 0.95 * 2^-32 rounded once
+        x = __fmaf_rn(prng_noise_raw(rng), kNoiseScale, __fmul_rn(x, scale));
+        y = __fmaf_rn(prng_noise_raw(rng), kNoiseScale, __fmul_rn(y, scale));
+        z = __fmaf_rn(prng_noise_raw(rng), kNoiseScale, __fmul_rn(z, scale));
     } else {
         x = __fmul_rn(x, scale);
         y = __fmul_rn(y, scale);
@@ -134,6 +146,10 @@ __device__ __forceinline__ Cf3Quantised cf3_encode_impl(float x, float y, float 
 __device__ __forceinline__ uint32_t cf3_encode(float x, float y, float z, int32_t& rng) {
     return cf3_encode_impl<true, false>(x, y, z, rng).word;
 }
+// The reference's standalone encoder (compressed_float3(float3, fast_prng&) in its own kernel).
+__device__ __forceinline__ uint32_t cf3_encode_codec(float x, float y, float z, int32_t& rng) {
+    return cf3_encode_impl<true, false, true>(x, y, z, rng).word;
+}
 // Encode and also return the decoded (quantised) value, as a consumer reading the word back sees it.
 __device__ __forceinline__ Cf3Quantised cf3_encode_quantised(float x, float y, float z, int32_t& rng) {
     return cf3_encode_impl<true, true>(x, y, z, rng);
@@ -145,14 +161,13 @@ __device__ __forceinline__ uint32_t cf3_encode_det(float x, float y, float z) {
 // ------------------------------------------------------------------ the encoder on pairs
 // Two independent stochastic encodes (lanes x and y) with their floating-point steps done as
 // packed pairs; each lane is cf3_encode_impl<true, WANT_VALUE> bit for bit.  The noise pairs
-// (nx, ny, nz) are the lanes' three draws in the order the scalar encoder takes them (x, y, z).
+// (nx, ny, nz) are the lanes' three draws (unscaled) in the order the scalar encoder takes them.
 struct Cf3Pair {
     uint32_t w0, w1;        // the words of lanes x and y
     float2 vx, vy, vz;      // WANT_VALUE: the decoded components (lane x of each: the first word)
 };
-__device__ __forceinline__ float2 noise_pair(int32_t s0, int32_t s1) {
-    constexpr float kScale = 0.95f * 0x1p-32f;   // as prng_noise
-    return mul2(make_float2(__int2float_rn(s0), __int2float_rn(s1)), splat2(kScale));
+__device__ __forceinline__ float2 noise_pair(int32_t s0, int32_t s1) {   // the draws, unscaled
+    return make_float2(__int2float_rn(s0), __int2float_rn(s1));
 }
 // Noise pairs of two generators, one per lane.
 __device__ __forceinline__ void noise_pairs2(int32_t& r0, int32_t& r1, float2& nx, float2& ny, float2& nz) {
@@ -185,9 +200,10 @@ __device__ __forceinline__ Cf3Pair cf3_encode2(float2 x, float2 y, float2 z, flo
     const uint32_t E0 = min(max(max_exponent3(x.x, y.x, z.x), 112u) - 112u, 31u);
     const uint32_t E1 = min(max(max_exponent3(x.y, y.y, z.y), 112u) - 112u, 31u);
     const float2 scale = make_float2(__uint_as_float((149u - E0) << 23), __uint_as_float((149u - E1) << 23));
-    x = fma2(x, scale, nx);
-    y = fma2(y, scale, ny);
-    z = fma2(z, scale, nz);
+    // x * scale (exact) + draw * 0.95 * 2^-32, one rounding (the stencil kernels' fused noise)
+    x = fma2(nx, splat2(kNoiseScale), mul2(x, scale));
+    y = fma2(ny, splat2(kNoiseScale), mul2(y, scale));
+    z = fma2(nz, splat2(kNoiseScale), mul2(z, scale));
     const Cf3Field2 fx = cf3_field2(x), fy = cf3_field2(y), fz = cf3_field2(z);
     Cf3Pair r;
     r.w0 = (E0 << 27) + (__float_as_uint(fx.bits.x) & 511u) + __float_as_uint(fy.bits.x) * 512u +

@@ -8,23 +8,28 @@
 //
 // Scheme, per substep (the reference's counter; the domains active at it advance one step of
 // their own dt = cfl * dx):
-//   restriction   old <- new of every active domain, cells covered by a child <- mean of its 2x2x2
-//   RK4           four stages over every active evolved domain (a domain is evolved unless its
-//                 eight children cover it): derivative pass, then pointwise right-hand side and
-//                 stage update; the ghost cells of each stage's state and of the final state are
-//                 filled from the neighbours (three passes, x then y then z, so that edges and
-//                 corners are filled too)
+//   restriction   old <- new of every active domain; a cell covered by a child <- the child's state
+//                 at the cell's centre by the 4-point midpoint rule along each axis (fourth order;
+//                 the reference's 2x2x2 mean, AMR.h:961-996, is second order)
+//   RK4           four stages over every active domain (covered parents included: a same-depth
+//                 neighbour of a covered parent takes its ghost values from it at every stage):
+//                 derivative pass, then pointwise right-hand side and stage update; the ghost cells
+//                 of each stage's state and of the final state are filled from the neighbours
+//                 (three passes, x then y then z, so that edges and corners are filled too)
 //   ghost values  same-depth neighbour: its state at the same stage; coarser neighbour active at
 //                 this substep: old + (its stage state - old) * 2^-Δdepth; coarser neighbour in the
-//                 middle of its step: old + (new - old) * (k' + c_stage) / 2^Δdepth; a neighbour
-//                 that is not evolved (the root at the outer boundary): its old state.  Space
-//                 interpolation is the reference's 10-point quadratic-plus-cross rule
-//                 (AMR.h:672-699) for coarser neighbours and a copy for same-depth ones.
+//                 middle of its step: old + (new - old) * (k' + c_stage) / 2^Δdepth.  Space
+//                 interpolation from a coarser neighbour is tricubic (the reference's 10-point
+//                 quadratic rule, AMR.h:672-699, leaves O(h^3) ghost errors that second-derivative
+//                 stencils turn into O(h)); same-depth values are copied.  The root's ghost layer
+//                 keeps the initial data (the outer boundary) unless the root is periodic.
 // Finite differences: 4th-order centred first and second derivatives (mixed ones as the product of
 // first-derivative stencils), 6th-derivative Kreiss-Oliger dissipation (3 ghost cells needed).
 #pragma once
 
 #include <cstdint>
+
+#include <cuda_runtime.h>
 
 #include "amr_types.h"
 
@@ -42,6 +47,15 @@ enum BssnField : int {
     F_BX = 21, F_BY, F_BZ,        // Gamma-driver auxiliary
     BSSN_NF = 24
 };
+// The BSSN fields are stored as their deviation from flat space: chi, the conformal metric's
+// diagonal and the lapse less 1.  Derivatives, interpolation, restriction and the RK update are the
+// same for both forms (the offsets are constants), but single-precision rounding then acts on the
+// deviation (for a weak field ~1e-2 of the value), which lowers the rounding noise that second
+// derivatives amplify by 1/dx^2 by the same factor.
+__host__ __device__ constexpr float bssn_offset(int f) {
+    return (f == 0 || f == 1 || f == 4 || f == 6 || f == 17) ? 1.f : 0.f;
+}
+
 // Wave equation fields: u and v = u_t.
 enum WaveField : int { W_U = 0, W_V = 1, WAVE_NF = 2 };
 

@@ -59,6 +59,12 @@ public:
         if (e == cudaSuccess) e = dev_alloc(&d_lists, s * 2u * ((size_t)1u << kDepthLimit) + 2u * s);
         if (e == cudaSuccess) e = dev_alloc(&d_part, s * 5u);
         if (e == cudaSuccess) e = dev_alloc(&d_norms, 8);
+        if (e == cudaSuccess) {   // the derivative pass's shared-memory limit, outside any stream capture
+            EvoArgs none;
+            std::memset(&none, 0, sizeof(none));
+            none.n = dims.n;
+            e = launch_evo_derivs(none, stream);
+        }
         return cuda_status(e);
     }
 

@@ -52,9 +52,10 @@ __global__ void k_evo_init(EvoInitArgs a) {
     float u[kMaxFields];
     evo_initial_values(a.id, a.physics, x, u);
     for (int f = 0; f < a.nf; f++) {
-        a.out1[f][gid] = u[f];
-        a.out2[f][gid] = u[f];
-        a.out3[f][gid] = u[f];
+        const float v = a.physics == 0 ? u[f] - bssn_offset(f) : u[f];   // stored as the deviation
+        a.out1[f][gid] = v;
+        a.out2[f][gid] = v;
+        a.out3[f][gid] = v;
     }
 }
 
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(128) k_evo_rhs_bssn(const __grid_constant__ Ev
     const uint64_t ii = (uint64_t)slot * N * N * N + cell;
     float u[BSSN_NF];
 #pragma unroll
-    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi];
+    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi] + bssn_offset(f);
     const float* D = a.deriv;
     const uint64_t ds = a.deriv_stride;
     auto dv = [&](int k) { return D[(uint64_t)k * ds + ii]; };
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(128) k_evo_rhs_bssn(const __grid_constant__ Ev
 #pragma unroll 1
     for (int f = 0; f < BSSN_NF; f++) {
         const float r = rhs[f] + dv(D_EXTRA + f);
-        const float uo = a.stage == 1 ? u[f] : a.old_f[f][pi];
+        const float uo = a.stage == 1 ? a.fields[f][pi] : a.old_f[f][pi];   // the stored form
         rk_update(a, f, pi, ii, uo, r, dt);
     }
 }
@@ -447,7 +448,7 @@ __global__ void __launch_bounds__(128) k_evo_constraints(const __grid_constant__
     const uint64_t ii = (uint64_t)slot * N * N * N + cell;
     float u[BSSN_NF];
 #pragma unroll
-    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi];
+    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi] + bssn_offset(f);
     const float* D = a.deriv;
     const uint64_t ds = a.deriv_stride;
     auto dv = [&](int k) { return D[(uint64_t)k * ds + ii]; };

@@ -45,7 +45,7 @@ __global__ void k_cf3_encode(const float* __restrict__ xyz, const int32_t* __res
     const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
     if (seeds) {
         int32_t s = seeds[i];
-        out[i] = cf3_encode(x, y, z, s);
+        out[i] = cf3_encode_codec(x, y, z, s);
     } else {
         out[i] = cf3_encode_det(x, y, z);
     }

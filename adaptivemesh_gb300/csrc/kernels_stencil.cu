@@ -617,7 +617,10 @@ __global__ void __launch_bounds__(StencilShape<N, P, SK_BSSN>::THREADS, StencilS
                 const uint32_t sq = g + j;
                 ok &= mbar_wait(&full[sq % R], (sq / R) & 1u, spins);
             }
-            if (!ok) s_abort = 1;
+            if (!ok) {   // this warp's wait gave up: report it (the producer may have nothing left to wait for)
+                s_abort = 1;
+                if (lane == 0) atomicExch(a.err, 1);
+            }
             if (s_abort) { bulk_wait(); return; }
             const uint32_t base_s = g % R;
             uint32_t slot[2 * P + 1];

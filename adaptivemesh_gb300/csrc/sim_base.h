@@ -67,8 +67,9 @@ public:
         if (e == cudaSuccess) e = dev_alloc(&d_boundaries, (size_t)s * 6u);
         if (e == cudaSuccess) e = dev_alloc(&d_items, (size_t)s << (kDepthLimit + 1));   // active and parent lists
         if (e == cudaSuccess) { err_flag = device_error_flag(); if (!err_flag) e = cudaErrorMemoryAllocation; }
-        if (e == cudaSuccess) {
-            // set the kernels' shared-memory limits now, outside any later stream capture
+        if (e == cudaSuccess && config_supported(&cfg)) {
+            // set the kernels' shared-memory limits now, outside any later stream capture (the
+            // evolutions, whose sizes these kernels need not support, set their own)
             StencilArgs none;
             std::memset(&none, 0, sizeof(none));
             for (int kind : {SK_GRAD, SK_GRAD_HESS, SK_MIXED, SK_BSSN}) {

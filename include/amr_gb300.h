@@ -340,6 +340,12 @@ int amr_sim_kernel_timing(amr_sim* s, double* ms, uint64_t* launches);
  * Compiled for padding_domain 3 and size_domain 8, 16 or 32.  No counterpart in the reference. */
 #define AMR_SIM_BSSN_EVOLVE 3   /* 24 fields: chi, gt_ij (6), K, At_ij (6), Gt^i (3), alpha, beta^i (3), B^i (3) */
 #define AMR_SIM_WAVE_RK4 4      /* 2 fields: u, v = u_t */
+/* Buffers of these simulations (amr_sim_buffer, comp = field): which 0 the state at the start of
+ * the current step (padded), 1 the latest state (padded), 2 the RK stage state (padded), 3 the RK
+ * accumulator (inner layout), 4 the constraints H, M_x, M_y, M_z (inner layout, comp 0..3, written
+ * by amr_sim_constraint_norms), 5 derivative scratch planes (inner layout).  The BSSN fields chi,
+ * gt_xx, gt_yy, gt_zz and alpha are stored less 1 (their deviation from flat space), which keeps
+ * single-precision rounding relative to the deviation. */
 #define AMR_SLICING_1PLUSLOG 0  /* d_t alpha = beta.d alpha - 2 alpha K */
 #define AMR_SLICING_HARMONIC 1  /* d_t alpha = beta.d alpha - alpha^2 K */
 typedef struct amr_evolution {

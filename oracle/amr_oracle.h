@@ -33,9 +33,11 @@ typedef struct {
 } orc_cfg;
 
 /* ORC_FUSED_NOISE: the stochastic codec adds its noise with one fused multiply-add instead of
- *                  a rounded product then a sum.  Both builds of the reference round the
- *                  product (pinned on the device by tests/golden/codec_fused_probe_inputs.npz);
- *                  the flag exists to show that the distinction is observable.
+ *                  a rounded product then a sum.  The reference's host build and its device
+ *                  build's standalone encoder round the product (pinned on the device by
+ *                  tests/golden/codec_fused_probe_inputs.npz); the encodes its device build
+ *                  inlines into the stencil and Christoffel kernels fuse it (pinned against its
+ *                  BSSN plugin on the 585-domain tree), so the kernel restatements run with it.
  * ORC_FTZ:         flush subnormal inputs/results of the codec to zero (device build). */
 #define ORC_FUSED_NOISE 1u
 #define ORC_FTZ 2u

@@ -18,8 +18,12 @@ SRC = [os.path.join(HERE, "amr_oracle.c"), os.path.join(HERE, "fp64_path.c"), os
 
 FUSED_NOISE = 1
 FTZ = 2
-DEVICE_FLAGS = FTZ                 # the reference's device build (fast-math: flush-to-zero; its
-                                   # noise product is rounded before the add, see test_codec_noise_rounding)
+DEVICE_FLAGS = FTZ                 # the reference's device build, its standalone encoder (fast-math:
+                                   # flush-to-zero; the noise product is rounded before the add, see
+                                   # test_codec_noise_rounding)
+STENCIL_FLAGS = FTZ | FUSED_NOISE  # the encodes inlined into its stencil and Christoffel kernels: the
+                                   # noise product is fused into the add (pinned against the reference's
+                                   # plugin on a GB300: tests/test_gpu_workload.py)
 HOST_FLAGS = 0                     # the reference's host build (no contraction, no flush)
 
 VP = ctypes.c_void_p
@@ -126,7 +130,7 @@ def ptrs(arrs) -> ctypes.Array:
     return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
 
 
-def cfg(n: int, p: int, outer_size: float = 100.0, flags: int = DEVICE_FLAGS, inv_dx=None) -> Cfg:
+def cfg(n: int, p: int, outer_size: float = 100.0, flags: int = STENCIL_FLAGS, inv_dx=None) -> Cfg:
     c = Cfg()
     lib().orc_cfg_init(ctypes.byref(c), n, p, outer_size, flags)
     if inv_dx is not None:
