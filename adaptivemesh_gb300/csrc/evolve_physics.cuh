@@ -58,46 +58,48 @@ __device__ __forceinline__ void inverse_sym(const float* g, float gi[3][3]) {
 }
 
 // ------------------------------------------------------------------ initial data at a point
-__device__ __forceinline__ void evo_initial_values(const InitData& id, int physics, const float* x, float* u) {
+// In double precision (a one-off cost): the stored deviations from flat space (evolve.h) are then
+// rounded once, instead of carrying the float rounding of the values near 1.
+__device__ __forceinline__ void evo_initial_values(const InitData& id, int physics, const double* x, double* u) {
     if (physics != 0) {   // scalar wave: Gaussian pulse at rest
-        const float r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
-        u[W_U] = id.kind == AMR_ID_GAUSSIAN_PULSE ? expf(-r2 / (id.width * id.width)) : 0.f;
-        u[W_V] = 0.f;
+        const double r2 = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
+        u[W_U] = id.kind == AMR_ID_GAUSSIAN_PULSE ? exp(-r2 / ((double)id.width * id.width)) : 0.0;
+        u[W_V] = 0.0;
         return;
     }
-    for (int f = 0; f < BSSN_NF; f++) u[f] = 0.f;
-    u[F_CHI] = 1.f;
-    u[F_GXX] = u[F_GYY] = u[F_GZZ] = 1.f;
-    u[F_ALPHA] = 1.f;
+    for (int f = 0; f < BSSN_NF; f++) u[f] = 0.0;
+    u[F_CHI] = 1.0;
+    u[F_GXX] = u[F_GYY] = u[F_GZZ] = 1.0;
+    u[F_ALPHA] = 1.0;
     if (id.kind == AMR_ID_GAUGE_WAVE) {
         // ds^2 = -H dt^2 + H dx^2 + dy^2 + dz^2, H = 1 - A sin(2 pi (x - t) / d), at t = 0
-        const float k = 6.283185307179586f / id.wavelength;
-        const float sn = sinf(k * x[0]), cs = cosf(k * x[0]);
-        const float H = 1.f - id.amplitude * sn;
-        const float dH = -id.amplitude * k * cs;                 // d_x H
-        const float sq = sqrtf(H);
-        const float Kxx = -0.5f * id.amplitude * k * cs / sq;   // -d_t gamma_xx / (2 alpha)
-        const float chi = 1.f / cbrtf(H);
-        const float K = Kxx / H;
+        const double A = id.amplitude, k = 6.283185307179586476925 / id.wavelength;
+        const double sn = sin(k * x[0]), cs = cos(k * x[0]);
+        const double H = 1.0 - A * sn;
+        const double dH = -A * k * cs;                       // d_x H
+        const double sq = sqrt(H);
+        const double Kxx = -0.5 * A * k * cs / sq;           // -d_t gamma_xx / (2 alpha)
+        const double chi = 1.0 / cbrt(H);
+        const double K = Kxx / H;
         u[F_CHI] = chi;
         u[F_GXX] = chi * H;
         u[F_GYY] = u[F_GZZ] = chi;
         u[F_K] = K;
-        u[F_AXX] = chi * (Kxx - H * K / 3.f);
-        u[F_AYY] = u[F_AZZ] = -chi * K / 3.f;
-        u[F_GAMX] = (2.f / 3.f) * dH / (H * cbrtf(H * H));      // -d_x (H^(-2/3))
+        u[F_AXX] = chi * (Kxx - H * K / 3.0);
+        u[F_AYY] = u[F_AZZ] = -chi * K / 3.0;
+        u[F_GAMX] = (2.0 / 3.0) * dH / (H * cbrt(H * H));    // -d_x (H^(-2/3))
         u[F_ALPHA] = sq;
     } else if (id.kind == AMR_ID_BRILL_LINDQUIST) {
         // psi = 1 + sum m_a / (2 r_a); chi = psi^-4, conformally flat, K_ij = 0, lapse psi^-2
-        float psi = 1.f;
+        double psi = 1.0;
         for (int a = 0; a < id.n_punctures && a < 4; a++) {
-            const float dx = x[0] - id.pos[a][0], dy = x[1] - id.pos[a][1], dz = x[2] - id.pos[a][2];
-            const float r = fmaxf(sqrtf(dx * dx + dy * dy + dz * dz), 1e-6f);
-            psi += id.mass[a] / (2.f * r);
+            const double dx = x[0] - id.pos[a][0], dy = x[1] - id.pos[a][1], dz = x[2] - id.pos[a][2];
+            const double r = fmax(sqrt(dx * dx + dy * dy + dz * dz), 1e-6);
+            psi += id.mass[a] / (2.0 * r);
         }
-        const float p2 = psi * psi;
-        u[F_CHI] = 1.f / (p2 * p2);
-        u[F_ALPHA] = 1.f / p2;
+        const double p2 = psi * psi;
+        u[F_CHI] = 1.0 / (p2 * p2);
+        u[F_ALPHA] = 1.0 / p2;
     }
 }
 

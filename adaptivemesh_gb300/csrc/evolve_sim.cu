@@ -10,6 +10,8 @@
 //                 pointwise update, with the ghost cells of stages 2-4 filled in between
 //   copy_bounds   ghost fill of the final state (so that the next restriction copies valid ghosts)
 //   corrector     nothing (RK4 has no separate corrector stage)
+// Modes: PLAIN launches every kernel once per domain (the plain per-domain form), BATCHED once per
+// phase over the substep's active domains, GRAPH replays a captured CUDA graph of a whole timestep.
 // Buffers per field: old (state at the start of a step), new (final state; also the stage-3 input),
 // stage (stages 2 and 4), all padded; the RK accumulator (inner layout).
 #include <algorithm>
@@ -173,6 +175,15 @@ public:
         g.n = dims.n; g.p = dims.p; g.t = dims.t;
         g.nf = nf;
         (void)md;
+        if (mode == AMR_MODE_PLAIN) {   // one launch per domain
+            const uint32_t* base = g.items;
+            for (uint32_t i = 0; i < act_cnt[s]; i++) {
+                g.items = base + i;
+                g.n_items = 1;
+                if ((st = check(launch_evo_restrict(g, stream)))) return st;
+            }
+            return AMR_OK;
+        }
         return check(launch_evo_restrict(g, stream));
     }
     int modify_nodes() override { return AMR_OK; }
@@ -186,10 +197,20 @@ public:
         const float c_next[3] = {.5f, .5f, 1.f};
         for (int stage = 1; stage <= 4; stage++) {
             EvoArgs a = args(s, in[stage - 1], out[stage - 1], stage, 0);
-            if ((st = check(launch_evo_derivs(a, stream)))) return st;
-            time_begin();
-            if ((st = check(launch_evo_rhs(a, stream)))) return st;
-            time_end();
+            if (mode == AMR_MODE_PLAIN) {
+                // the plain per-domain form: each domain's derivative pass and update launched alone
+                const uint32_t* base = a.items;
+                for (uint32_t i = 0; i < evo_cnt[s]; i++) {
+                    a.items = base + i;
+                    a.n_items = 1;
+                    if ((st = check(launch_evo_derivs(a, stream))) || (st = check(launch_evo_rhs(a, stream)))) return st;
+                }
+            } else {
+                if ((st = check(launch_evo_derivs(a, stream)))) return st;
+                time_begin();
+                if ((st = check(launch_evo_rhs(a, stream)))) return st;
+                time_end();
+            }
             if (stage < 4 && (st = fill(s, out[stage - 1], c_next[stage - 1]))) return st;
         }
         return AMR_OK;
@@ -346,8 +367,18 @@ private:
         g.max_depth = (uint32_t)tree.read_max_depth();
         g.nf = nf;
         g.c_stage = c_stage;
-        for (int axis = 0; axis < 3; axis++) {
+        for (int axis = 0; axis < 3; axis++) {   // every domain's pass along an axis before the next axis
             g.axis = axis;
+            if (mode == AMR_MODE_PLAIN) {   // one launch per domain
+                const uint32_t* base = d_lists + evo_off[s];
+                for (uint32_t i = 0; i < evo_cnt[s]; i++) {
+                    g.items = base + i;
+                    g.n_items = 1;
+                    const int st = check(launch_evo_ghost(g, stream));
+                    if (st) return st;
+                }
+                continue;
+            }
             const int st = check(launch_evo_ghost(g, stream));
             if (st) return st;
         }

@@ -44,15 +44,15 @@ __global__ void k_evo_init(EvoInitArgs a) {
     const int depth = pos_depth(pos);
     if (depth == -1) return;
     float ctr[3];
-    slot_centre(pos, ctr);
-    const float h = a.outer_size / ((float)a.n * (float)(1u << depth));
+    slot_centre(pos, ctr);   // exact: sums of powers of two
+    const double h = (double)a.outer_size / ((double)a.n * (double)(1u << depth));
     const uint32_t idx[3] = {c % t, (c / t) % t, c / (t * t)};
-    float x[3];
-    for (int k = 0; k < 3; k++) x[k] = ctr[k] * a.outer_size + ((float)idx[k] + .5f - .5f * (float)t) * h;
-    float u[kMaxFields];
+    double x[3];
+    for (int k = 0; k < 3; k++) x[k] = (double)ctr[k] * a.outer_size + ((double)idx[k] + .5 - .5 * (double)t) * h;
+    double u[kMaxFields];
     evo_initial_values(a.id, a.physics, x, u);
     for (int f = 0; f < a.nf; f++) {
-        const float v = a.physics == 0 ? u[f] - bssn_offset(f) : u[f];   // stored as the deviation
+        const float v = (float)(a.physics == 0 ? u[f] - bssn_offset(f) : u[f]);   // stored as the deviation
         a.out1[f][gid] = v;
         a.out2[f][gid] = v;
         a.out3[f][gid] = v;
