@@ -72,6 +72,18 @@ class Evolution(ctypes.Structure):
         super().__init__(slicing, shift, eta, ko_sigma, cfl, periodic)
 
 
+class Regrid(ctypes.Structure):
+    """amr_regrid: thresholds of the refinement decision (plain criterion and learned estimator)."""
+    _fields_ = [("refine_threshold", ctypes.c_float), ("coarsen_threshold", ctypes.c_float),
+                ("learned_refine", ctypes.c_float), ("learned_coarsen", ctypes.c_float),
+                ("judge_factor", ctypes.c_float), ("max_depth", U32), ("min_depth", U32)]
+
+    def __init__(self, refine_threshold=0.02, coarsen_threshold=0.005, learned_refine=-5.0, learned_coarsen=-6.5,
+                 judge_factor=4.0, max_depth=6, min_depth=1):
+        super().__init__(refine_threshold, coarsen_threshold, learned_refine, learned_coarsen, judge_factor,
+                         max_depth, min_depth)
+
+
 class InitialData(ctypes.Structure):
     """amr_initial_data: analytic initial data of an evolution simulation."""
     _fields_ = [("kind", ctypes.c_int), ("amplitude", ctypes.c_float), ("wavelength", ctypes.c_float),
@@ -156,6 +168,16 @@ EXPORTS = {
     "amr_sim_initial_data": (ctypes.c_int, [VP, VP]),
     "amr_sim_constraint_norms": (ctypes.c_int, [VP, ctypes.c_float, VP]),
     "amr_octree_set_periodic": (ctypes.c_int, [VP, ctypes.c_int]),
+    "amr_estimator_create": (ctypes.c_int, [U32, U64, ctypes.POINTER(VP)]),
+    "amr_estimator_destroy": (ctypes.c_int, [VP]),
+    "amr_estimator_param_count": (U64, []),
+    "amr_estimator_get_params": (ctypes.c_int, [VP, VP]),
+    "amr_estimator_set_params": (ctypes.c_int, [VP, VP]),
+    "amr_estimator_forward": (ctypes.c_int, [VP, VP, U32, VP]),
+    "amr_estimator_gradients": (ctypes.c_int, [VP, VP, VP, U32, VP, ctypes.POINTER(ctypes.c_float)]),
+    "amr_estimator_train_step": (ctypes.c_int, [VP, VP, VP, U32, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
+    "amr_sim_tile_features": (ctypes.c_int, [VP, VP, VP, VP, U32, ctypes.POINTER(U32)]),
+    "amr_sim_regrid": (ctypes.c_int, [VP, VP, VP, VP]),
     "amr_sim_enable_kernel_timing": (ctypes.c_int, [VP, ctypes.c_int]),
     "amr_sim_kernel_timing": (ctypes.c_int, [VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(U64)]),
     "amr_inclusive_scan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, VP, U64, VP]),
@@ -219,6 +241,7 @@ def _ptr_array(ts) -> ctypes.Array:
 
 from . import ops  # noqa: E402
 from .octree import Octree, Sim  # noqa: E402
+from .estimator import Estimator  # noqa: E402
 
-__all__ = ["Config", "Evolution", "InitialData", "Octree", "Sim", "ops", "load", "check", "AmrError", "LIB_PATH",
-           "EXPORTS"]
+__all__ = ["Config", "Evolution", "InitialData", "Regrid", "Octree", "Sim", "Estimator", "ops", "load", "check",
+           "AmrError", "LIB_PATH", "EXPORTS"]

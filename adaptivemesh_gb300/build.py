@@ -40,7 +40,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-fmad=false", "-ftz=true
               "-I", INCLUDE, "-I", CSRC]
 # Units without a reference build to reproduce bit for bit (the evolutions, held to an FP64 oracle
 # within stated tolerances) let the compiler contract products and sums into fused multiply-adds.
-CONTRACTED = {"kernels_evolve.cu"}
+CONTRACTED = {"kernels_evolve.cu", "estimator.cu"}
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 

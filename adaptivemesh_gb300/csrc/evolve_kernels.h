@@ -53,6 +53,30 @@ struct EvoRestrictArgs {
     int nf;
 };
 
+// Tile features of the learned estimator and the plain criterion's indicator, per listed slot
+// (kernels_evolve.cu, k_evo_features): features [slot][3][8^3], indicator [slot].
+struct EvoFeatureArgs {
+    const float* state[kMaxFields];
+    const uint32_t* positions;
+    const uint32_t* items;
+    uint32_t n_items;
+    uint32_t n, p, t;
+    float outer_size;
+    float* features;
+    float* indicator;
+};
+cudaError_t launch_evo_features(const EvoFeatureArgs& g, cudaStream_t st);
+
+// Prolongation of new domains: every padded cell of each listed child, in every buffer, by tricubic
+// interpolation of its parent's padded cells.  The items of one launch share a depth.
+struct EvoProlongArgs {
+    float* bufs[2 * kMaxFields];
+    const int32_t* items;   // (node, parent, offset) triples
+    uint32_t n_items, nbuf;
+    uint32_t n, p, t;
+};
+cudaError_t launch_evo_prolong(const EvoProlongArgs& g, cudaStream_t st);
+
 bool evo_config_supported(uint32_t n, uint32_t p);
 cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st);
 cudaError_t launch_evo_init(const EvoInitArgs& a, cudaStream_t st);

@@ -5,7 +5,8 @@
 //   copy_back     restriction of every active domain: old <- new, child-covered cells <- the child's
 //                 new field at the cell's centre, fourth order (the reference's copy_new_to_old,
 //                 AMR.h:961-996, averages the 2x2x2 cells: second order)
-//   modify_nodes  nothing (regridding is driven from outside, amr_sim_add_nodes / remove_nodes)
+//   modify_nodes  nothing (regridding is driven from outside between timesteps: amr_sim_regrid, or
+//                 amr_sim_add_nodes / remove_nodes; new domains are interpolated tricubically)
 //   predictor     the four RK4 stages over the active evolved domains, each a derivative pass and a
 //                 pointwise update, with the ghost cells of stages 2-4 filled in between
 //   copy_bounds   ghost fill of the final state (so that the next restriction copies valid ghosts)
@@ -42,6 +43,7 @@ public:
         for (int f = 0; f < kMaxFields; f++) { cudaFree(old_f[f]); cudaFree(new_f[f]); cudaFree(stage_f[f]); cudaFree(acc[f]); }
         for (float* c : cons.c) cudaFree(c);
         cudaFree(deriv); cudaFree(d_evolved); cudaFree(d_lists); cudaFree(d_part); cudaFree(d_norms);
+        cudaFree(d_feat); cudaFree(d_ind); cudaFree(d_pred);
     }
     int init() override {
         int st = SimBase::init();
@@ -70,25 +72,32 @@ public:
         return cuda_status(e);
     }
 
-    // ---- node constructors: prolongate both state buffers of every field (AMR.h:1053-1115)
+    // ---- node constructors: both state buffers of every field of a new domain by tricubic
+    // interpolation of its parent's padded state (fourth order, in place of the reference's rule,
+    // AMR.h:1053-1115, whose second-order error seeds O(1) constraint violations on refined cells)
     void node_ctor(int32_t node) override {
-        const uint32_t off = (uint32_t)pos_final_offset(tree.positions()[node]);
-        const int32_t parent = tree.parents()[node];
-        for (int f = 0; f < nf; f++) {
-            check(launch_copy_to_child(dims, old_f[f], off, node, parent, stream));
-            check(launch_copy_to_child(dims, new_f[f], off, node, parent, stream));
-        }
-        graph_valid = false;
-        lists_valid = false;
+        const NodeCtor c = {node, tree.parents()[node], (int32_t)pos_final_offset(tree.positions()[node])};
+        const uint32_t end = 1;
+        node_ctor_groups(&c, &end, 1);
     }
     void node_ctor_groups(const NodeCtor* items, const uint32_t* group_end, uint32_t groups) override {
-        float* bufs[2 * kMaxFields];
-        for (int f = 0; f < nf; f++) { bufs[f] = old_f[f]; bufs[nf + f] = new_f[f]; }
-        // the prolongation launch takes up to 12 buffers: run every group once per chunk of buffers
-        for (int b0 = 0; b0 < 2 * nf; b0 += 12)
-            prolongate_groups(items, group_end, groups, bufs + b0, std::min(12, 2 * nf - b0));
         graph_valid = false;
         lists_valid = false;
+        const size_t n = groups ? group_end[groups - 1] : 0u;
+        if (n == 0 || !upload_ctor_items(items, n)) return;
+        EvoProlongArgs g;
+        std::memset(&g, 0, sizeof(g));
+        for (int f = 0; f < nf; f++) { g.bufs[f] = old_f[f]; g.bufs[nf + f] = new_f[f]; }
+        g.nbuf = 2u * (uint32_t)nf;
+        g.n = dims.n; g.p = dims.p; g.t = dims.t;
+        cudaError_t e = cudaSuccess;
+        for (uint32_t k = 0, b = 0; k < groups && e == cudaSuccess; b = group_end[k++]) {   // depth order
+            g.items = reinterpret_cast<const int32_t*>(ctor_items + b);
+            g.n_items = group_end[k] - b;
+            e = launch_evo_prolong(g, stream);
+            launches++;
+        }
+        if (e != cudaSuccess) ctor_status = cuda_status(e);
     }
     void node_dtor(int32_t) override { lists_valid = false; }
 
@@ -327,7 +336,129 @@ public:
         return cuda_status(e);
     }
 
+    // ---- refinement (the learned estimator with the plain criterion as fallback and judge)
+    // Features and plain-criterion indicators of every leaf, in leaf order (device buffers kept).
+    int tile_features(std::vector<uint32_t>& leaf_slots) {
+        if (kind != AMR_SIM_BSSN_EVOLVE) return AMR_ERR_INVALID;
+        int st = prepare();
+        if (st) return st;
+        leaf_slots = leaves;
+        const size_t need = leaves.size();
+        if (need > feat_cap) {
+            cudaStreamSynchronize(stream);
+            cudaFree(d_feat); cudaFree(d_ind); cudaFree(d_pred);
+            d_feat = d_ind = d_pred = nullptr;
+            feat_cap = 0;
+            cudaError_t e = dev_alloc(&d_feat, need * 1536u);
+            if (e == cudaSuccess) e = dev_alloc(&d_ind, need);
+            if (e == cudaSuccess) e = dev_alloc(&d_pred, need);
+            if (e != cudaSuccess) return cuda_status(e);
+            feat_cap = need;
+        }
+        EvoFeatureArgs g;
+        std::memset(&g, 0, sizeof(g));
+        for (int f = 0; f < nf; f++) g.state[f] = new_f[f];
+        g.positions = d_positions;
+        g.items = d_lists + leaves_off;
+        g.n_items = (uint32_t)leaves.size();
+        g.n = dims.n; g.p = dims.p; g.t = dims.t;
+        g.outer_size = cfg.outer_size;
+        g.features = d_feat;
+        g.indicator = d_ind;
+        return check(launch_evo_features(g, stream));
+    }
+    int regrid(amr_estimator* est, const amr_regrid& r, uint32_t* stats) {
+        std::vector<uint32_t> leaf;
+        int st = tile_features(leaf);
+        if (st) return st;
+        const size_t nl = leaf.size();
+        std::vector<float> ind(nl), pred(nl, 0.f);
+        cudaError_t e = cudaMemcpyAsync(ind.data(), d_ind, nl * 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return cuda_status(e);
+        if (est) {
+            if ((st = amr_estimator_forward(est, d_feat, (uint32_t)nl, d_pred))) return st;
+            if ((e = cudaMemcpy(pred.data(), d_pred, nl * 4, cudaMemcpyDeviceToHost)) != cudaSuccess) return cuda_status(e);
+        }
+        // decisions per leaf: refine by the network (or the plain criterion without one); the
+        // plain criterion overrides a network that declines a tile whose indicator exceeds
+        // judge_factor times its own refinement threshold
+        const auto& pos = tree.positions();
+        const auto& ch = tree.children();
+        uint32_t refined = 0, coarsened = 0, overridden = 0;
+        std::vector<int32_t> add_p, add_o;
+        std::vector<char> calm(tree.max_slots(), 0);   // leaf whose criterion allows coarsening
+        for (size_t i = 0; i < nl; i++) {
+            const uint32_t sl = leaf[i];
+            const int d = pos_depth_host(pos[sl]);
+            const bool plain_refine = ind[i] > r.refine_threshold;
+            const bool judge = ind[i] > r.judge_factor * r.refine_threshold;
+            bool refine = est ? pred[i] > r.learned_refine : plain_refine;
+            if (est && !refine && judge) { refine = true; overridden++; }
+            calm[sl] = !refine && (est ? (pred[i] < r.learned_coarsen && !plain_refine) : ind[i] < r.coarsen_threshold);
+            if (refine && (uint32_t)d < r.max_depth) {
+                for (int c = 0; c < 8; c++) { add_p.push_back((int32_t)sl); add_o.push_back(c); }
+                refined++;
+            }
+        }
+        // coarsen: parents whose eight children are all calm leaves, above the minimum depth
+        std::vector<int32_t> rem;
+        const uint32_t used = tree.curr_used_slots();
+        for (uint32_t sl = 0; sl < used; sl++) {
+            const int d = pos_depth_host(pos[sl]);
+            if (d == -1 || (uint32_t)d < r.min_depth) continue;
+            bool all = true;
+            for (int c = 0; c < 8 && all; c++) {
+                const int32_t k = ch[(size_t)sl * 8u + c];
+                all = k != -1 && calm[k];
+                if (all)
+                    for (int cc = 0; cc < 8; cc++) all &= ch[(size_t)k * 8u + cc] == -1;
+            }
+            if (!all) continue;
+            for (int c = 0; c < 8; c++) rem.push_back(ch[(size_t)sl * 8u + c]);
+            coarsened++;
+        }
+        if (!rem.empty()) {
+            tree.begin_batch();
+            for (int32_t k : rem) tree.remove_node(k);
+            tree.end_batch();
+        }
+        if (!add_p.empty()) {
+            // the parents' ghost layers feed the new domains' interpolation stencils at their faces
+            if ((st = prepare()) || (st = fill(tree.timer(), new_f, 1.f))) return st;
+            tree.begin_batch();
+            for (size_t i = 0; i < add_p.size(); i++) tree.add_node(add_p[i], add_o[i]);
+            tree.end_batch();
+        }
+        if ((st = take_ctor_status())) return st;
+        lists_valid = false;
+        graph_valid = false;
+        if (!rem.empty() || !add_p.empty()) {
+            // the new state's ghost cells from the new neighbours, and the start-of-step state equal to it
+            if ((st = prepare()) || (st = fill(tree.timer(), new_f, 1.f))) return st;
+            for (int f = 0; f < nf; f++) {
+                const size_t bytes = (size_t)tree.max_slots() * dims.t * dims.t * dims.t * 4u;
+                if ((e = cudaMemcpyAsync(old_f[f], new_f[f], bytes, cudaMemcpyDeviceToDevice, stream)) != cudaSuccess)
+                    return cuda_status(e);
+            }
+        }
+        if (stats) {
+            stats[0] = refined;
+            stats[1] = coarsened;
+            stats[2] = overridden;
+            stats[3] = (uint32_t)(nl + 7u * refined - 7u * coarsened);
+        }
+        return AMR_OK;
+    }
+    float* features_ptr() const { return d_feat; }
+    float* indicator_ptr() const { return d_ind; }
+
 private:
+    float* d_feat = nullptr;
+    float* d_ind = nullptr;
+    float* d_pred = nullptr;
+    size_t feat_cap = 0;
+
     EvoArgs args(uint32_t s, float* const* in, float* const* out, int stage, int constraints) {
         EvoArgs a;
         std::memset(&a, 0, sizeof(a));
@@ -432,6 +563,36 @@ AMR_API int amr_sim_initial_data(amr_sim* s, const amr_initial_data* d) {
     if (d->kind == AMR_ID_GAUSSIAN_PULSE && !(d->width > 0.f)) return AMR_ERR_INVALID;
     const int st = s->impl->wait_side(-1, 0);
     return st ? st : v->initial_data(*d);
+}
+AMR_API int amr_sim_tile_features(amr_sim* s, float* features, float* indicators, uint32_t* leaf_slots,
+                                  uint32_t capacity, uint32_t* n_leaves) {
+    if (!s || !n_leaves) return AMR_ERR_INVALID;
+    EvolveSim* v = dynamic_cast<EvolveSim*>(s->impl);
+    if (!v) return AMR_ERR_INVALID;
+    int st = s->impl->wait_side(-1, 0);
+    std::vector<uint32_t> leaf;
+    if (!st) st = v->tile_features(leaf);
+    if (st) return st;
+    *n_leaves = (uint32_t)leaf.size();
+    if (leaf.size() > capacity) return AMR_ERR_CAPACITY;
+    cudaStream_t stream = s->impl->stream;
+    cudaError_t e = cudaSuccess;
+    if (features && !leaf.empty())
+        e = cudaMemcpyAsync(features, v->features_ptr(), leaf.size() * 1536u * 4u, cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess && indicators && !leaf.empty())
+        e = cudaMemcpyAsync(indicators, v->indicator_ptr(), leaf.size() * 4u, cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    if (leaf_slots) std::memcpy(leaf_slots, leaf.data(), leaf.size() * 4u);
+    return AMR_OK;
+}
+AMR_API int amr_sim_regrid(amr_sim* s, amr_estimator* est, const amr_regrid* r, uint32_t* stats4) {
+    if (!s || !r || r->max_depth > kDepthLimit || !(r->judge_factor >= 1.f)) return AMR_ERR_INVALID;
+    EvolveSim* v = dynamic_cast<EvolveSim*>(s->impl);
+    if (!v) return AMR_ERR_INVALID;
+    if (s->impl->tree.timer() != 0u) return AMR_ERR_INVALID;   // between timesteps only
+    const int st = s->impl->wait_side(-1, 0);
+    return st ? st : v->regrid(est, *r, stats4);
 }
 AMR_API int amr_sim_constraint_norms(amr_sim* s, float excision_radius, double* out5) {
     if (!s || !out5 || !(excision_radius >= 0.f)) return AMR_ERR_INVALID;

@@ -527,9 +527,111 @@ __global__ void k_evo_norms_total(const double* part, uint32_t n_items, double* 
     out[4] = s[4];
 }
 
+// ------------------------------------------------------------------ prolongation of new domains
+// One CTA per (child, buffer).  Child cell w (padded index) lies at parent index coordinate
+// o * n/2 + p + (w - p + 1/2) / 2 - 1/2 along each axis (o: the child's octant bit), which stays in
+// [1.25, n + 3.75]: the cubic stencil b-1 .. b+2 (b = floor) fits in the parent's padded range.
+__global__ void __launch_bounds__(256) k_evo_prolong(const __grid_constant__ EvoProlongArgs g) {
+    const uint32_t item = blockIdx.x, buf = blockIdx.y;
+    if (item >= g.n_items || buf >= g.nbuf) return;
+    const int32_t node = g.items[3 * item], parent = g.items[3 * item + 1], off = g.items[3 * item + 2];
+    const uint32_t n = g.n, p = g.p, t = g.t;
+    const uint64_t cells = (uint64_t)t * t * t;
+    const float* src = g.bufs[buf] + (uint64_t)parent * cells;
+    float* dst = g.bufs[buf] + (uint64_t)node * cells;
+    const uint32_t oct[3] = {(uint32_t)off & 1u, ((uint32_t)off >> 1) & 1u, ((uint32_t)off >> 2) & 1u};
+    for (uint32_t k = threadIdx.x; k < (uint32_t)cells; k += blockDim.x) {
+        const uint32_t w[3] = {k % t, (k / t) % t, k / (t * t)};
+        int idx[3];
+        float wgt[3][4];
+        for (int a = 0; a < 3; a++) {
+            const float x = (float)(oct[a] * (n / 2u) + p) + ((float)w[a] - (float)p + .5f) * .5f - .5f;
+            int b = __float2int_rd(x);
+            b = b < 1 ? 1 : (b > (int)t - 3 ? (int)t - 3 : b);
+            const float s = x - (float)b;
+            idx[a] = b;
+            wgt[a][0] = -s * (s - 1.f) * (s - 2.f) * (1.f / 6.f);
+            wgt[a][1] = (s + 1.f) * (s - 1.f) * (s - 2.f) * .5f;
+            wgt[a][2] = -(s + 1.f) * s * (s - 2.f) * .5f;
+            wgt[a][3] = (s + 1.f) * s * (s - 1.f) * (1.f / 6.f);
+        }
+        const int64_t si = ((int64_t)idx[2] * t + idx[1]) * t + idx[0];
+        float v = 0.f;
+#pragma unroll
+        for (int k2 = 0; k2 < 4; k2++)
+#pragma unroll
+            for (int k1 = 0; k1 < 4; k1++) {
+                const float w12 = wgt[1][k1] * wgt[2][k2];
+                const int64_t row = si + ((int64_t)(k2 - 1) * t + (k1 - 1)) * t - 1;
+#pragma unroll
+                for (int k0 = 0; k0 < 4; k0++) v = fmaf(wgt[0][k0] * w12, src[row + k0], v);
+            }
+        dst[k] = v;
+    }
+}
+
+// ------------------------------------------------------------------ tile features and the plain criterion
+// One CTA of 512 threads per leaf; thread = cell of the 8^3 feature grid, which covers (N/8)^3
+// domain cells.  Per domain cell: the undivided gradients |d chi| and |d alpha| (second-order centred
+// differences, i.e. the gradient times the cell size) and |d gt| (the norm over the conformal
+// metric's components and axes).  Features of a feature cell: the mean conformal factor,
+// log10(max (|d chi| + |d alpha|) + 1e-10) / 5 + 1 and log10(rms |d gt| + 1e-10) / 5 + 1.  The plain
+// criterion's indicator of the tile is the largest |d chi| + |d alpha| over its cells.
+__global__ void __launch_bounds__(512) k_evo_features(const EvoFeatureArgs g) {
+    const uint32_t b = blockIdx.x;
+    if (b >= g.n_items) return;
+    const uint32_t slot = g.items[b], n = g.n, t = g.t, p = g.p, r = n / 8u;
+    const uint32_t c = threadIdx.x, cx = c % 8, cy = (c / 8) % 8, cz = c / 64;
+    const uint64_t base = (uint64_t)slot * t * t * t;
+    const uint64_t st[3] = {1, t, (uint64_t)t * t};
+    float chi = 0.f, g2 = 0.f, ind = 0.f;
+    for (uint32_t k = 0; k < r * r * r; k++) {
+        const uint32_t x = cx * r + k % r + p, y = cy * r + (k / r) % r + p, z = cz * r + k / (r * r) + p;
+        const uint64_t o = base + ((uint64_t)z * t + y) * t + x;
+        chi += g.state[F_CHI][o] + bssn_offset(F_CHI);
+        float dchi = 0.f, dal = 0.f;
+        for (int a = 0; a < 3; a++) {
+            const float dc = .5f * (g.state[F_CHI][o + st[a]] - g.state[F_CHI][o - st[a]]);
+            const float da = .5f * (g.state[F_ALPHA][o + st[a]] - g.state[F_ALPHA][o - st[a]]);
+            dchi += dc * dc;
+            dal += da * da;
+            for (int q = 0; q < 6; q++) {
+                const float dg = .5f * (g.state[F_GXX + q][o + st[a]] - g.state[F_GXX + q][o - st[a]]);
+                g2 += dg * dg;
+            }
+        }
+        ind = fmaxf(ind, sqrtf(dchi) + sqrtf(dal));   // per-cell differences are already times dx
+    }
+    const float inv = 1.f / (float)(r * r * r);
+    float* f = g.features + (uint64_t)b * 3u * 512u;
+    f[c] = chi * inv;
+    f[512 + c] = log10f(ind + 1e-10f) * .2f + 1.f;
+    f[1024 + c] = log10f(sqrtf(g2 * inv) + 1e-10f) * .2f + 1.f;
+    __shared__ float red[512];
+    red[c] = ind;
+    __syncthreads();
+    for (uint32_t w = 256; w > 0; w >>= 1) {
+        if (c < w) red[c] = fmaxf(red[c], red[c + w]);
+        __syncthreads();
+    }
+    if (c == 0) g.indicator[b] = red[0];
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
+cudaError_t launch_evo_prolong(const EvoProlongArgs& g, cudaStream_t st) {
+    if (g.n_items == 0 || g.nbuf == 0) return cudaSuccess;
+    k_evo_prolong<<<dim3(g.n_items, g.nbuf), 256, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evo_features(const EvoFeatureArgs& g, cudaStream_t st) {
+    if (g.n_items == 0) return cudaSuccess;
+    k_evo_features<<<g.n_items, 512, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
 bool evo_config_supported(uint32_t n, uint32_t p) { return p == 3u && (n == 8u || n == 16u || n == 32u); }
 
 cudaError_t launch_evo_init(const EvoInitArgs& a, cudaStream_t st) {

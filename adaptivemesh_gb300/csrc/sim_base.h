@@ -112,10 +112,9 @@ public:
     void node_dtor(int32_t) override {}
     // Batched node_ctor: upload the deferred constructors once, then prolongate each group into
     // every buffer of `bufs` with one launch; errors are kept for take_ctor_status().
-    void prolongate_groups(const NodeCtor* items, const uint32_t* group_end, uint32_t groups, float* const* bufs,
-                           int nbuf) {
-        const size_t n = groups ? group_end[groups - 1] : 0u;
-        if (n == 0) return;
+    // Copy a batch of deferred constructors to the device (ctor_items); false (and ctor_status set)
+    // on failure.
+    bool upload_ctor_items(const NodeCtor* items, size_t n) {
         if (!ctor_items || ctor_items_cap < n) {
             cudaError_t e = cudaStreamSynchronize(stream);   // a launch of the last batch may still read it
             cudaFree(ctor_items);
@@ -123,11 +122,19 @@ public:
             ctor_items_cap = 0;
             const size_t cap = std::max<size_t>(n, tree.max_slots());
             if (e == cudaSuccess) e = cudaMalloc(&ctor_items, sizeof(NodeCtor) * cap);
-            if (e != cudaSuccess) { ctor_status = cuda_status(e); return; }
+            if (e != cudaSuccess) { ctor_status = cuda_status(e); return false; }
             ctor_items_cap = cap;
         }
         cudaError_t e = cudaMemcpyAsync(ctor_items, items, sizeof(NodeCtor) * n, cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);   // `items` is pageable and short-lived
+        if (e != cudaSuccess) { ctor_status = cuda_status(e); return false; }
+        return true;
+    }
+    void prolongate_groups(const NodeCtor* items, const uint32_t* group_end, uint32_t groups, float* const* bufs,
+                           int nbuf) {
+        const size_t n = groups ? group_end[groups - 1] : 0u;
+        if (n == 0 || !upload_ctor_items(items, n)) return;
+        cudaError_t e = cudaSuccess;
         for (uint32_t g = 0, b = 0; g < groups && e == cudaSuccess; b = group_end[g++]) {
             e = launch_copy_to_children(dims, bufs, nbuf, reinterpret_cast<const int32_t*>(ctor_items + b),
                                         group_end[g] - b, stream);

@@ -1,0 +1,209 @@
+"""The learned refinement / error estimator (include/amr_gb300.h, amr_estimator_*): a per-tile
+BF16 3-D convolutional network, trained on the GPU by the library's own forward and backward
+kernels, on targets the solver generates itself.
+
+  Estimator            the network (create, forward, gradients, train_step, parameters)
+  richardson_samples   features, targets and plain indicators from paired coarse / fine runs of one
+                       configuration:
+                       for each leaf of the coarse run, log10 of the Richardson estimate of its
+                       truncation error after a short evolution, (|u_coarse - u_fine| * 2^p / (2^p - 1),
+                       p = 4, over the conformal factor and the lapse), with the features of the
+                       coarse state it started from
+  train                Adam steps over a sample set
+  captured_error       the share of the true error held by the k leaves a criterion ranks highest
+
+No counterpart in the reference, whose refinement criterion is a gradient / curvature threshold
+(SimpleWave.h:91-187).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import (F_ALPHA, F_CHI, ID_BRILL_LINDQUIST, MODE_GRAPH, SIM_BSSN_EVOLVE, SLICING_1PLUSLOG, VP, Config,
+               Evolution, InitialData, check, load)
+from .octree import Sim
+
+
+class Estimator:
+    def __init__(self, max_batch: int = 256, seed: int = 1):
+        h = VP()
+        check(load().amr_estimator_create(max_batch, seed, ctypes.byref(h)), "amr_estimator_create")
+        self.h, self.max_batch = h, max_batch
+
+    @staticmethod
+    def param_count() -> int:
+        return int(load().amr_estimator_param_count())
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        check(load().amr_estimator_get_params(self.h, p.ctypes.data), "amr_estimator_get_params")
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        check(load().amr_estimator_set_params(self.h, p.ctypes.data), "amr_estimator_set_params")
+
+    def forward(self, features):
+        """Predicted log10 errors of the tiles (a device tensor [n][3][512] in, a device tensor out)."""
+        import torch
+        features = features.contiguous()
+        out = torch.empty(features.shape[0], dtype=torch.float32, device=features.device)
+        check(load().amr_estimator_forward(self.h, features.data_ptr(), features.shape[0], out.data_ptr()),
+              "amr_estimator_forward")
+        return out
+
+    def gradients(self, features, targets):
+        g = np.zeros(self.param_count(), np.float32)
+        loss = ctypes.c_float()
+        check(load().amr_estimator_gradients(self.h, features.contiguous().data_ptr(), targets.contiguous().data_ptr(),
+                                             features.shape[0], g.ctypes.data, ctypes.byref(loss)),
+              "amr_estimator_gradients")
+        return g, loss.value
+
+    def train_step(self, features, targets, lr: float = 1e-3) -> float:
+        loss = ctypes.c_float()
+        check(load().amr_estimator_train_step(self.h, features.contiguous().data_ptr(),
+                                              targets.contiguous().data_ptr(), features.shape[0], lr,
+                                              ctypes.byref(loss)), "amr_estimator_train_step")
+        return loss.value
+
+    def close(self) -> None:
+        if self.h:
+            load().amr_estimator_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def binary_punctures(seed: int, separation: float = 6.0, mass: float = 0.5, jitter: float = 0.01):
+    """Two equal-mass punctures on the x axis with seeded positional jitter."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for sgn in (-1.0, 1.0):
+        pos = np.array([sgn * separation / 2, 0.0, 0.0]) + rng.uniform(-jitter, jitter, 3)
+        out.append((mass, tuple(float(v) for v in pos)))
+    return out
+
+
+def refine_around(sim, points, depth: int, outer: float) -> None:
+    """Refine every domain that contains or touches one of the points down to `depth`."""
+    for d in range(depth):
+        st = sim.state()
+        used, pos, ch = st["used_slots"], st["positions"], st["children"]
+        parents, offsets = [], []
+        for s in range(used):
+            p = int(pos[s])
+            if p == 0xFFFFFFFF or (p >> 27) != d:
+                continue
+            # centre and half edge of slot s
+            c = np.zeros(3)
+            path = p & ((1 << 27) - 1)
+            for i in range(d):
+                for a in range(3):
+                    c[a] += (0.25 if path & (1 << a) else -0.25) / (1 << i)
+                path >>= 3
+            c *= outer
+            half = outer / 2 / (1 << d)
+            if not any(np.all(np.abs(np.asarray(q) - c) <= half * 1.25) for q in points):
+                continue
+            for o in range(8):
+                if ch[s * 8 + o] == -1:
+                    parents.append(s)
+                    offsets.append(o)
+        if parents:
+            sim.add_nodes(parents, offsets)
+
+
+def build_sim(n: int, outer: float, punctures, depth: int, extra_levels: int = 0, slots: int = 4096,
+              mode: int = MODE_GRAPH):
+    """A BSSN evolution of Brill-Lindquist punctures on an octree refined around them to `depth`,
+    every leaf then refined `extra_levels` more times (the fine member of a Richardson pair)."""
+    sim = Sim(Config(n, 3, outer), SIM_BSSN_EVOLVE, slots=slots, mode=mode)
+    refine_around(sim, [p for _, p in punctures], depth, outer)
+    for _ in range(extra_levels):
+        st = sim.state()
+        used, pos, ch = st["used_slots"], st["positions"], st["children"]
+        leaves = [s for s in range(used) if pos[s] != 0xFFFFFFFF and all(c == -1 for c in ch[8 * s:8 * s + 8])]
+        sim.add_nodes([s for s in leaves for _ in range(8)], [o for _ in leaves for o in range(8)])
+    sim.set_evolution(Evolution(slicing=SLICING_1PLUSLOG, shift=1, eta=2.0, ko_sigma=0.1, cfl=0.25))
+    sim.initial_data(InitialData(kind=ID_BRILL_LINDQUIST, punctures=punctures))
+    return sim
+
+
+def richardson_samples(seed: int, n: int = 8, outer: float = 32.0, depth: int = 4, steps: int = 1):
+    """(features [k][3][512], targets [k], plain indicators [k]) as device tensors for the k leaves of
+    one seeded binary configuration: the coarse run's tile features and plain-criterion indicators at
+    the start and the log10 Richardson estimate of its truncation error after `steps` root steps."""
+    import torch
+    punct = binary_punctures(seed)
+    coarse = build_sim(n, outer, punct, depth)
+    feats, ind, leaves = coarse.tile_features()
+    feats, ind = feats.clone(), ind.clone()
+    fine = build_sim(n, outer, punct, depth, extra_levels=1)
+    for _ in range(steps):
+        coarse.timestep()
+        fine.timestep()
+    coarse.synchronize()
+    fine.synchronize()
+    cs, fs = coarse.state(), fine.state()
+    t = n + 6
+    fields = (F_CHI, F_ALPHA)
+    cdat = [coarse.tensor(Sim.NEW_STATE, f)[: cs["used_slots"] * t ** 3].view(-1, t, t, t)[:, 3:3 + n, 3:3 + n, 3:3 + n]
+            for f in fields]
+    fdat = [fine.tensor(Sim.NEW_STATE, f)[: fs["used_slots"] * t ** 3].view(-1, t, t, t)[:, 3:3 + n, 3:3 + n, 3:3 + n]
+            for f in fields]
+    # the fine run's children of each coarse leaf (same slots for the shared part of the tree: the fine
+    # tree is built by the same calls followed by one more level)
+    fch = fs["children"]
+    targets = torch.empty(len(leaves), dtype=torch.float32, device="cuda")
+    h = n // 2
+    for i, s in enumerate(leaves):
+        err = torch.zeros((), device="cuda")
+        for cd, fd in zip(cdat, fdat):
+            block = torch.empty((n, n, n), device="cuda")
+            for o in range(8):
+                k = int(fch[8 * s + o])
+                child = fd[k]
+                # 2x2x2 means of the child's cells -> the coarse cells of octant o
+                m = child.reshape(h, 2, h, 2, h, 2).mean(dim=(1, 3, 5))
+                ox, oy, oz = o & 1, (o >> 1) & 1, (o >> 2) & 1
+                block[oz * h:(oz + 1) * h, oy * h:(oy + 1) * h, ox * h:(ox + 1) * h] = m
+            diff = (cd[s] - block).abs().max()
+            err = torch.maximum(err, diff)
+        targets[i] = torch.log10(err * 16.0 / 15.0 + 1e-12)
+    coarse.close()
+    fine.close()
+    return feats, targets, ind
+
+
+def train(est: Estimator, feats, targets, epochs: int = 200, batch: int = 64, lr: float = 2e-3, seed: int = 0) -> list:
+    """Adam over shuffled mini-batches; returns the mean loss of each epoch."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    n = feats.shape[0]
+    losses = []
+    for _ in range(epochs):
+        perm = torch.randperm(n, generator=g).to(feats.device)
+        tot, cnt = 0.0, 0
+        for b0 in range(0, n, batch):
+            idx = perm[b0:b0 + batch]
+            loss = est.train_step(feats[idx], targets[idx], lr)
+            tot += loss * len(idx)
+            cnt += len(idx)
+        losses.append(tot / cnt)
+    return losses
+
+
+def captured_error(scores, targets, k: int) -> float:
+    """Share of the total Richardson error (10**targets) held by the k leaves with the highest scores:
+    how much of the error a refinement budget of k leaves removes when spent by this ranking."""
+    import torch
+    err = torch.pow(10.0, targets.double())
+    top = torch.topk(scores.double(), k).indices
+    return float(err[top].sum() / err.sum())

@@ -5,7 +5,7 @@ import ctypes
 
 import numpy as np
 
-from . import MODE_GRAPH, SIM_BSSN, Config, VP, U64, check, load
+from . import MODE_GRAPH, SIM_BSSN, Config, VP, U32, U64, check, load
 
 
 def _state(fn, h, slots: int) -> dict:
@@ -266,6 +266,27 @@ class Sim:
         out = (ctypes.c_double * 5)()
         check(load().amr_sim_constraint_norms(self.h, excision, out), "amr_sim_constraint_norms")
         return {"H_l2": out[0], "H_max": out[1], "M_l2": out[2], "M_max": out[3], "cells": int(out[4])}
+
+    def tile_features(self):
+        """(features [n][3][512], plain indicators [n]) as device tensors, and the leaf slots."""
+        import torch
+        import numpy as np
+        n = U32()
+        load().amr_sim_tile_features(self.h, None, None, None, 0, ctypes.byref(n))
+        feats = torch.empty((max(n.value, 1), 3, 512), dtype=torch.float32, device="cuda")
+        ind = torch.empty(max(n.value, 1), dtype=torch.float32, device="cuda")
+        slots = np.zeros(max(n.value, 1), np.uint32)
+        check(load().amr_sim_tile_features(self.h, feats.data_ptr(), ind.data_ptr(), slots.ctypes.data, n.value,
+                                           ctypes.byref(n)), "amr_sim_tile_features")
+        return feats[: n.value], ind[: n.value], slots[: n.value]
+
+    def regrid(self, params, estimator=None) -> dict:
+        """Refine / coarsen between timesteps (amr_sim_regrid): by the estimator judged by the plain
+        criterion, or by the plain criterion alone."""
+        stats = (U32 * 4)()
+        check(load().amr_sim_regrid(self.h, estimator.h if estimator is not None else None, ctypes.byref(params),
+                                    stats), "amr_sim_regrid")
+        return {"refined": stats[0], "coarsened": stats[1], "overridden": stats[2], "leaves": stats[3]}
 
     def set_fault_injection(self, spin_limit: int = 0, withhold_plane: int = 0) -> None:
         """Failure-path test hook of the fused pass (amr_sim_set_fault_injection); (0, 0) is off."""

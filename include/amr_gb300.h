@@ -381,6 +381,55 @@ int amr_sim_initial_data(amr_sim* s, const amr_initial_data* d);
  * fields themselves are amr_sim_buffer(4, 0..3).  Synchronises the simulation's stream.  BSSN only. */
 int amr_sim_constraint_norms(amr_sim* s, float excision_radius, double* out5);
 
+/* ---------------------------------------------------------------- learned refinement estimator
+ * No counterpart in the reference, whose refinement is a gradient / curvature threshold per octant
+ * (SimpleWave.h:91-187, 228-248).  A small network predicts each tile's (domain's) log10 truncation
+ * error from 3 x 8^3 features (conformal factor, lapse, |d gt| dx, averaged onto 8^3): conv 3->16
+ * (3^3, ReLU), conv 16->16 (3^3, stride 2, ReLU), dense 1024->32 (ReLU), dense 32->1.  Forward and
+ * backward run on the tensor cores (BF16 operands, FP32 accumulation); FP32 master weights and
+ * Adam.  Buffers are device pointers; features are [tile][3][512] floats. */
+typedef struct amr_estimator amr_estimator;
+int amr_estimator_create(uint32_t max_batch, uint64_t seed, amr_estimator** out);
+int amr_estimator_destroy(amr_estimator* e);
+uint64_t amr_estimator_param_count(void);
+/* The FP32 parameters as one flat host array: W1[96][16] (rows 81..95 zero), b1[16], W2[432][16],
+ * b2[16], W3[1024][32], b3[32], W4[32], b4[1]; im2col row j = channel * 27 + dz * 9 + dy * 3 + dx. */
+int amr_estimator_get_params(amr_estimator* e, float* host);
+int amr_estimator_set_params(amr_estimator* e, const float* host);
+/* Predictions for n tiles (any n; batches of max_batch), synchronous. */
+int amr_estimator_forward(amr_estimator* e, const float* features, uint32_t n, float* out);
+/* Gradients of the mean squared error against targets (n <= max_batch) into a host array laid out
+ * as the parameters; *loss = the mean squared error.  One Adam step with amr_estimator_train_step. */
+int amr_estimator_gradients(amr_estimator* e, const float* features, const float* targets, uint32_t n,
+                            float* grads_host, float* loss);
+int amr_estimator_train_step(amr_estimator* e, const float* features, const float* targets, uint32_t n, float lr,
+                             float* loss);
+/* Features (device [n][3][512]), plain-criterion indicators (device [n]: the largest undivided
+ * gradient |d chi| + |d alpha| over the tile's cells) and slots (host [n]) of the leaves of a BSSN
+ * evolution, from its latest state.  Per cell of an 8^3 grid over the tile: the mean conformal
+ * factor, log10(max(|d chi| + |d alpha|) + 1e-10) / 5 + 1, log10(rms |d gt| + 1e-10) / 5 + 1.
+ * *n_leaves is set even when capacity is too small (AMR_ERR_CAPACITY). */
+int amr_sim_tile_features(amr_sim* s, float* features, float* indicators, uint32_t* leaf_slots, uint32_t capacity,
+                          uint32_t* n_leaves);
+typedef struct amr_regrid {
+    float refine_threshold;   /* plain criterion: refine a leaf whose indicator exceeds this */
+    float coarsen_threshold;  /* plain criterion: a leaf below this may merge with its siblings */
+    float learned_refine;     /* network: refine a leaf whose predicted log10 error exceeds this */
+    float learned_coarsen;    /* network: a leaf predicted below this may merge with its siblings */
+    float judge_factor;       /* the plain criterion refines a leaf the network declines when its
+                                 indicator exceeds judge_factor * refine_threshold (>= 1) */
+    uint32_t max_depth;       /* no leaf is refined beyond this depth */
+    uint32_t min_depth;       /* no parent shallower than this is coarsened */
+} amr_regrid;
+/* Refine / coarsen the leaves of a BSSN evolution between timesteps: with an estimator its
+ * predictions decide and the plain criterion is the judge (overriding declined refinements it
+ * finds strong, and vetoing coarsening where it would refine); with est == NULL the plain
+ * criterion decides.  New domains are interpolated from their parents' padded cells (tricubic, as
+ * for every domain added to an evolution; the parents' ghost layers are refilled first), removed
+ * ones dropped, ghost cells refilled.  stats4 (optional) = {refined leaves, coarsened parents,
+ * refinements the judge forced, leaves after}. */
+int amr_sim_regrid(amr_sim* s, amr_estimator* est, const amr_regrid* r, uint32_t* stats4);
+
 /* ---------------------------------------------------------------- scan and reductions
  * The reference's general-purpose device algorithms (AdaptiveMesh/parallel.h) on a device array
  * of `count` elements (count < 2^32), each `ncomp` (1-4) consecutive values of type `dtype` (the
