@@ -74,6 +74,12 @@ struct EvoProlongArgs {
     const int32_t* items;   // (node, parent, offset) triples
     uint32_t n_items, nbuf;
     uint32_t n, p, t;
+    int floor_buf[2];       // buffers whose values are kept at or above floor_val (-1: none)
+    float floor_val;
+    // per buffer: 0 interpolates the stored values; 2 and 4 interpolate the square and the fourth
+    // root of (stored + 1) and raise the result back (the lapse and the conformal factor, stored
+    // less 1, which fall to zero at a puncture as r^2 and r^4 while their roots stay smooth)
+    signed char root[2 * kMaxFields];
 };
 cudaError_t launch_evo_prolong(const EvoProlongArgs& g, cudaStream_t st);
 

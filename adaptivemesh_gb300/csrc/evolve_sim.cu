@@ -74,7 +74,8 @@ public:
 
     // ---- node constructors: both state buffers of every field of a new domain by tricubic
     // interpolation of its parent's padded state (fourth order, in place of the reference's rule,
-    // AMR.h:1053-1115, whose second-order error seeds O(1) constraint violations on refined cells)
+    // AMR.h:1053-1115, whose second-order error seeds O(1) constraint violations on refined cells;
+    // chi and alpha through their fourth and square roots)
     void node_ctor(int32_t node) override {
         const NodeCtor c = {node, tree.parents()[node], (int32_t)pos_final_offset(tree.positions()[node])};
         const uint32_t end = 1;
@@ -90,6 +91,12 @@ public:
         for (int f = 0; f < nf; f++) { g.bufs[f] = old_f[f]; g.bufs[nf + f] = new_f[f]; }
         g.nbuf = 2u * (uint32_t)nf;
         g.n = dims.n; g.p = dims.p; g.t = dims.t;
+        const bool bssn = kind == AMR_SIM_BSSN_EVOLVE;   // chi, stored less 1, kept at its floor
+        g.floor_buf[0] = bssn ? F_CHI : -1;
+        g.floor_buf[1] = bssn ? nf + F_CHI : -1;
+        g.floor_val = prm.chi_floor - 1.f;
+        if (bssn)
+            for (int b = 0; b < 2; b++) { g.root[b * nf + F_CHI] = 4; g.root[b * nf + F_ALPHA] = 2; }
         cudaError_t e = cudaSuccess;
         for (uint32_t k = 0, b = 0; k < groups && e == cudaSuccess; b = group_end[k++]) {   // depth order
             g.items = reinterpret_cast<const int32_t*>(ctor_items + b);
@@ -418,6 +425,21 @@ public:
             for (int c = 0; c < 8; c++) rem.push_back(ch[(size_t)sl * 8u + c]);
             coarsened++;
         }
+        // Between root steps every domain holds its state at one time in `new`; `old` (the start of
+        // each domain's last step) is rewritten by the next step's restriction.  Setting old = new
+        // first makes every ghost fill below take the current state: the fill blends a coarser
+        // neighbour's old and new states by the substep's time fraction.
+        auto sync_old = [&]() -> int {
+            const size_t bytes = (size_t)tree.max_slots() * dims.t * dims.t * dims.t * 4u;
+            for (int f = 0; f < nf; f++) {
+                const cudaError_t ce = cudaMemcpyAsync(old_f[f], new_f[f], bytes, cudaMemcpyDeviceToDevice, stream);
+                if (ce != cudaSuccess) return cuda_status(ce);
+            }
+            return AMR_OK;
+        };
+        if (!rem.empty() || !add_p.empty()) {
+            if ((st = sync_old())) return st;
+        }
         if (!rem.empty()) {
             tree.begin_batch();
             for (int32_t k : rem) tree.remove_node(k);
@@ -434,13 +456,8 @@ public:
         lists_valid = false;
         graph_valid = false;
         if (!rem.empty() || !add_p.empty()) {
-            // the new state's ghost cells from the new neighbours, and the start-of-step state equal to it
-            if ((st = prepare()) || (st = fill(tree.timer(), new_f, 1.f))) return st;
-            for (int f = 0; f < nf; f++) {
-                const size_t bytes = (size_t)tree.max_slots() * dims.t * dims.t * dims.t * 4u;
-                if ((e = cudaMemcpyAsync(old_f[f], new_f[f], bytes, cudaMemcpyDeviceToDevice, stream)) != cudaSuccess)
-                    return cuda_status(e);
-            }
+            // the ghost cells from the new neighbours, in both state buffers
+            if ((st = prepare()) || (st = fill(tree.timer(), new_f, 1.f)) || (st = sync_old())) return st;
         }
         if (stats) {
             stats[0] = refined;

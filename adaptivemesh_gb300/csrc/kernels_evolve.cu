@@ -223,25 +223,29 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS) k_evo_derivs(const __g
 // ------------------------------------------------------------------ right-hand sides and stage update
 // RK4: stage 1: acc = old + dt/6 k1, out = old + dt/2 k1; stage 2: acc += dt/3 k2, out = old + dt/2 k2;
 // stage 3: acc += dt/3 k3, out = old + dt k3; stage 4: out = acc + dt/6 k4.
+// `lo`: the stage outputs' lower bound (the conformal factor's floor; -inf for the other fields).
+// A NaN stays a NaN.
 __device__ __forceinline__ void rk_update(const EvoArgs& a, int f, uint64_t pi, uint64_t ii, float u_old, float r,
-                                          float dt) {
+                                          float dt, float lo = -INFINITY) {
+    float v;
     switch (a.stage) {
         case 1:
             a.acc[f][ii] = fmaf(dt * (1.f / 6.f), r, u_old);
-            a.out[f][pi] = fmaf(dt * .5f, r, u_old);
+            v = fmaf(dt * .5f, r, u_old);
             break;
         case 2:
             a.acc[f][ii] = fmaf(dt * (1.f / 3.f), r, a.acc[f][ii]);
-            a.out[f][pi] = fmaf(dt * .5f, r, u_old);
+            v = fmaf(dt * .5f, r, u_old);
             break;
         case 3:
             a.acc[f][ii] = fmaf(dt * (1.f / 3.f), r, a.acc[f][ii]);
-            a.out[f][pi] = fmaf(dt, r, u_old);
+            v = fmaf(dt, r, u_old);
             break;
         default:
-            a.out[f][pi] = fmaf(dt * (1.f / 6.f), r, a.acc[f][ii]);
+            v = fmaf(dt * (1.f / 6.f), r, a.acc[f][ii]);
             break;
     }
+    a.out[f][pi] = v < lo ? lo : v;
 }
 
 template <int N>
@@ -268,7 +272,8 @@ __global__ void __launch_bounds__(128) k_evo_rhs_bssn(const __grid_constant__ Ev
     for (int f = 0; f < BSSN_NF; f++) {
         const float r = rhs[f] + dv(D_EXTRA + f);
         const float uo = a.stage == 1 ? a.fields[f][pi] : a.old_f[f][pi];   // the stored form
-        rk_update(a, f, pi, ii, uo, r, dt);
+        // chi (stored less 1) is kept at or above its floor, as the geometry divides by it
+        rk_update(a, f, pi, ii, uo, r, dt, f == F_CHI ? a.prm.chi_floor - 1.f : -INFINITY);
     }
 }
 
@@ -531,6 +536,9 @@ __global__ void k_evo_norms_total(const double* part, uint32_t n_items, double* 
 // One CTA per (child, buffer).  Child cell w (padded index) lies at parent index coordinate
 // o * n/2 + p + (w - p + 1/2) / 2 - 1/2 along each axis (o: the child's octant bit), which stays in
 // [1.25, n + 3.75]: the cubic stencil b-1 .. b+2 (b = floor) fits in the parent's padded range.
+// Near a puncture chi ~ r^4 and alpha ~ r^2 (precollapsed lapse): a cubic through their values
+// undershoots zero, so they are interpolated as chi^(1/4) and alpha^(1/2), which vary like r, and
+// raised back; chi is then kept at or above its floor.
 __global__ void __launch_bounds__(256) k_evo_prolong(const __grid_constant__ EvoProlongArgs g) {
     const uint32_t item = blockIdx.x, buf = blockIdx.y;
     if (item >= g.n_items || buf >= g.nbuf) return;
@@ -540,6 +548,13 @@ __global__ void __launch_bounds__(256) k_evo_prolong(const __grid_constant__ Evo
     const float* src = g.bufs[buf] + (uint64_t)parent * cells;
     float* dst = g.bufs[buf] + (uint64_t)node * cells;
     const uint32_t oct[3] = {(uint32_t)off & 1u, ((uint32_t)off >> 1) & 1u, ((uint32_t)off >> 2) & 1u};
+    const float lo = (int)buf == g.floor_buf[0] || (int)buf == g.floor_buf[1] ? g.floor_val : -INFINITY;
+    const int root = g.root[buf];
+    auto fwd = [&](float v) {   // the interpolated quantity of a stored value
+        if (root == 0) return v;
+        const float u = sqrtf(fmaxf(v + 1.f, 0.f));
+        return root == 2 ? u : sqrtf(u);
+    };
     for (uint32_t k = threadIdx.x; k < (uint32_t)cells; k += blockDim.x) {
         const uint32_t w[3] = {k % t, (k / t) % t, k / (t * t)};
         int idx[3];
@@ -564,9 +579,13 @@ __global__ void __launch_bounds__(256) k_evo_prolong(const __grid_constant__ Evo
                 const float w12 = wgt[1][k1] * wgt[2][k2];
                 const int64_t row = si + ((int64_t)(k2 - 1) * t + (k1 - 1)) * t - 1;
 #pragma unroll
-                for (int k0 = 0; k0 < 4; k0++) v = fmaf(wgt[0][k0] * w12, src[row + k0], v);
+                for (int k0 = 0; k0 < 4; k0++) v = fmaf(wgt[0][k0] * w12, fwd(src[row + k0]), v);
             }
-        dst[k] = v;
+        if (root != 0) {
+            const float v2 = v * v;
+            v = (root == 2 ? v2 : v2 * v2) - 1.f;
+        }
+        dst[k] = v < lo ? lo : v;
     }
 }
 

@@ -11,6 +11,12 @@ kernels, on targets the solver generates itself.
                        coarse state it started from
   train                Adam steps over a sample set
   captured_error       the share of the true error held by the k leaves a criterion ranks highest
+  calibrate            least-squares line log10(error) ~ a + b log10(plain indicator): the plain
+                       criterion expressed as an error estimate, for thresholds in error units
+  train_default        the network of the binary-puncture configuration (16^3 tiles), trained on
+                       seeded jittered configurations, with the held-out error of both estimates;
+                       save / load_trained keep it in an .npz file
+                       (python -m adaptivemesh_gb300.estimator --out FILE trains one)
 
 No counterpart in the reference, whose refinement criterion is a gradient / curvature threshold
 (SimpleWave.h:91-187).
@@ -136,16 +142,32 @@ def build_sim(n: int, outer: float, punctures, depth: int, extra_levels: int = 0
     return sim
 
 
-def richardson_samples(seed: int, n: int = 8, outer: float = 32.0, depth: int = 4, steps: int = 1):
+def richardson_samples(seed: int, n: int = 8, outer: float = 32.0, depth: int = 4, steps: int = 1,
+                       pre_steps: int = 0):
     """(features [k][3][512], targets [k], plain indicators [k]) as device tensors for the k leaves of
-    one seeded binary configuration: the coarse run's tile features and plain-criterion indicators at
-    the start and the log10 Richardson estimate of its truncation error after `steps` root steps."""
+    one seeded binary configuration after `pre_steps` root steps of its coarse run: that state's tile
+    features and plain-criterion indicators, and the log10 Richardson estimate of each leaf's
+    truncation error over the next `steps` root steps.  The fine run starts from the same state with
+    every leaf refined once (from the analytic initial data when pre_steps is 0, else by the
+    tricubic prolongation of the coarse state)."""
     import torch
     punct = binary_punctures(seed)
     coarse = build_sim(n, outer, punct, depth)
+    for _ in range(pre_steps):
+        coarse.timestep()
+    coarse.synchronize()
     feats, ind, leaves = coarse.tile_features()
     feats, ind = feats.clone(), ind.clone()
-    fine = build_sim(n, outer, punct, depth, extra_levels=1)
+    if pre_steps == 0:
+        fine = build_sim(n, outer, punct, depth, extra_levels=1)
+    else:
+        fine = build_sim(n, outer, punct, depth)
+        nf = 24
+        for f in range(nf):
+            for buf in (Sim.OLD_STATE, Sim.NEW_STATE):
+                fine.tensor(buf, f).copy_(coarse.tensor(buf, f))
+        torch.cuda.synchronize()
+        fine.add_nodes([s for s in leaves for _ in range(8)], [o for _ in leaves for o in range(8)])
     for _ in range(steps):
         coarse.timestep()
         fine.timestep()
@@ -207,3 +229,97 @@ def captured_error(scores, targets, k: int) -> float:
     err = torch.pow(10.0, targets.double())
     top = torch.topk(scores.double(), k).indices
     return float(err[top].sum() / err.sum())
+
+
+def calibrate(indicators, targets) -> tuple[float, float]:
+    """(a, b) of the least-squares line targets ~ a + b log10(indicators)."""
+    import torch
+    x = torch.log10(indicators.double() + 1e-12)
+    X = torch.stack([torch.ones_like(x), x], 1)
+    coef = torch.linalg.lstsq(X, targets.double()[:, None]).solution[:, 0]
+    return float(coef[0]), float(coef[1])
+
+
+def training_set(seeds, n: int = 16, outer: float = 32.0, depth: int = 4, dropped: list | None = None,
+                 pre_steps=(0,)):
+    """Concatenated (features, targets, indicators) of richardson_samples over the seeds, each at
+    every start time in pre_steps.  A sample set that is not all finite (a run that diverged) is
+    left out and its (seed, pre_steps) appended to `dropped`."""
+    import torch
+    fs, ts, inds = [], [], []
+    for seed, k in [(seed, k) for seed in seeds for k in pre_steps]:
+        f, t, i = richardson_samples(seed, n=n, outer=outer, depth=depth, pre_steps=k)
+        if not (bool(torch.isfinite(f).all()) and bool(torch.isfinite(t).all()) and bool(torch.isfinite(i).all())):
+            if dropped is not None:
+                dropped.append((seed, k))
+            continue
+        fs.append(f)
+        ts.append(t)
+        inds.append(i)
+    return torch.cat(fs), torch.cat(ts), torch.cat(inds)
+
+
+def train_default(n_seeds: int = 64, held_out: int = 8, n: int = 16, outer: float = 32.0, depth: int = 4,
+                  epochs: int = 60, batch: int = 64, lr: float = 2e-3, pre_steps=(0, 8), log=None):
+    """The binary-puncture configuration's network: Richardson samples of n_seeds seeded jittered
+    configurations at the start times pre_steps (the last held_out seeds kept for validation), Adam
+    on the GPU.  Returns (estimator, calibration (a, b) of the plain indicator on the training
+    samples, metadata)."""
+    import time
+    import torch
+    t0 = time.perf_counter()
+    train_seeds = list(range(1, n_seeds - held_out + 1))
+    val_seeds = list(range(n_seeds - held_out + 1, n_seeds + 1))
+    dropped = []
+    ft, tt, it = training_set(train_seeds, n, outer, depth, dropped, pre_steps)
+    fv, tv, iv = training_set(val_seeds, n, outer, depth, dropped, pre_steps)
+    t1 = time.perf_counter()
+    est = Estimator(batch, seed=1)
+    losses = train(est, ft, tt, epochs=epochs, batch=batch, lr=lr)
+    t2 = time.perf_counter()
+    a, b = calibrate(it, tt)
+    pred = est.forward(fv)
+    mse_net = float(((pred - tv) ** 2).mean())
+    mse_plain = float(((a + b * torch.log10(iv.double() + 1e-12) - tv.double()) ** 2).mean())
+    meta = {"configuration": f"binary Brill-Lindquist, m = 0.5 at x = +-3, jitter 0.01; {n}^3 tiles, "
+                             f"root edge {outer}, refined to depth {depth} around the punctures",
+            "start_root_steps": list(pre_steps), "train_seeds": len(train_seeds),
+            "diverged_samples_left_out": dropped, "train_tiles": int(ft.shape[0]), "val_seeds": len(val_seeds),
+            "val_tiles": int(fv.shape[0]), "epochs": epochs, "loss_first": losses[0], "loss_last": losses[-1],
+            "val_mse_network": mse_net, "val_mse_calibrated_indicator": mse_plain,
+            "val_target_variance": float(tv.var()), "target_quantiles": [float(q) for q in torch.quantile(
+                tt, torch.tensor([0.5, 0.8, 0.9], device=tt.device))],
+            "seconds_samples": t1 - t0, "seconds_training": t2 - t1}
+    if log:
+        log(f"estimator: {meta}")
+    return est, (a, b), meta
+
+
+def save(path: str, est: Estimator, calib, meta: dict) -> None:
+    import json
+    np.savez(path, params=est.get_params(), calibration=np.array(calib, np.float64),
+             meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
+
+
+def load_trained(path: str, max_batch: int = 256):
+    """(estimator, calibration, metadata) from a file written by save()."""
+    import json
+    d = np.load(path)
+    est = Estimator(max_batch, seed=1)
+    est.set_params(d["params"])
+    return est, tuple(float(v) for v in d["calibration"]), json.loads(bytes(d["meta"]).decode())
+
+
+if __name__ == "__main__":
+    import argparse
+    import sys
+    ap = argparse.ArgumentParser(description="train the binary-puncture refinement estimator on the GPU")
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--seeds", type=int, default=64)
+    ap.add_argument("--held-out", type=int, default=8)
+    ap.add_argument("--epochs", type=int, default=60)
+    a = ap.parse_args()
+    e, c, m = train_default(a.seeds, a.held_out, epochs=a.epochs,
+                            log=lambda s: print(s, file=sys.stderr, flush=True))
+    save(a.out, e, c, m)
+    print(m)

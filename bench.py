@@ -288,6 +288,195 @@ def wave_line(args) -> None:
                                              "padding 2", "mode": "batched"}}))
 
 
+def zone_cycles_per_root_step(st, n: int) -> int:
+    """Leaf zones advanced per root step: a leaf at depth d takes 2^d steps (2:1 subcycling)."""
+    used, pos, ch = st["used_slots"], st["positions"], st["children"]
+    total = 0
+    for s in range(used):
+        p = int(pos[s])
+        if p != 0xFFFFFFFF and all(c == -1 for c in ch[8 * s:8 * s + 8]):
+            total += n ** 3 << (p >> 27)
+    return total
+
+
+class CpuEvolution:
+    """The FP64 oracle of the BSSN evolution (oracle/bssn_evolve.c, OpenMP over domains) on the
+    gauge-wave octree: one finest substep timed on all host cores."""
+
+    def __init__(self, depth: int, n: int = 16):
+        import numpy as np
+        from oracle import oracle as orc
+        self.np, self.orc, self.L = np, orc, orc.lib()
+        st = golden_tree(depth)
+        used = st["used_slots"]
+        bd = np.zeros(used * 6, np.uint64)
+        self.L.orc_periodic_boundaries(orc.P(st["positions"]), orc.P(st["children"]), used, orc.P(bd))
+        st["boundaries"] = bd
+        self.st, self.used, self.n = st, used, n
+        e = orc.Evo()
+        e.n, e.p, e.outer_size, e.physics, e.slicing, e.shift = n, 3, 1.0, 0, 0, 0
+        e.eta, e.ko_sigma, e.cfl, e.chi_floor = 2.0, 0.1, 0.25, 1e-6
+        e.id_kind, e.amplitude, e.wavelength = 1, 0.01, 1.0
+        self.e = e
+        t = n + 6
+        padded, inner = used * t ** 3, used * n ** 3
+        self.old = [np.zeros(padded) for _ in range(24)]
+        self.L.orc_evo_initial_data(ctypes.byref(e), orc.P(orc.ptrs(self.old)), orc.P(st["positions"]), used)
+        self.new = [f.copy() for f in self.old]
+        self.stage = [f.copy() for f in self.old]
+        self.acc = [np.zeros(inner) for _ in range(24)]
+        self.cores = int(self.L.orc_num_threads())
+        self.zones = sum(1 for s in range(used) if all(c == -1 for c in st["children"][8 * s:8 * s + 8])) * n ** 3
+
+    def substep(self) -> float:
+        orc, st = self.orc, self.st
+        timer = ctypes.c_uint32(0)
+        t0 = time.perf_counter()
+        self.L.orc_evo_timestep(ctypes.byref(self.e), orc.P(orc.ptrs(self.old)), orc.P(orc.ptrs(self.new)),
+                                orc.P(orc.ptrs(self.stage)), orc.P(orc.ptrs(self.acc)), orc.P(st["positions"]),
+                                orc.P(st["children"]), orc.P(st["boundaries"]), self.used, st["max_depth"],
+                                ctypes.byref(timer))
+        return time.perf_counter() - t0
+
+
+def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: str = "all",
+                     batched_mode: str = "graph", plain: bool = True) -> dict:
+    """The full BSSN evolution's throughput (zone-cycles/s: leaf zones x steps at their own level)
+    at fixed constraint error, batched (CUDA-graph replay of whole root steps) against the plain
+    per-domain launches, which compute the same state bit for bit:
+
+      gauge_wave  the linear gauge wave, A = 1e-2, L = 1, periodic box, uniform depth 3 (512 domains
+                  of 16^3 = 128^3 zones), 1+log slicing, zero shift: 25 root steps (200 finest steps)
+                  batched, the first untimed; 2 root steps plain, the first untimed; H and M L2 after
+                  the 200 steps (FP64 reductions).  FP64 CPU baseline: one substep of the oracle.
+      binary      binary Brill-Lindquist punctures (m = 0.5 at x = +-3, seeded jitter 0.01), 16^3
+                  domains, root edge 32, refined around the punctures to depth 4; regridded every
+                  8 root steps (before steps 0 and 8) up to depth 5 by the learned estimator judged
+                  by the plain criterion ('learned') or by the plain criterion alone ('plain'),
+                  both aiming at the same error tolerance (the plain indicator calibrated to an
+                  error estimate on the estimator's training samples); 16 root steps batched,
+                  regrids and graph recaptures included in the time; the plain per-domain launches
+                  timed over one root step on the plain-criterion tree.  H and M L2 outside r = 1
+                  of each puncture after the run."""
+    import adaptivemesh_gb300 as am
+    from adaptivemesh_gb300 import estimator as E
+    import cases
+    out = {}
+    bmode = {"graph": am.MODE_GRAPH, "batched": am.MODE_BATCHED}[batched_mode]
+    if case in ("all", "gauge_wave"):
+        out["gauge_wave"] = gauge_wave_report(am, cases, bmode, cpu, plain)
+    if case in ("all", "binary"):
+        out["binary"] = binary_report(am, E, estimator_path, bmode, plain)
+    return out
+
+
+def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool) -> dict:
+    gw = {}
+    arms = [("batched", bmode, 24)] + ([("plain", am.MODE_PLAIN, 1)] if plain else [])
+    for name, mode, steps in arms:
+        progress(f"evolution: gauge wave, {name}")
+        sim = am.Sim(am.Config(16, 3, 1.0), am.SIM_BSSN_EVOLVE, slots=585, mode=mode)
+        cases.tree_uniform(sim, 3)
+        sim.set_evolution(am.Evolution(slicing=am.SLICING_1PLUSLOG, shift=0, ko_sigma=0.1, cfl=0.25, periodic=1))
+        sim.initial_data(am.InitialData(kind=am.ID_GAUGE_WAVE, amplitude=1e-2, wavelength=1.0))
+        sim.timestep()                       # warm-up (graph capture)
+        sim.synchronize()
+        l0 = sim.kernel_launches
+        sim.event_record(0)
+        for _ in range(steps):
+            sim.timestep()
+        sim.event_record(1)
+        sim.synchronize()
+        ms = sim.event_elapsed(0, 1)
+        zc = zone_cycles_per_root_step(sim.state(), 16) * steps
+        gw[name] = {"value": zc / (ms / 1e3), "ms_per_root_step": ms / steps, "root_steps": steps,
+                    "gpu_launches_per_root_step": (sim.kernel_launches - l0) / steps}
+        if name == "batched":
+            gw[name].update({k: v for k, v in sim.constraint_norms().items() if k != "cells"})
+            gw[name]["finest_steps"] = 8 * (steps + 1)
+        sim.close()
+    if plain:
+        gw["speedup"] = gw["batched"]["value"] / gw["plain"]["value"]
+    if cpu:
+        try:
+            progress("evolution: FP64 CPU baseline")
+            ce = CpuEvolution(3)
+            sec = ce.substep()
+            gw["cpu_fp64"] = {"value": ce.zones / sec, "unit": UNIT, "cores": ce.cores, "kind": "port",
+                              "sample": f"one finest substep of the FP64 oracle over all {ce.used} domains, "
+                                        f"{sec:.2f} s"}
+        except Exception as e:   # no fixture or oracle library
+            gw["cpu_fp64"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    return gw
+
+
+def binary_report(am, E, estimator_path, bmode: int, plain: bool) -> dict:
+    path = estimator_path or os.path.join(ROOT, "adaptivemesh_gb300", "data", "estimator_binary16.npz")
+    if os.path.exists(path):
+        est, (a, b), meta = E.load_trained(path)
+        origin = "trained weights " + os.path.relpath(path, ROOT)
+    else:
+        progress("evolution: training the estimator (no trained weights found)")
+        est, (a, b), meta = E.train_default(n_seeds=10, held_out=2, epochs=40)
+        origin = "trained in this run on 8 seeded configurations"
+    tol = meta["target_quantiles"][1]            # log10 error tolerance: the training targets' 80th percentile
+    params = am.Regrid(refine_threshold=float(10 ** ((tol - a) / b)),
+                       coarsen_threshold=float(10 ** ((tol - 1.5 - a) / b)),
+                       learned_refine=tol, learned_coarsen=tol - 1.5, judge_factor=4.0, max_depth=5, min_depth=2)
+    punct = E.binary_punctures(1001)
+    bi = {"estimator": origin, "log10_error_tolerance": tol, "calibration": [a, b],
+          "estimator_val_mse": {"network": meta["val_mse_network"],
+                                "calibrated_indicator": meta["val_mse_calibrated_indicator"]}}
+    for name, net in (("learned", est), ("plain_criterion", None)):
+        progress(f"evolution: binary punctures, {name}")
+        sim = E.build_sim(16, 32.0, punct, 4, mode=bmode)
+        sim.timestep()                                   # warm-up
+        sim.synchronize()
+        zc, regrids = 0, []
+        t0 = time.perf_counter()
+        for step in range(16):
+            if step % 8 == 0:
+                regrids.append(sim.regrid(params, net))
+            zc += zone_cycles_per_root_step(sim.state(), 16)
+            sim.timestep()
+        sim.synchronize()
+        sec = time.perf_counter() - t0
+        norms = sim.constraint_norms(1.0)
+        st = sim.state()
+        bi[name] = {"value": zc / sec, "ms_per_root_step": sec * 1e3 / 16, "root_steps": 16,
+                    "leaves": regrids[-1]["leaves"], "regrids": regrids,
+                    **{k: v for k, v in norms.items() if k != "cells"}}
+        if net is None and plain:   # the plain per-domain launches on this tree: one root step
+            progress("evolution: binary punctures, plain per-domain launches")
+            sim.set_mode(am.MODE_PLAIN)
+            sim.synchronize()
+            z1 = zone_cycles_per_root_step(st, 16)
+            sim.event_record(0)
+            sim.timestep()
+            sim.event_record(1)
+            sim.synchronize()
+            ms = sim.event_elapsed(0, 1)
+            bi["plain_launches"] = {"value": z1 / (ms / 1e3), "ms_per_root_step": ms, "root_steps": 1}
+        sim.close()
+    est.close()
+    if plain:
+        bi["speedup_learned_batched_vs_plain_launches"] = bi["learned"]["value"] / bi["plain_launches"]["value"]
+    return bi
+
+
+def evolution_line(args) -> None:
+    """--plugin evolution: the evolution's report as its own line."""
+    rep = evolution_report(cpu=not args.no_cpu_baseline, estimator_path=args.estimator, case=args.evo_case,
+                           batched_mode="batched" if args.mode == "batched" else "graph", plain=not args.no_plain)
+    bi = rep.get("binary")
+    print(json.dumps({"metric": "BSSN zone-cycles/s at fixed constraint error, batched+learned vs plain",
+                      "value": bi["learned"]["value"] if bi else None, "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+                      "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "full BSSN evolution, binary Brill-Lindquist punctures with learned "
+                                             "regridding (and the gauge wave on 128^3)"},
+                      "evolution": rep}))
+
+
 def main() -> None:
     global N, P
     ap = argparse.ArgumentParser()
@@ -300,12 +489,21 @@ def main() -> None:
     ap.add_argument("--depth", type=int, default=DEPTH, help="uniform octree depth (3 = the benchmark workload)")
     ap.add_argument("--size", type=int, default=N, help="size_domain (16 = the benchmark workload; 8, 16, 28, 32)")
     ap.add_argument("--padding", type=int, default=P, help="padding_domain (3 = the benchmark workload)")
-    ap.add_argument("--plugin", default="bssn", choices=["bssn", "wave"],
-                    help="wave: time the SimpleWave plugin instead (an extra line, not the benchmark)")
+    ap.add_argument("--plugin", default="bssn", choices=["bssn", "wave", "evolution"],
+                    help="wave: time the SimpleWave plugin instead (an extra line, not the benchmark); "
+                         "evolution: the full BSSN evolution's report alone")
+    ap.add_argument("--no-evolution", action="store_true", help="leave out the evolution's report")
+    ap.add_argument("--estimator", default=None, help="trained estimator weights (.npz) for the evolution's report")
+    ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "binary"],
+                    help="--plugin evolution: the configurations to run")
+    ap.add_argument("--no-plain", action="store_true", help="--plugin evolution: leave out the plain launches")
     args = ap.parse_args()
     N, P = args.size, args.padding
     if args.plugin == "wave":
         wave_line(args)
+        return
+    if args.plugin == "evolution":
+        evolution_line(args)
         return
     if args.impl == "reference":
         reference_arm(args)

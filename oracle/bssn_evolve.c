@@ -474,6 +474,8 @@ static void rk_stage(const orc_evo* e, double* const* in, double* const* out, do
                         case 3: acc[f][ii] += dt / 3 * r; out[f][o] = uo + dt * r; break;
                         default: out[f][o] = acc[f][ii] + dt / 6 * r; break;
                     }
+                    /* the conformal factor is kept at or above its floor (a NaN stays a NaN) */
+                    if (e->physics == 0 && f == CHI && out[f][o] < e->chi_floor) out[f][o] = e->chi_floor;
                 }
             }
     }

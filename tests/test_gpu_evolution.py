@@ -202,7 +202,9 @@ def test_modes_agree(am, cuda):
 def test_new_domains_are_prolongated_to_fourth_order(am, cuda):
     """A domain added to an evolution takes its padded cells from its parent by tricubic
     interpolation: a cubic polynomial in the parent's padded cells (ghost layer included) is
-    reproduced exactly, to single-precision rounding, in every cell of each child, ghosts included."""
+    reproduced exactly, to single-precision rounding, in every cell of each child, ghosts included.
+    The conformal factor and the lapse are interpolated through their fourth and square roots: chi =
+    q^4 and alpha = q^2 with q linear are reproduced exactly."""
     import torch
     n, p = 8, 3
     t = n + 2 * p
@@ -214,6 +216,9 @@ def test_new_domains_are_prolongated_to_fourth_order(am, cuda):
     z, y, x = torch.meshgrid(ix, ix, ix, indexing="ij")
 
     def cubic(x, y, z, f):
+        if f in (am.F_CHI, am.F_ALPHA):   # stored less 1; q = 0.2 + 0.03 x + 0.02 y + 0.01 z > 0
+            q = 0.2 + 0.03 * x + 0.02 * y + 0.01 * z
+            return (q ** 4 if f == am.F_CHI else q ** 2) - 1.0
         return 0.1 * f + 1e-3 * (x ** 3 - 2 * y ** 2 * z + 3 * x * y * z + z ** 3 / 4 - 5 * x + 7)
 
     for f in range(24):
@@ -229,7 +234,7 @@ def test_new_domains_are_prolongated_to_fourth_order(am, cuda):
         oc = [(o >> a) & 1 for a in range(3)]
         # child cell w sits at parent coordinate o * n / 2 + p + (w - p + 1/2) / 2 - 1/2
         px, py, pz = [oc[a] * (n // 2) + p + ((c - p + 0.5) / 2 - 0.5) for a, c in enumerate((x, y, z))]
-        for f in (0, 5, 17, 23):
+        for f in (0, 5, 12, 17, 23):
             want = cubic(px, py, pz, f)
             for buf in (sim.OLD_STATE, sim.NEW_STATE):
                 got = sim.tensor(buf, f)[child * t ** 3:(child + 1) * t ** 3].double().reshape(t, t, t)
