@@ -367,6 +367,8 @@ def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: 
         out["gauge_wave"] = gauge_wave_report(am, cases, bmode, cpu, plain)
     if case in ("all", "binary"):
         out["binary"] = binary_report(am, E, estimator_path, bmode, plain)
+    if case == "pareto":
+        out["pareto"] = pareto_report(am, E, estimator_path, bmode)
     return out
 
 
@@ -410,6 +412,53 @@ def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool) -> dict:
     return gw
 
 
+def binary_run(am, E, punct, params, net, bmode: int, steps: int = 16) -> tuple[dict, object]:
+    """One binary-puncture run: regrid every 8 root steps (before steps 0 and 8) by `net` judged by
+    the plain criterion, or by the plain criterion alone (net None); the simulation is returned open."""
+    sim = E.build_sim(16, 32.0, punct, 4, mode=bmode)
+    sim.timestep()                                   # warm-up
+    sim.synchronize()
+    zc, regrids = 0, []
+    t0 = time.perf_counter()
+    for step in range(steps):
+        if step % 8 == 0:
+            regrids.append(sim.regrid(params, net))
+        zc += zone_cycles_per_root_step(sim.state(), 16)
+        sim.timestep()
+    sim.synchronize()
+    sec = time.perf_counter() - t0
+    norms = sim.constraint_norms(1.0)
+    return ({"value": zc / sec, "ms_per_root_step": sec * 1e3 / steps, "root_steps": steps,
+             "leaves": regrids[-1]["leaves"], "regrids": regrids,
+             **{k: v for k, v in norms.items() if k != "cells"}}, sim)
+
+
+def regrid_params(am, tol: float, a: float, b: float):
+    """Thresholds aiming at log10 error `tol`: the network's directly, the plain indicator's through
+    the calibration log10(error) ~ a + b log10(indicator); coarsening 1.5 decades below."""
+    return am.Regrid(refine_threshold=float(10 ** ((tol - a) / b)), coarsen_threshold=float(10 ** ((tol - 1.5 - a) / b)),
+                     learned_refine=tol, learned_coarsen=tol - 1.5, judge_factor=4.0, max_depth=5, min_depth=2)
+
+
+def pareto_report(am, E, estimator_path, bmode: int) -> dict:
+    """Leaves and constraint norms of both criteria over a range of error tolerances."""
+    est, (a, b), meta = E.load_trained(estimator_path or os.path.join(ROOT, "adaptivemesh_gb300", "data",
+                                                                      "estimator_binary16.npz"))
+    punct = E.binary_punctures(1001)
+    out = []
+    q50, q80, q90 = meta["target_quantiles"]
+    for tol in (q50, 0.5 * (q50 + q80), q80, q90):   # the training targets' percentiles
+        row = {"log10_tolerance": tol}
+        for name, net in (("learned", est), ("plain_criterion", None)):
+            progress(f"pareto: tolerance {tol:.2f}, {name}")
+            r, sim = binary_run(am, E, punct, regrid_params(am, tol, a, b), net, bmode)
+            sim.close()
+            row[name] = {k: r[k] for k in ("leaves", "H_l2", "M_l2", "value")}
+        out.append(row)
+    est.close()
+    return {"rows": out}
+
+
 def binary_report(am, E, estimator_path, bmode: int, plain: bool) -> dict:
     path = estimator_path or os.path.join(ROOT, "adaptivemesh_gb300", "data", "estimator_binary16.npz")
     if os.path.exists(path):
@@ -420,34 +469,17 @@ def binary_report(am, E, estimator_path, bmode: int, plain: bool) -> dict:
         est, (a, b), meta = E.train_default(n_seeds=10, held_out=2, epochs=40)
         origin = "trained in this run on 8 seeded configurations"
     tol = meta["target_quantiles"][1]            # log10 error tolerance: the training targets' 80th percentile
-    params = am.Regrid(refine_threshold=float(10 ** ((tol - a) / b)),
-                       coarsen_threshold=float(10 ** ((tol - 1.5 - a) / b)),
-                       learned_refine=tol, learned_coarsen=tol - 1.5, judge_factor=4.0, max_depth=5, min_depth=2)
+    params = regrid_params(am, tol, a, b)
     punct = E.binary_punctures(1001)
     bi = {"estimator": origin, "log10_error_tolerance": tol, "calibration": [a, b],
           "estimator_val_mse": {"network": meta["val_mse_network"],
                                 "calibrated_indicator": meta["val_mse_calibrated_indicator"]}}
     for name, net in (("learned", est), ("plain_criterion", None)):
         progress(f"evolution: binary punctures, {name}")
-        sim = E.build_sim(16, 32.0, punct, 4, mode=bmode)
-        sim.timestep()                                   # warm-up
-        sim.synchronize()
-        zc, regrids = 0, []
-        t0 = time.perf_counter()
-        for step in range(16):
-            if step % 8 == 0:
-                regrids.append(sim.regrid(params, net))
-            zc += zone_cycles_per_root_step(sim.state(), 16)
-            sim.timestep()
-        sim.synchronize()
-        sec = time.perf_counter() - t0
-        norms = sim.constraint_norms(1.0)
-        st = sim.state()
-        bi[name] = {"value": zc / sec, "ms_per_root_step": sec * 1e3 / 16, "root_steps": 16,
-                    "leaves": regrids[-1]["leaves"], "regrids": regrids,
-                    **{k: v for k, v in norms.items() if k != "cells"}}
+        bi[name], sim = binary_run(am, E, punct, params, net, bmode)
         if net is None and plain:   # the plain per-domain launches on this tree: one root step
             progress("evolution: binary punctures, plain per-domain launches")
+            st = sim.state()
             sim.set_mode(am.MODE_PLAIN)
             sim.synchronize()
             z1 = zone_cycles_per_root_step(st, 16)
@@ -456,7 +488,8 @@ def binary_report(am, E, estimator_path, bmode: int, plain: bool) -> dict:
             sim.event_record(1)
             sim.synchronize()
             ms = sim.event_elapsed(0, 1)
-            bi["plain_launches"] = {"value": z1 / (ms / 1e3), "ms_per_root_step": ms, "root_steps": 1}
+            bi["plain_launches"] = {"value": z1 / (ms / 1e3), "ms_per_root_step": ms, "root_steps": 1,
+                                    "leaves": bi[name]["leaves"]}
         sim.close()
     est.close()
     if plain:
@@ -494,7 +527,7 @@ def main() -> None:
                          "evolution: the full BSSN evolution's report alone")
     ap.add_argument("--no-evolution", action="store_true", help="leave out the evolution's report")
     ap.add_argument("--estimator", default=None, help="trained estimator weights (.npz) for the evolution's report")
-    ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "binary"],
+    ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "binary", "pareto"],
                     help="--plugin evolution: the configurations to run")
     ap.add_argument("--no-plain", action="store_true", help="--plugin evolution: leave out the plain launches")
     args = ap.parse_args()
@@ -690,8 +723,6 @@ def main() -> None:
                                      "sample": f"the last timed step recomputed by the FP32 restatement, {t32:.2f} s"}
         except ValueError as e:   # no fixture of this tree depth
             line["parity"] = f"unchecked: {e}"
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     # release every torch object that refers to the simulation's memory or stream first
     torch.cuda.synchronize()
     del h_in, h_out
@@ -699,6 +730,15 @@ def main() -> None:
     gc.collect()
     torch.cuda.synchronize()
     sim.close()
+    if rank == 0 and world == 1 and not args.no_evolution:
+        # the full BSSN evolution's throughput at fixed constraint error, batched+learned against the
+        # plain per-domain launches (not part of the timed region above)
+        try:
+            line["evolution"] = evolution_report(cpu=not args.no_cpu_baseline, estimator_path=args.estimator)
+        except Exception as e:
+            line["evolution"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 
