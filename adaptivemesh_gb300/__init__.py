@@ -163,6 +163,8 @@ EXPORTS = {
     "amr_sim_synchronize": (ctypes.c_int, [VP]),
     "amr_sim_kernel_launches": (U64, [VP]),
     "amr_sim_set_stencil_ctas": (ctypes.c_int, [VP, U32]),
+    "amr_sim_autotune": (ctypes.c_int, [VP, U32, VP]),
+    "amr_sim_tuned_shapes": (ctypes.c_int, [VP, U32, VP, VP, VP]),
     "amr_sim_set_fault_injection": (ctypes.c_int, [VP, U32, U32]),
     "amr_sim_set_evolution": (ctypes.c_int, [VP, VP]),
     "amr_sim_initial_data": (ctypes.c_int, [VP, VP]),

@@ -161,10 +161,10 @@ __device__ __forceinline__ void geometry(const float* u, const DV& dv, const Evo
             tr_dd += G.gi[i][j] * ddchi[sidx(i, j)];
             dchi2 += G.gi[i][j] * G.dchi[i] * G.dchi[j];
         }
-    // Ricci tensor
-#pragma unroll 1
+    // Ricci tensor (unrolled: every index is a constant, so the geometry stays in registers)
+#pragma unroll
     for (int i = 0; i < 3; i++)
-#pragma unroll 1
+#pragma unroll
         for (int j = i; j < 3; j++) {
             const int ij = sidx(i, j);
             float r = 0.f;

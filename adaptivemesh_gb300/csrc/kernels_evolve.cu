@@ -72,6 +72,13 @@ struct DerivShape {
     static constexpr uint32_t SLAB_BYTES = SLAB * 4u;
     static constexpr size_t SMEM = 2u * SLAB_BYTES + 64u;
     static_assert(CELLS % THREADS == 0 && N % ZS == 0, "whole cells per thread and planes per slab");
+    // The row of a cell.  At N = 16 a warp would cover rows y and y + 1 of the 22-float padded
+    // rows, whose shared-memory banks overlap for 6 lanes; rows y and y + 8 (176 floats = 16 banks
+    // apart) make every tap of the warp conflict-free.
+    __device__ static uint32_t row(uint32_t cell) {
+        const uint32_t r = (cell / N) % N;
+        return N == 16 ? (r >> 1) | ((r & 1u) << 3) : r;
+    }
     static_assert(SLAB_BYTES % 16u == 0u && (T * T * 4) % 16 == 0, "slabs are aligned bulk copies");
 };
 
@@ -83,7 +90,7 @@ __device__ __forceinline__ int deriv_field_order(int physics, int i) {
 }
 
 template <int N>
-__global__ void __launch_bounds__(DerivShape<N>::THREADS) k_evo_derivs(const __grid_constant__ EvoArgs a) {
+__global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo_derivs(const __grid_constant__ EvoArgs a) {
     using S = DerivShape<N>;
     constexpr int T = S::T, ZS = S::ZS, CPT = S::CPT;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -125,7 +132,7 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS) k_evo_derivs(const __g
 #pragma unroll
     for (int c = 0; c < CPT; c++) {
         const uint32_t cell = tid + (uint32_t)c * S::THREADS;
-        const uint32_t x = cell % N, y = (cell / N) % N, z = slab * ZS + cell / (N * N);
+        const uint32_t x = cell % N, y = S::row(cell), z = slab * ZS + cell / (N * N);
         const size_t pi = (size_t)slot * T * T * T + ((size_t)(z + 3) * T + (y + 3)) * T + (x + 3);
 #pragma unroll
         for (int k = 0; k < 3; k++) beta[c][k] = bssn ? a.fields[F_BETAX + k][pi] : 0.f;
@@ -144,7 +151,7 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS) k_evo_derivs(const __g
 #pragma unroll
         for (int c = 0; c < CPT; c++) {
             const uint32_t cell = tid + (uint32_t)c * S::THREADS;
-            const uint32_t x = cell % N, y = (cell / N) % N, zl = cell / (N * N);
+            const uint32_t x = cell % N, y = S::row(cell), zl = cell / (N * N);
             const uint32_t z = slab * ZS + zl;
             const float* q = tile + ((zl + 3) * T + (y + 3)) * T + (x + 3);
             const uint64_t o = ((uint64_t)slot * N + z) * N * N + (uint64_t)y * N + x;
@@ -248,32 +255,69 @@ __device__ __forceinline__ void rk_update(const EvoArgs& a, int f, uint64_t pi, 
     a.out[f][pi] = v < lo ? lo : v;
 }
 
+// BSSN right-hand side and RK stage update: a CTA per kRhsCells consecutive interior cells of one
+// domain.  The cells' BSSN_ND derivative values arrive in shared memory as one bulk copy per
+// derivative plane (kRhsCells * 4 bytes, contiguous in the inner layout), all issued at once by
+// thread 0 and counted on one mbarrier, while every thread loads its cell's fields; the
+// right-hand side then reads its derivatives from shared memory (consecutive threads read
+// consecutive words).
+constexpr int kRhsCells = 128;
+constexpr size_t kRhsSmem = (size_t)BSSN_ND * kRhsCells * 4u + 16u;
+
 template <int N>
-__global__ void __launch_bounds__(128) k_evo_rhs_bssn(const __grid_constant__ EvoArgs a) {
+__global__ void __launch_bounds__(kRhsCells) k_evo_rhs_bssn(const __grid_constant__ EvoArgs a) {
     constexpr int P = 3, T = N + 2 * P;
-    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (uint64_t)a.n_items * N * N * N) return;
-    const uint32_t item = (uint32_t)(gid / (N * N * N)), cell = (uint32_t)(gid % (N * N * N));
+    constexpr uint32_t CHUNKS = (uint32_t)(N * N * N / kRhsCells);
+    static_assert((N * N * N) % kRhsCells == 0 && (kRhsCells * 4) % 16 == 0, "whole, aligned chunks per domain");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float* sd = reinterpret_cast<float*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)BSSN_ND * kRhsCells * 4u);
+    const uint32_t tid = threadIdx.x;
+    const uint32_t item = blockIdx.x / CHUNKS, chunk = blockIdx.x % CHUNKS;
+    if (item >= a.n_items) return;   // the whole CTA
     const uint32_t slot = a.items[item];
+    const uint32_t cell = chunk * (uint32_t)kRhsCells + tid;
+    const uint64_t ii0 = (uint64_t)slot * N * N * N + chunk * (uint32_t)kRhsCells;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(bar, (uint32_t)(BSSN_ND * kRhsCells * 4));
+        for (int k = 0; k < BSSN_ND; k++)
+            bulk_g2s(sd + k * kRhsCells, a.deriv + (uint64_t)k * a.deriv_stride + ii0, kRhsCells * 4u, bar);
+    }
     const uint32_t x = cell % N, y = (cell / N) % N, z = cell / (N * N);
     const int depth = pos_depth(a.positions[slot]);
     const float dt = a.dt0 / (float)(1u << depth);
     const uint64_t pi = (uint64_t)slot * T * T * T + ((uint64_t)(z + P) * T + (y + P)) * T + (x + P);
-    const uint64_t ii = (uint64_t)slot * N * N * N + cell;
-    float u[BSSN_NF];
+    const uint64_t ii = ii0 + tid;
+    float u[BSSN_NF], uo[BSSN_NF];
 #pragma unroll
-    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi] + bssn_offset(f);
-    const float* D = a.deriv;
-    const uint64_t ds = a.deriv_stride;
-    auto dv = [&](int k) { return D[(uint64_t)k * ds + ii]; };
+    for (int f = 0; f < BSSN_NF; f++) {
+        const float s = a.fields[f][pi];   // the stored form
+        u[f] = s + bssn_offset(f);
+        uo[f] = a.stage == 1 ? s : a.old_f[f][pi];
+    }
+    // every copy lands before any thread reads shared memory or leaves (bounded waits)
+    const bool ok = __syncthreads_and(mbar_wait(bar, 0));
+    if (!ok) {
+        if (tid == 0) {
+            atomicExch(a.err, 1);
+            mbar_wait(bar, 0);
+        }
+        __syncthreads();
+        return;
+    }
+    auto dv = [&](int k) { return sd[k * kRhsCells + tid]; };
     float rhs[BSSN_NF];
     bssn_rhs(u, dv, a.prm, rhs);
-#pragma unroll 1
+#pragma unroll
     for (int f = 0; f < BSSN_NF; f++) {
         const float r = rhs[f] + dv(D_EXTRA + f);
-        const float uo = a.stage == 1 ? a.fields[f][pi] : a.old_f[f][pi];   // the stored form
         // chi (stored less 1) is kept at or above its floor, as the geometry divides by it
-        rk_update(a, f, pi, ii, uo, r, dt, f == F_CHI ? a.prm.chi_floor - 1.f : -INFINITY);
+        rk_update(a, f, pi, ii, uo[f], r, dt, f == F_CHI ? a.prm.chi_floor - 1.f : -INFINITY);
     }
 }
 
@@ -299,9 +343,16 @@ __global__ void __launch_bounds__(256) k_evo_rhs_wave(const __grid_constant__ Ev
 }
 
 // ------------------------------------------------------------------ ghost fill
-__global__ void __launch_bounds__(256) k_evo_ghost(const __grid_constant__ EvoGhostArgs g) {
+// A CTA per (slot, side, group of kGhostFields fields): the geometry of a ghost cell is computed
+// once per group, and every load of a cell's group is issued before its stores.  Within one launch
+// (one face-normal axis) no cell is both read and written: the fill writes the cells whose index
+// along the axis lies in a ghost layer and reads sources inside the interior along it.
+constexpr int kGhostFields = 4;
+
+__global__ void __launch_bounds__(256, 4) k_evo_ghost(const __grid_constant__ EvoGhostArgs g) {
     const uint32_t item = blockIdx.x >> 1, side = blockIdx.x & 1u;   // side 0: + face, 1: - face
-    if (item >= g.n_items) return;
+    const int f0 = (int)blockIdx.y * kGhostFields;
+    if (item >= g.n_items || f0 >= g.nf) return;
     const uint32_t slot = g.items[item];
     const uint32_t n = g.n, p = g.p, t = g.t, d = (uint32_t)g.axis;
     const uint32_t face = d + 3u * side;
@@ -326,76 +377,89 @@ __global__ void __launch_bounds__(256) k_evo_ghost(const __grid_constant__ EvoGh
         const uint32_t kp = (g.substep >> (g.max_depth - (uint32_t)cd)) & ((1u << dd) - 1u);
         frac = ((float)kp + g.c_stage) / (float)(1u << dd);
     }
+    const bool use0 = mode != 1, use1 = mode != 0;   // which of the two source states are read
     const float3 relp = cf3_decode((uint32_t)(bd >> 32));
-    const float rel[3] = {relp.x, relp.y, relp.z};
     const float rel_scale = 1.f / (float)(1u << dd);
     // extents of the fill: axes before d over the whole padded range (their ghosts are filled),
     // axes after d over the interior
-    uint32_t lo[3], ext[3];
-    for (uint32_t a2 = 0; a2 < 3; a2++) {
-        if (a2 == d) { lo[a2] = side == 0 ? p + n : 0; ext[a2] = p; }
-        else if (a2 < d) { lo[a2] = 0; ext[a2] = t; }
-        else { lo[a2] = p; ext[a2] = n; }
-    }
-    const uint32_t count = ext[0] * ext[1] * ext[2];
+    auto lo_of = [&](uint32_t a2) { return a2 == d ? (side == 0 ? p + n : 0u) : (a2 < d ? 0u : p); };
+    auto ext_of = [&](uint32_t a2) { return a2 == d ? p : (a2 < d ? t : n); };
+    const uint32_t lo0 = lo_of(0), lo1 = lo_of(1), lo2 = lo_of(2);
+    const uint32_t ext0 = ext_of(0), ext1 = ext_of(1), ext2 = ext_of(2);
+    const int nfg = min(kGhostFields, g.nf - f0);
+    // field of group member q (members past the last field repeat it; they are never stored)
+    auto fld = [&](int q) { return f0 + min(q, nfg - 1); };
+    auto A0 = [&](int q) { return g.old_f[fld(q)]; };
+    auto A1 = [&](int q) { return mode == 3 ? g.new_f[fld(q)] : (const float*)g.X[fld(q)]; };
+    const uint32_t count = ext0 * ext1 * ext2;
     const uint64_t cells = (uint64_t)t * t * t;
+    const bool exact = dd == 0u;
     for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) {
-        const uint32_t w[3] = {lo[0] + k % ext[0], lo[1] + (k / ext[0]) % ext[1], lo[2] + k / (ext[0] * ext[1])};
-        const uint64_t dst = (uint64_t)slot * cells + ((uint64_t)w[2] * t + w[1]) * t + w[0];
+        const uint32_t w0 = lo0 + k % ext0, w1 = lo1 + (k / ext0) % ext1, w2 = lo2 + k / (ext0 * ext1);
+        const uint64_t dst = (uint64_t)slot * cells + ((uint64_t)w2 * t + w1) * t + w0;
         // source cell (same depth: the cell itself) or the base cell b of a tricubic stencil b-1 .. b+2
         // kept inside the cells that are valid: the interior along the normal axis and the later
         // axes, the whole padded range along the earlier axes (filled by earlier passes) and
         // everywhere in the root (its frozen ghost layer is the outer boundary)
         int idx[3];
         float wgt[3][4];
-        const bool exact = dd == 0u;
-        for (uint32_t a2 = 0; a2 < 3; a2++) {
-            float rp = ((float)w[a2] - (float)p + .5f) / (float)n - .5f;
-            rp = rp * rel_scale + rel[a2];
+        auto axis_taps = [&](uint32_t a2, uint32_t wa, float rela) {
+            float rp = ((float)wa - (float)p + .5f) / (float)n - .5f;
+            rp = rp * rel_scale + rela;
             const float ri = (rp + .5f) * (float)n + (float)p - .5f;
             if (exact) {
                 idx[a2] = __float2int_rn(ri);
-                continue;
-            }
-            const int lo_c = root_src || a2 < d ? 1 : (int)p + 1;
-            const int hi_c = root_src || a2 < d ? (int)t - 3 : (int)(t - p) - 3;
-            int b = __float2int_rd(ri);
-            b = b < lo_c ? lo_c : (b > hi_c ? hi_c : b);
-            const float x = ri - (float)b;
-            idx[a2] = b;
-            wgt[a2][0] = -x * (x - 1.f) * (x - 2.f) * (1.f / 6.f);
-            wgt[a2][1] = (x + 1.f) * (x - 1.f) * (x - 2.f) * .5f;
-            wgt[a2][2] = -(x + 1.f) * x * (x - 2.f) * .5f;
-            wgt[a2][3] = (x + 1.f) * x * (x - 1.f) * (1.f / 6.f);
-        }
-        const int64_t si = (int64_t)src * (int64_t)cells + ((int64_t)idx[2] * t + idx[1]) * t + idx[0];
-        for (int f = 0; f < g.nf; f++) {
-            const float* A0 = g.old_f[f];
-            const float* A1 = mode == 3 ? g.new_f[f] : g.X[f];
-            float va = 0.f, vb = 0.f;
-            if (exact) {
-                va = A0[si];
-                vb = A1[si];
             } else {
+                const int lo_c = root_src || a2 < d ? 1 : (int)p + 1;
+                const int hi_c = root_src || a2 < d ? (int)t - 3 : (int)(t - p) - 3;
+                int b = __float2int_rd(ri);
+                b = b < lo_c ? lo_c : (b > hi_c ? hi_c : b);
+                const float x = ri - (float)b;
+                idx[a2] = b;
+                wgt[a2][0] = -x * (x - 1.f) * (x - 2.f) * (1.f / 6.f);
+                wgt[a2][1] = (x + 1.f) * (x - 1.f) * (x - 2.f) * .5f;
+                wgt[a2][2] = -(x + 1.f) * x * (x - 2.f) * .5f;
+                wgt[a2][3] = (x + 1.f) * x * (x - 1.f) * (1.f / 6.f);
+            }
+        };
+        axis_taps(0, w0, relp.x);
+        axis_taps(1, w1, relp.y);
+        axis_taps(2, w2, relp.z);
+        const int64_t si = (int64_t)src * (int64_t)cells + ((int64_t)idx[2] * t + idx[1]) * t + idx[0];
+        float va[kGhostFields], vb[kGhostFields];
 #pragma unroll
-                for (int k2 = 0; k2 < 4; k2++)
+        for (int q = 0; q < kGhostFields; q++) { va[q] = 0.f; vb[q] = 0.f; }
+        if (exact) {
 #pragma unroll
-                    for (int k1 = 0; k1 < 4; k1++) {
-                        const float w12 = wgt[1][k1] * wgt[2][k2];
-                        const int64_t row = si + ((int64_t)(k2 - 1) * t + (k1 - 1)) * t - 1;
+            for (int q = 0; q < kGhostFields; q++) {
+                if (use0) va[q] = A0(q)[si];
+                if (use1) vb[q] = A1(q)[si];
+            }
+        } else {
 #pragma unroll
-                        for (int k0 = 0; k0 < 4; k0++) {
-                            const float wk = wgt[0][k0] * w12;
-                            va = fmaf(wk, A0[row + k0], va);
-                            if (mode != 0) vb = fmaf(wk, A1[row + k0], vb);
+            for (int k2 = 0; k2 < 4; k2++)
+#pragma unroll
+                for (int k1 = 0; k1 < 4; k1++) {
+                    const float w12 = wgt[1][k1] * wgt[2][k2];
+                    const int64_t row = si + ((int64_t)(k2 - 1) * t + (k1 - 1)) * t - 1;
+#pragma unroll
+                    for (int k0 = 0; k0 < 4; k0++) {
+                        const float wk = wgt[0][k0] * w12;
+#pragma unroll
+                        for (int q = 0; q < kGhostFields; q++) {
+                            if (use0) va[q] = fmaf(wk, A0(q)[row + k0], va[q]);
+                            if (use1) vb[q] = fmaf(wk, A1(q)[row + k0], vb[q]);
                         }
                     }
-            }
+                }
+        }
+#pragma unroll
+        for (int q = 0; q < kGhostFields; q++) {
             float v;
-            if (mode == 0) v = va;
-            else if (mode == 1) v = vb;
-            else v = fmaf(frac, vb, (1.f - frac) * va);
-            g.X[f][dst] = v;
+            if (mode == 0) v = va[q];
+            else if (mode == 1) v = vb[q];
+            else v = fmaf(frac, vb[q], (1.f - frac) * va[q]);
+            if (q < nfg) g.X[f0 + q][dst] = v;
         }
     }
 }
@@ -417,25 +481,43 @@ __global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ Ev
         const uint32_t tx = (x - p) / hn, ty = (y - p) / hn, tz = (z - p) / hn;   // unsigned wrap for ghosts
         const int32_t ch = (tx < 2u && ty < 2u && tz < 2u) ? g.children[tx + ty * 2u + tz * 4u + slot * 8u] : -1;
         const uint64_t o = slot * cells + ((uint64_t)z * t + y) * t + x;
+        // fields in groups, every load of a group before its stores (old and new are distinct buffers)
+        constexpr int G = 8;
         if (ch == -1) {
-            for (int f = 0; f < g.nf; f++) g.old_f[f][o] = g.new_f[f][o];
+            for (int f0 = 0; f0 < g.nf; f0 += G) {
+                float v[G];
+#pragma unroll
+                for (int q = 0; q < G; q++)
+                    if (f0 + q < g.nf) v[q] = g.new_f[f0 + q][o];
+#pragma unroll
+                for (int q = 0; q < G; q++)
+                    if (f0 + q < g.nf) g.old_f[f0 + q][o] = v[q];
+            }
             continue;
         }
         const uint32_t cx = ((x - p) * 2u) % n + p, cy = ((y - p) * 2u) % n + p, cz = ((z - p) * 2u) % n + p;
         const uint64_t base = (uint64_t)ch * cells + ((uint64_t)(cz - 1) * t + (cy - 1)) * t + (cx - 1);
-        for (int f = 0; f < g.nf; f++) {
-            const float* v = g.new_f[f];
-            float acc = 0.f;
+        constexpr int GI = 2;
+        for (int f0 = 0; f0 < g.nf; f0 += GI) {
+            float acc[GI];
+#pragma unroll
+            for (int q = 0; q < GI; q++) acc[q] = 0.f;
 #pragma unroll
             for (int k2 = 0; k2 < 4; k2++)
 #pragma unroll
                 for (int k1 = 0; k1 < 4; k1++) {
-                    float row = 0.f;
 #pragma unroll
-                    for (int k0 = 0; k0 < 4; k0++) row = fmaf(w4[k0], v[base + ((uint64_t)k2 * t + k1) * t + k0], row);
-                    acc = fmaf(w4[k1] * w4[k2], row, acc);
+                    for (int q = 0; q < GI; q++) {
+                        const float* v = g.new_f[min(f0 + q, g.nf - 1)];
+                        float row = 0.f;
+#pragma unroll
+                        for (int k0 = 0; k0 < 4; k0++) row = fmaf(w4[k0], v[base + ((uint64_t)k2 * t + k1) * t + k0], row);
+                        acc[q] = fmaf(w4[k1] * w4[k2], row, acc[q]);
+                    }
                 }
-            g.old_f[f][o] = acc;
+#pragma unroll
+            for (int q = 0; q < GI; q++)
+                if (f0 + q < g.nf) g.old_f[f0 + q][o] = acc[q];
         }
     }
 }
@@ -682,8 +764,14 @@ template <int N>
 static cudaError_t rhs_t(const EvoArgs& a, cudaStream_t st) {
     const uint64_t total = (uint64_t)a.n_items * N * N * N;
     if (total == 0) return cudaSuccess;
-    if (a.prm.physics == 0) k_evo_rhs_bssn<N><<<(unsigned)((total + 127) / 128), 128, 0, st>>>(a);
-    else k_evo_rhs_wave<N><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
+    if (a.prm.physics == 0) {
+        static std::atomic<uint64_t> configured{0};
+        const cudaError_t e = ensure_smem_limit(k_evo_rhs_bssn<N>, kRhsSmem, configured);
+        if (e != cudaSuccess) return e;
+        k_evo_rhs_bssn<N><<<(unsigned)(total / kRhsCells), kRhsCells, kRhsSmem, st>>>(a);
+    } else {
+        k_evo_rhs_wave<N><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
+    }
     return cudaGetLastError();
 }
 cudaError_t launch_evo_rhs(const EvoArgs& a, cudaStream_t st) {
@@ -703,7 +791,8 @@ cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st) {
 
 cudaError_t launch_evo_ghost(const EvoGhostArgs& g, cudaStream_t st) {
     if (g.n_items == 0) return cudaSuccess;
-    k_evo_ghost<<<g.n_items * 2u, 256, 0, st>>>(g);
+    const dim3 grid(g.n_items * 2u, (unsigned)((g.nf + kGhostFields - 1) / kGhostFields));
+    k_evo_ghost<<<grid, 256, 0, st>>>(g);
     return cudaGetLastError();
 }
 

@@ -7,6 +7,8 @@
 // launch per operator and component); BATCHED issues one launch per phase for all components over
 // the list of domains active at the substep; GRAPH replays a captured CUDA graph of one whole BSSN
 // timestep (all substeps).
+#include <algorithm>
+
 #include "sim_base.h"
 
 namespace amr {
@@ -129,6 +131,91 @@ public:
             case 4: *ptr = chr6[comp]; *count = s * dims.n * dims.n * dims.n; return AMR_OK;
             default: return AMR_ERR_INVALID;
         }
+    }
+
+    // The fused pass's grid, tuned per active-domain count of this octree: every distinct count of
+    // a timestep's substeps is timed at a set of candidate grids (CUDA events on the simulation's
+    // stream, the predictor's form with the leaves' restriction) and the fastest is kept.  The
+    // candidate launches read the metric and write only scratch buffers allocated here, so the
+    // simulation's state and outputs are left as they were.  Results do not depend on the grid.
+    int autotune(uint32_t reps, uint32_t* n_tuned) override {
+        if (n_tuned) *n_tuned = 0;
+        if (!bssn_fused_supported(&cfg) || capturing || reps == 0u || reps > 100u) return AMR_ERR_INVALID;
+        int st = wait_side(-1, 0);
+        if (!st) st = sync_octree();
+        if (!st) st = build_items();
+        if (st) return st;
+        const uint32_t md = (uint32_t)tree.read_max_depth(), nsub = 1u << md, used = tree.curr_used_slots();
+        const size_t padded = (size_t)used * dims.t * dims.t * dims.t, inner = (size_t)used * dims.n * dims.n * dims.n;
+        float* scratch = nullptr;
+        cudaError_t e = cudaMalloc(&scratch, sizeof(float) * (6u * padded + 18u * inner));
+        if (e != cudaSuccess) return cuda_status(e);
+        e = cudaMemsetAsync(scratch, 0, sizeof(float) * (6u * padded + 18u * inner), stream);
+        cudaEvent_t ev[2] = {nullptr, nullptr};
+        e = cudaEventCreate(&ev[0]);
+        if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+        int sms = 0, dev = 0;
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        std::vector<std::pair<uint32_t, uint32_t>> tuned;
+        for (uint32_t s = 0; s < nsub && e == cudaSuccess; s++) {
+            const uint32_t n = item_count[s];
+            bool seen = n == 0u;
+            for (const auto& t : tuned) seen |= t.first == n;
+            if (seen) continue;
+            StencilArgs a;
+            std::memset(&a, 0, sizeof(a));
+            a.positions = d_positions;
+            a.substep = s;
+            a.max_depth = md;
+            a.geo = geo;
+            a.err = err_flag;
+            a.christoffel_mode = AMR_CHRISTOFFEL_REFERENCE;
+            for (int k = 0; k < 6; k++) { a.seed_d[k] = 1 + k; a.seed_m[k] = 7 + k; }
+            a.seed_c = 13;
+            a.items = d_items + item_offset[s];
+            a.n_items = n;
+            for (int k = 0; k < 6; k++) {
+                a.field[k] = scratch + k * padded;   // read by domains with children, written for leaves
+                a.leaf_src[k] = new6[k];
+                a.grad[k] = reinterpret_cast<uint32_t*>(scratch + 6u * padded + k * inner);
+                a.lap[k] = scratch + 6u * padded + (6u + k) * inner;
+                a.chr[k] = reinterpret_cast<uint32_t*>(scratch + 6u * padded + (12u + k) * inner);
+            }
+            a.children = d_children;
+            // candidates: the library's rule, one and two CTAs per SM, and ranges of 2 to 64 planes
+            const uint32_t rule = stencil_grid(cfg, SK_BSSN, n), planes = n * dims.n;
+            std::vector<uint32_t> cand = {rule, (uint32_t)sms, 2u * (uint32_t)sms, 3u * (uint32_t)sms, 4u * (uint32_t)sms};
+            for (uint32_t r = 2; r <= 64; r *= 2) cand.push_back((planes + r - 1u) / r);
+            std::sort(cand.begin(), cand.end());
+            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+            uint32_t best = rule;
+            float best_ms = 0.f;
+            for (uint32_t g : cand) {
+                if (g == 0u || g > planes) continue;
+                e = launch_stencil(cfg, SK_BSSN, a, g, stream);   // warm-up
+                if (e == cudaSuccess) e = cudaEventRecord(ev[0], stream);
+                for (uint32_t r = 0; r < reps && e == cudaSuccess; r++) e = launch_stencil(cfg, SK_BSSN, a, g, stream);
+                if (e == cudaSuccess) e = cudaEventRecord(ev[1], stream);
+                if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+                if (e != cudaSuccess) break;
+                if (best_ms == 0.f || ms < best_ms) { best_ms = ms; best = g; }
+            }
+            tuned.emplace_back(n, best);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        cudaFree(scratch);
+        if (e != cudaSuccess) return cuda_status(e);
+        st = take_device_error(err_flag);   // a candidate whose waits gave up leaves the flag set
+        if (st) return st;
+        tuned_ctas = tuned;
+        graph_valid = false;
+        if (n_tuned) *n_tuned = (uint32_t)tuned.size();
+        return AMR_OK;
     }
 
 private:
@@ -923,6 +1010,18 @@ AMR_API int amr_sim_set_fault_injection(amr_sim* s, uint32_t spin_limit, uint32_
     return AMR_OK;
 }
 AMR_API uint64_t amr_sim_kernel_launches(const amr_sim* s) { return s ? s->impl->launches : 0u; }
+AMR_API int amr_sim_autotune(amr_sim* s, uint32_t reps, uint32_t* n_tuned) {
+    if (!s) return AMR_ERR_INVALID;
+    return s->impl->autotune(reps, n_tuned);
+}
+AMR_API int amr_sim_tuned_shapes(const amr_sim* s, uint32_t capacity, uint32_t* domains, uint32_t* ctas,
+                                 uint32_t* count) {
+    if (!s || !count || (capacity && (!domains || !ctas))) return AMR_ERR_INVALID;
+    const auto& t = s->impl->tuned_ctas;
+    *count = (uint32_t)t.size();
+    for (uint32_t i = 0; i < capacity && i < t.size(); i++) { domains[i] = t[i].first; ctas[i] = t[i].second; }
+    return t.size() > capacity ? AMR_ERR_CAPACITY : AMR_OK;
+}
 AMR_API int amr_sim_set_stencil_ctas(amr_sim* s, uint32_t ctas) {
     if (!s || ctas > (1u << 20)) return AMR_ERR_INVALID;
     s->impl->stencil_ctas = ctas;

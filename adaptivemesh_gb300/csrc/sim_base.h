@@ -108,6 +108,12 @@ public:
     // so every active domain has old == new outside the cells its children cover.
     bool in_timestep = false;
     virtual int buffer(int which, int comp, void** ptr, uint64_t* count) = 0;
+    // Launch-shape autotuning (amr_sim_autotune): only the BSSN plugin has a tunable pass.
+    virtual int autotune(uint32_t reps, uint32_t* n_tuned) {
+        (void)reps;
+        if (n_tuned) *n_tuned = 0;
+        return AMR_ERR_INVALID;
+    }
 
     void node_dtor(int32_t) override {}
     // Batched node_ctor: upload the deferred constructors once, then prolongate each group into

@@ -249,6 +249,21 @@ class Sim:
         """CTAs of the fused BSSN derivative pass (0: the library's choice)."""
         check(load().amr_sim_set_stencil_ctas(self.h, ctas), "amr_sim_set_stencil_ctas")
 
+    def autotune(self, reps: int = 3) -> dict:
+        """Tune the fused BSSN pass's grid for the current octree (amr_sim_autotune); returns
+        {active domains: CTAs}."""
+        n = ctypes.c_uint32(0)
+        check(load().amr_sim_autotune(self.h, reps, ctypes.byref(n)), "amr_sim_autotune")
+        return self.tuned_shapes()
+
+    def tuned_shapes(self) -> dict:
+        cap = 64
+        dom = (ctypes.c_uint32 * cap)()
+        ctas = (ctypes.c_uint32 * cap)()
+        cnt = ctypes.c_uint32(0)
+        check(load().amr_sim_tuned_shapes(self.h, cap, dom, ctas, ctypes.byref(cnt)), "amr_sim_tuned_shapes")
+        return {int(dom[i]): int(ctas[i]) for i in range(cnt.value)}
+
     # ---- evolution simulations (SIM_BSSN_EVOLVE, SIM_WAVE_RK4)
     OLD_STATE, NEW_STATE, STAGE, ACC, CONSTRAINTS, DERIVS = 0, 1, 2, 3, 4, 5
 

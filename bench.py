@@ -340,7 +340,7 @@ class CpuEvolution:
 
 
 def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: str = "all",
-                     batched_mode: str = "graph", plain: bool = True) -> dict:
+                     batched_mode: str = "graph", plain: bool = True, gw_depth: int = 3, gw_steps: int = 24) -> dict:
     """The full BSSN evolution's throughput (zone-cycles/s: leaf zones x steps at their own level)
     at fixed constraint error, batched (CUDA-graph replay of whole root steps) against the plain
     per-domain launches, which compute the same state bit for bit:
@@ -364,7 +364,7 @@ def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: 
     out = {}
     bmode = {"graph": am.MODE_GRAPH, "batched": am.MODE_BATCHED}[batched_mode]
     if case in ("all", "gauge_wave"):
-        out["gauge_wave"] = gauge_wave_report(am, cases, bmode, cpu, plain)
+        out["gauge_wave"] = gauge_wave_report(am, cases, bmode, cpu, plain, gw_depth, gw_steps)
     if case in ("all", "binary"):
         out["binary"] = binary_report(am, E, estimator_path, bmode, plain)
     if case == "pareto":
@@ -372,13 +372,13 @@ def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: 
     return out
 
 
-def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool) -> dict:
+def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool, depth: int = 3, steps_batched: int = 24) -> dict:
     gw = {}
-    arms = [("batched", bmode, 24)] + ([("plain", am.MODE_PLAIN, 1)] if plain else [])
+    arms = [("batched", bmode, steps_batched)] + ([("plain", am.MODE_PLAIN, 1)] if plain else [])
     for name, mode, steps in arms:
         progress(f"evolution: gauge wave, {name}")
-        sim = am.Sim(am.Config(16, 3, 1.0), am.SIM_BSSN_EVOLVE, slots=585, mode=mode)
-        cases.tree_uniform(sim, 3)
+        sim = am.Sim(am.Config(16, 3, 1.0), am.SIM_BSSN_EVOLVE, slots=sum(8 ** d for d in range(depth + 1)), mode=mode)
+        cases.tree_uniform(sim, depth)
         sim.set_evolution(am.Evolution(slicing=am.SLICING_1PLUSLOG, shift=0, ko_sigma=0.1, cfl=0.25, periodic=1))
         sim.initial_data(am.InitialData(kind=am.ID_GAUGE_WAVE, amplitude=1e-2, wavelength=1.0))
         sim.timestep()                       # warm-up (graph capture)
@@ -395,14 +395,14 @@ def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool) -> dict:
                     "gpu_launches_per_root_step": (sim.kernel_launches - l0) / steps}
         if name == "batched":
             gw[name].update({k: v for k, v in sim.constraint_norms().items() if k != "cells"})
-            gw[name]["finest_steps"] = 8 * (steps + 1)
+            gw[name]["finest_steps"] = (1 << depth) * (steps + 1)
         sim.close()
     if plain:
         gw["speedup"] = gw["batched"]["value"] / gw["plain"]["value"]
     if cpu:
         try:
             progress("evolution: FP64 CPU baseline")
-            ce = CpuEvolution(3)
+            ce = CpuEvolution(depth)
             sec = ce.substep()
             gw["cpu_fp64"] = {"value": ce.zones / sec, "unit": UNIT, "cores": ce.cores, "kind": "port",
                               "sample": f"one finest substep of the FP64 oracle over all {ce.used} domains, "
@@ -500,7 +500,8 @@ def binary_report(am, E, estimator_path, bmode: int, plain: bool) -> dict:
 def evolution_line(args) -> None:
     """--plugin evolution: the evolution's report as its own line."""
     rep = evolution_report(cpu=not args.no_cpu_baseline, estimator_path=args.estimator, case=args.evo_case,
-                           batched_mode="batched" if args.mode == "batched" else "graph", plain=not args.no_plain)
+                           batched_mode="batched" if args.mode == "batched" else "graph", plain=not args.no_plain,
+                           gw_depth=args.evo_depth, gw_steps=args.evo_steps)
     bi = rep.get("binary")
     print(json.dumps({"metric": "BSSN zone-cycles/s at fixed constraint error, batched+learned vs plain",
                       "value": bi["learned"]["value"] if bi else None, "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
@@ -526,10 +527,13 @@ def main() -> None:
                     help="wave: time the SimpleWave plugin instead (an extra line, not the benchmark); "
                          "evolution: the full BSSN evolution's report alone")
     ap.add_argument("--no-evolution", action="store_true", help="leave out the evolution's report")
+    ap.add_argument("--no-autotune", action="store_true", help="time the library's launch-shape rule, untuned")
     ap.add_argument("--estimator", default=None, help="trained estimator weights (.npz) for the evolution's report")
     ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "binary", "pareto"],
                     help="--plugin evolution: the configurations to run")
     ap.add_argument("--no-plain", action="store_true", help="--plugin evolution: leave out the plain launches")
+    ap.add_argument("--evo-depth", type=int, default=3, help="--plugin evolution: the gauge wave's uniform octree depth")
+    ap.add_argument("--evo-steps", type=int, default=24, help="--plugin evolution: the gauge wave's timed root steps")
     args = ap.parse_args()
     N, P = args.size, args.padding
     if args.plugin == "wave":
@@ -598,6 +602,24 @@ def main() -> None:
         sim.synchronize()
         if dist is not None:
             dist.barrier()
+
+    tune = None
+    if not args.no_autotune and mode != am.MODE_PLAIN:
+        # the same timesteps on the library's launch-shape rule first, then the fused pass's grid
+        # tuned for this octree (amr_sim_autotune), which the timed region below uses
+        progress("autotune")
+        for _ in range(args.warmup):
+            sim.timestep()
+        barrier()
+        sim.event_record(0)
+        for _ in range(args.steps):
+            sim.timestep()
+        sim.event_record(1)
+        barrier()
+        ms_rule = sim.event_elapsed(0, 1)
+        shapes = sim.autotune(3)
+        tune = {"ctas_by_active_domains": {str(k): v for k, v in sorted(shapes.items())},
+                "ms_per_step_library_rule": ms_rule / args.steps}
 
     progress("value: device-resident timesteps")
     # ---- device-resident timesteps (value); clocks are sampled from the warm-up on, through the
@@ -697,6 +719,9 @@ def main() -> None:
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": ms_e2e / args.steps},
             "gpu_launches": int(gpu_launches), "roofline": roofline, "clocks": clocks.summary()}
+    if tune:
+        tune["ms_per_step_tuned"] = ms / args.steps
+        line["autotune"] = tune
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         progress("cpu baseline and parity of the last timed step")
         try:

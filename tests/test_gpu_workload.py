@@ -192,6 +192,49 @@ def test_fused_pass_independent_of_grid(am, cuda, n, p):
                 same(got[k], v, f"{n}/{p} {label} vs auto: {k}")
 
 
+@pytest.mark.parametrize("mode", ["graph", "batched"])
+def test_autotune_leaves_state_and_results_unchanged(am, cuda, mode):
+    """amr_sim_autotune on the benchmark's 585-slot tree between timesteps: every buffer of the
+    simulation is bit-identical before and after it, it tunes every distinct active-domain count of
+    the substeps (585, 584, 576 and 512 here), and the next two timesteps on the tuned grids equal
+    those of an untuned simulation bit for bit."""
+    cfg = am.Config(16, 3, 100.0)
+    m = {"graph": am.MODE_GRAPH, "batched": am.MODE_BATCHED}[mode]
+    results = []
+    for tune in (False, True):
+        sim, st, _ = _uniform_sim(am, cfg, 3, m)
+        used = st["used_slots"]
+        sim.timestep()
+        sim.synchronize()
+        if tune:
+            before = dump(am, sim, used, cfg)
+            shapes = sim.autotune(2)
+            after = dump(am, sim, used, cfg)
+            for k, v in before.items():
+                if k != "rng":
+                    same(after[k], v, f"autotune changed {k}")
+            assert after["rng"] == before["rng"]
+            assert sorted(shapes) == [512, 576, 584, 585], shapes
+            assert all(c >= 1 for c in shapes.values())
+            assert sim.tuned_shapes() == shapes
+        sim.timestep()
+        sim.timestep()
+        sim.synchronize()
+        results.append(dump(am, sim, used, cfg))
+        sim.close()
+    for k, v in results[0].items():
+        if k != "rng":
+            same(results[1][k], v, f"tuned vs library grid: {k}")
+    assert results[1]["rng"] == results[0]["rng"]
+
+
+def test_autotune_rejects_other_kinds(am, cuda):
+    sim = am.Sim(am.Config(16, 3, 1.0), am.SIM_BSSN_EVOLVE, slots=9, mode=am.MODE_BATCHED)
+    with pytest.raises(RuntimeError):
+        sim.autotune(2)
+    sim.close()
+
+
 def test_bounded_wait_failure_is_reported_and_recovers(am, cuda):
     """The host tells each CTA's producer to skip its first plane request and shortens the data
     waits: the waits run out, the pass leaves (after every copy it issued has landed) and the
