@@ -63,22 +63,26 @@ constexpr int kMaxFields = 24;
 
 // Derivative scratch written by the derivative pass, one float per inner cell each (slot * N^3 +
 // cell).  Symmetric second derivatives in the order xx, yy, zz, xy, xz, yz; first derivatives
-// x, y, z.  EXTRA[f] is the advection term beta^k d_k u_f plus the Kreiss-Oliger term of field f.
+// x, y, z.  Where the right-hand side only uses a contraction with the inverse conformal metric,
+// the pass stores the contraction: GLAP[ij] = gt^lm d_l d_m gt_ij, BELAP[i] = gt^jk d_j d_k beta^i,
+// and DDIVB[j] = d_j d_k beta^k.  EXTRA[f] is the advection term beta^k d_k u_f plus the
+// Kreiss-Oliger term of field f.
 enum BssnDeriv : int {
     D_CHI1 = 0,                   // 3
     D_CHI2 = 3,                   // 6
     D_G1 = 9,                     // 6 components x 3
-    D_G2 = 27,                    // 6 components x 6
-    D_K1 = 63,                    // 3
-    D_GAM1 = 66,                  // 3 components x 3: d_j Gamma^i at D_GAM1 + 3 i + j
-    D_AL1 = 75,                   // 3
-    D_AL2 = 78,                   // 6
-    D_BE1 = 84,                   // 3 components x 3: d_j beta^i at D_BE1 + 3 i + j
-    D_BE2 = 93,                   // 3 components x 6
-    D_EXTRA = 111,                // 24
-    BSSN_ND = 135,
-    D_AT1 = 135,                  // constraint mode only: d_k A_ij at D_AT1 + 3 c + k (6 components)
-    BSSN_ND_CONSTRAINTS = 153
+    D_GLAP = 27,                  // 6
+    D_K1 = 33,                    // 3
+    D_GAM1 = 36,                  // 3 components x 3: d_j Gamma^i at D_GAM1 + 3 i + j
+    D_AL1 = 45,                   // 3
+    D_AL2 = 48,                   // 6
+    D_BE1 = 54,                   // 3 components x 3: d_j beta^i at D_BE1 + 3 i + j
+    D_BELAP = 63,                 // 3
+    D_DDIVB = 66,                 // 3
+    D_EXTRA = 69,                 // 24
+    BSSN_ND = 93,
+    D_AT1 = 93,                   // constraint mode only: d_k A_ij at D_AT1 + 3 c + k (6 components)
+    BSSN_ND_CONSTRAINTS = 111
 };
 enum WaveDeriv : int { WD_LAP = 0, WD_EXTRA = 1, WAVE_ND = 3 };
 

@@ -168,9 +168,8 @@ __device__ __forceinline__ void geometry(const float* u, const DV& dv, const Evo
         for (int j = i; j < 3; j++) {
             const int ij = sidx(i, j);
             float r = 0.f;
-            // -1/2 gt^lm d_l d_m gt_ij
-            for (int l = 0; l < 3; l++)
-                for (int m = 0; m < 3; m++) r -= .5f * G.gi[l][m] * dv(D_G2 + 6 * ij + didx(l, m));
+            // -1/2 gt^lm d_l d_m gt_ij (contracted by the derivative pass)
+            r -= .5f * dv(D_GLAP + ij);
             // gt_k(i d_j) Gt^k
             for (int k = 0; k < 3; k++)
                 r += .5f * (G.g[sidx(k, i)] * dv(D_GAM1 + 3 * k + j) + G.g[sidx(k, j)] * dv(D_GAM1 + 3 * k + i));
@@ -257,17 +256,12 @@ __device__ __forceinline__ void bssn_rhs(const float* u, const DV& dv, const Evo
         }
     // conformal connection functions (core: without advection)
     float ddivb[3];   // d_j (d_k beta^k)
-    for (int j = 0; j < 3; j++) {
-        float s = 0.f;
-        for (int k = 0; k < 3; k++) s += dv(D_BE2 + 6 * k + didx(j, k));
-        ddivb[j] = s;
-    }
+    for (int j = 0; j < 3; j++) ddivb[j] = dv(D_DDIVB + j);
     float gcore[3];
     for (int i = 0; i < 3; i++) {
         float v = (2.f / 3.f) * u[F_GAMX + i] * divb;
         for (int k = 0; k < 3; k++) v -= u[F_GAMX + k] * db[i][k];
-        for (int j = 0; j < 3; j++)
-            for (int k = 0; k < 3; k++) v += G.gi[j][k] * dv(D_BE2 + 6 * i + didx(j, k));
+        v += dv(D_BELAP + i);   // gt^jk d_j d_k beta^i
         float s1 = 0.f, s2 = 0.f, s3 = 0.f;
         for (int j = 0; j < 3; j++) {
             v += (1.f / 3.f) * G.gi[i][j] * ddivb[j] - 2.f * Auu[i][j] * dal[j];

@@ -64,7 +64,9 @@ __global__ void k_evo_init(EvoInitArgs a) {
 template <int N>
 struct DerivShape {
     static constexpr int P = 3, T = N + 2 * P;
-    static constexpr int ZS = N >= 32 ? 2 : 4;
+    // two cells per thread at 16^3 (one at 8^3, four at 32^3): a thread keeps, per cell, the shift
+    // and the inverse metric through the whole pass
+    static constexpr int ZS = N == 8 ? 4 : (N == 16 ? 2 : 1);
     static constexpr int THREADS = 256;
     static constexpr int CELLS = N * N * ZS;
     static constexpr int CPT = CELLS / THREADS;          // cells per thread
@@ -127,15 +129,22 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo
     const float ko = a.prm.ko_sigma / (64.f * h);
     const bool bssn = a.prm.physics == 0;
     const bool shift_on = bssn && a.prm.shift != 0;
-    // the shift at each of this thread's cells, for the advection terms of every field
-    float beta[CPT][3];
+    // the shift at each of this thread's cells, for the advection terms of every field, and the
+    // inverse conformal metric, for the contracted second derivatives (evolve.h)
+    float beta[CPT][3], gi[CPT][6], ddb[CPT][3];
 #pragma unroll
     for (int c = 0; c < CPT; c++) {
         const uint32_t cell = tid + (uint32_t)c * S::THREADS;
         const uint32_t x = cell % N, y = S::row(cell), z = slab * ZS + cell / (N * N);
         const size_t pi = (size_t)slot * T * T * T + ((size_t)(z + 3) * T + (y + 3)) * T + (x + 3);
 #pragma unroll
-        for (int k = 0; k < 3; k++) beta[c][k] = bssn ? a.fields[F_BETAX + k][pi] : 0.f;
+        for (int k = 0; k < 3; k++) { beta[c][k] = bssn ? a.fields[F_BETAX + k][pi] : 0.f; ddb[c][k] = 0.f; }
+        float g[6], m[3][3];
+#pragma unroll
+        for (int k = 0; k < 6; k++) g[k] = bssn ? a.fields[F_GXX + k][pi] + bssn_offset(F_GXX + k) : (k == 0 || k == 3 || k == 5 ? 1.f : 0.f);
+        inverse_sym(g, m);
+        gi[c][0] = m[0][0]; gi[c][1] = m[1][1]; gi[c][2] = m[2][2];   // xx yy zz xy xz yz
+        gi[c][3] = m[0][1]; gi[c][4] = m[0][2]; gi[c][5] = m[1][2];
     }
     float* D = a.deriv;
     const uint64_t ds = a.deriv_stride;
@@ -167,12 +176,12 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo
             int first = -1, second = -1;
             if (bssn) {
                 if (f == F_CHI) { first = D_CHI1; second = D_CHI2; }
-                else if (f >= F_GXX && f <= F_GZZ) { first = D_G1 + 3 * (f - F_GXX); second = D_G2 + 6 * (f - F_GXX); }
+                else if (f >= F_GXX && f <= F_GZZ) { first = D_G1 + 3 * (f - F_GXX); second = D_GLAP + (f - F_GXX); }
                 else if (f == F_K) first = D_K1;
                 else if (f >= F_AXX && f <= F_AZZ) { if (a.constraints) first = D_AT1 + 3 * (f - F_AXX); }
                 else if (f >= F_GAMX && f <= F_GAMZ) first = D_GAM1 + 3 * (f - F_GAMX);
                 else if (f == F_ALPHA) { first = D_AL1; second = D_AL2; }
-                else if (f >= F_BETAX && f <= F_BETAZ) { first = D_BE1 + 3 * (f - F_BETAX); second = D_BE2 + 6 * (f - F_BETAX); }
+                else if (f >= F_BETAX && f <= F_BETAZ) { first = D_BE1 + 3 * (f - F_BETAX); second = D_BELAP + (f - F_BETAX); }
             }
             if (first >= 0)
 #pragma unroll
@@ -187,11 +196,10 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo
                 if (!bssn) {
                     if (f == W_U) D[(uint64_t)WD_LAP * ds + o] = dd[0] + dd[1] + dd[2];
                 } else {
-#pragma unroll
-                    for (int ax = 0; ax < 3; ax++) D[(uint64_t)(second + ax) * ds + o] = dd[ax];
                     constexpr int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
                     constexpr float w[4] = {1.f, -8.f, 8.f, -1.f};
                     constexpr int off[4] = {-2, -1, 1, 2};
+                    float d2[6] = {dd[0], dd[1], dd[2], 0.f, 0.f, 0.f};   // xx yy zz xy xz yz
 #pragma unroll
                     for (int m = 0; m < 3; m++) {
                         const int sa = st[pa[m]], sb = st[pb[m]];
@@ -203,7 +211,26 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo
                             for (int v = 0; v < 4; v++) row = fmaf(w[v], q[off[u] * sa + off[v] * sb], row);
                             acc = fmaf(w[u], row, acc);
                         }
-                        D[(uint64_t)(second + 3 + m) * ds + o] = acc * i144h2;
+                        d2[3 + m] = acc * i144h2;
+                    }
+                    if (f == F_CHI || f == F_ALPHA) {   // all six
+#pragma unroll
+                        for (int k = 0; k < 6; k++) D[(uint64_t)(second + k) * ds + o] = d2[k];
+                    } else {
+                        // gt^lm d_l d_m of the field (the metric's and the shift's components)
+                        const float* G = gi[c];
+                        const float lap = G[0] * d2[0] + G[1] * d2[1] + G[2] * d2[2] +
+                                          2.f * (G[3] * d2[3] + G[4] * d2[4] + G[5] * d2[5]);
+                        D[(uint64_t)second * ds + o] = lap;
+                        if (f >= F_BETAX) {   // d_j d_k beta^k, k = this component
+                            const int k = f - F_BETAX;
+                            ddb[c][0] += k == 0 ? d2[0] : (k == 1 ? d2[3] : d2[4]);
+                            ddb[c][1] += k == 0 ? d2[3] : (k == 1 ? d2[1] : d2[5]);
+                            ddb[c][2] += k == 0 ? d2[4] : (k == 1 ? d2[5] : d2[2]);
+                            if (k == 2)
+#pragma unroll
+                                for (int j = 0; j < 3; j++) D[(uint64_t)(D_DDIVB + j) * ds + o] = ddb[c][j];
+                        }
                     }
                 }
             }
@@ -394,9 +421,28 @@ __global__ void __launch_bounds__(256, 4) k_evo_ghost(const __grid_constant__ Ev
     const uint32_t count = ext0 * ext1 * ext2;
     const uint64_t cells = (uint64_t)t * t * t;
     const bool exact = dd == 0u;
+    // k -> (w0, w1, w2) by multiplication: floor(k * ceil(2^21 / e) / 2^21) = floor(k / e) for
+    // k < 2^21 / 38^2 and e <= 38 (the error k * (ceil - exact) / 2^21 stays below 1 / e)
+    const uint32_t m0 = ((1u << 21) + ext0 - 1u) / ext0, m1 = ((1u << 21) + ext1 - 1u) / ext1;
+    // a same-depth source is this domain shifted by rel * n cells (rel = 0 or +-1 per axis, exact)
+    const int r0 = __float2int_rn(relp.x * (float)n), r1 = __float2int_rn(relp.y * (float)n),
+              r2 = __float2int_rn(relp.z * (float)n);
     for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) {
-        const uint32_t w0 = lo0 + k % ext0, w1 = lo1 + (k / ext0) % ext1, w2 = lo2 + k / (ext0 * ext1);
+        const uint32_t q = (uint32_t)(((uint64_t)k * m0) >> 21), q2 = (uint32_t)(((uint64_t)q * m1) >> 21);
+        const uint32_t w0 = lo0 + (k - q * ext0), w1 = lo1 + (q - q2 * ext1), w2 = lo2 + q2;
         const uint64_t dst = (uint64_t)slot * cells + ((uint64_t)w2 * t + w1) * t + w0;
+        if (exact) {   // a copy: every load of the group, then the stores
+            const int64_t si = (int64_t)src * (int64_t)cells + ((int64_t)((int)w2 + r2) * t + ((int)w1 + r1)) * t +
+                               ((int)w0 + r0);
+            float v[kGhostFields];
+#pragma unroll
+            for (int q4 = 0; q4 < kGhostFields; q4++)
+                v[q4] = mode == 0 ? A0(q4)[si] : (mode == 1 ? A1(q4)[si] : fmaf(frac, A1(q4)[si], (1.f - frac) * A0(q4)[si]));
+#pragma unroll
+            for (int q4 = 0; q4 < kGhostFields; q4++)
+                if (q4 < nfg) g.X[f0 + q4][dst] = v[q4];
+            continue;
+        }
         // source cell (same depth: the cell itself) or the base cell b of a tricubic stencil b-1 .. b+2
         // kept inside the cells that are valid: the interior along the normal axis and the later
         // axes, the whole padded range along the earlier axes (filled by earlier passes) and
@@ -791,6 +837,7 @@ cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st) {
 
 cudaError_t launch_evo_ghost(const EvoGhostArgs& g, cudaStream_t st) {
     if (g.n_items == 0) return cudaSuccess;
+    if (g.t > 38u) return cudaErrorInvalidValue;   // the kernel's index arithmetic covers padded edges up to 38
     const dim3 grid(g.n_items * 2u, (unsigned)((g.nf + kGhostFields - 1) / kGhostFields));
     k_evo_ghost<<<grid, 256, 0, st>>>(g);
     return cudaGetLastError();
