@@ -12,6 +12,7 @@
 //   k_evo_ghost     ghost fill of a stage's state, one face-normal axis per launch
 //   k_evo_constraints, k_evo_norms_*   Hamiltonian and momentum constraints, FP64 norms
 #include <cmath>
+#include <type_traits>
 
 #include "amr_device.cuh"
 #include "evolve.h"
@@ -72,7 +73,9 @@ struct DerivShape {
     static constexpr int CPT = CELLS / THREADS;          // cells per thread
     static constexpr uint32_t SLAB = (uint32_t)((ZS + 6) * T * T);   // floats
     static constexpr uint32_t SLAB_BYTES = SLAB * 4u;
-    static constexpr size_t SMEM = 2u * SLAB_BYTES + 64u;
+    // two field slabs, then per cell the inverse conformal metric (6) and the running sums of
+    // d_j d_k beta^k (3), which the BSSN pass keeps across its visits
+    static constexpr size_t SMEM = 2u * SLAB_BYTES + 9u * CELLS * 4u + 64u;
     static_assert(CELLS % THREADS == 0 && N % ZS == 0, "whole cells per thread and planes per slab");
     // The row of a cell.  At N = 16 a warp would cover rows y and y + 1 of the 22-float padded
     // rows, whose shared-memory banks overlap for 6 lanes; rows y and y + 8 (176 floats = 16 banks
@@ -92,12 +95,14 @@ __device__ __forceinline__ int deriv_field_order(int physics, int i) {
 }
 
 template <int N>
-__global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo_derivs(const __grid_constant__ EvoArgs a) {
+__global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 3) k_evo_derivs(const __grid_constant__ EvoArgs a) {
     using S = DerivShape<N>;
     constexpr int T = S::T, ZS = S::ZS, CPT = S::CPT;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* buf = reinterpret_cast<float*>(smem_raw);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + 2u * S::SLAB_BYTES);
+    float* s_gi = reinterpret_cast<float*>(smem_raw + 2u * S::SLAB_BYTES);   // [6][CELLS]
+    float* s_ddb = s_gi + 6 * S::CELLS;                                         // [3][CELLS]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(s_ddb + 3 * S::CELLS);
     __shared__ int s_abort;
 
     const uint32_t tid = threadIdx.x;
@@ -131,20 +136,21 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo
     const bool shift_on = bssn && a.prm.shift != 0;
     // the shift at each of this thread's cells, for the advection terms of every field, and the
     // inverse conformal metric, for the contracted second derivatives (evolve.h)
-    float beta[CPT][3], gi[CPT][6], ddb[CPT][3];
+    float beta[CPT][3];
 #pragma unroll
     for (int c = 0; c < CPT; c++) {
         const uint32_t cell = tid + (uint32_t)c * S::THREADS;
         const uint32_t x = cell % N, y = S::row(cell), z = slab * ZS + cell / (N * N);
         const size_t pi = (size_t)slot * T * T * T + ((size_t)(z + 3) * T + (y + 3)) * T + (x + 3);
 #pragma unroll
-        for (int k = 0; k < 3; k++) { beta[c][k] = bssn ? a.fields[F_BETAX + k][pi] : 0.f; ddb[c][k] = 0.f; }
+        for (int k = 0; k < 3; k++) { beta[c][k] = bssn ? a.fields[F_BETAX + k][pi] : 0.f; s_ddb[k * S::CELLS + cell] = 0.f; }
         float g[6], m[3][3];
 #pragma unroll
         for (int k = 0; k < 6; k++) g[k] = bssn ? a.fields[F_GXX + k][pi] + bssn_offset(F_GXX + k) : (k == 0 || k == 3 || k == 5 ? 1.f : 0.f);
         inverse_sym(g, m);
-        gi[c][0] = m[0][0]; gi[c][1] = m[1][1]; gi[c][2] = m[2][2];   // xx yy zz xy xz yz
-        gi[c][3] = m[0][1]; gi[c][4] = m[0][2]; gi[c][5] = m[1][2];
+        const float gi6[6] = {m[0][0], m[1][1], m[2][2], m[0][1], m[0][2], m[1][2]};   // xx yy zz xy xz yz
+#pragma unroll
+        for (int k = 0; k < 6; k++) s_gi[k * S::CELLS + cell] = gi6[k];
     }
     float* D = a.deriv;
     const uint64_t ds = a.deriv_stride;
@@ -157,90 +163,110 @@ __global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 4) k_evo
         __syncthreads();
         if (s_abort) { stopped = i; break; }
         const float* tile = buf + (size_t)(i & 1) * S::SLAB;
+        // what this field keeps (evolve.h), decided once per visit: 0 nothing but its extra term,
+        // 1 first derivatives, 2 first and all six second (chi, alpha), 3 first and the metric
+        // contraction of the second (gt_ij), 4 as 3 plus d_j d_k beta^k (beta^i), 5 the Laplacian (u)
+        int kind = 0, first = -1, second = -1;
+        if (bssn) {
+            if (f == F_CHI) { kind = 2; first = D_CHI1; second = D_CHI2; }
+            else if (f >= F_GXX && f <= F_GZZ) { kind = 3; first = D_G1 + 3 * (f - F_GXX); second = D_GLAP + (f - F_GXX); }
+            else if (f == F_K) { kind = 1; first = D_K1; }
+            else if (f >= F_AXX && f <= F_AZZ) { if (a.constraints) { kind = 1; first = D_AT1 + 3 * (f - F_AXX); } }
+            else if (f >= F_GAMX && f <= F_GAMZ) { kind = 1; first = D_GAM1 + 3 * (f - F_GAMX); }
+            else if (f == F_ALPHA) { kind = 2; first = D_AL1; second = D_AL2; }
+            else if (f >= F_BETAX && f <= F_BETAZ) { kind = 4; first = D_BE1 + 3 * (f - F_BETAX); second = D_BELAP + (f - F_BETAX); }
+        } else if (f == W_U) {
+            kind = 5;
+        }
+        const int bk = f - F_BETAX;   // kind 4: the shift component
+        const bool zero_extra = bssn && !shift_on && f >= F_BETAX;   // a frozen shift and its driver
+        float* const Dx = D + (uint64_t)((bssn ? D_EXTRA : WD_EXTRA) + f) * ds;
+        float* const D1 = D + (uint64_t)(first < 0 ? 0 : first) * ds;
+        float* const D2 = D + (uint64_t)(second < 0 ? 0 : second) * ds;
+        auto cells = [&](auto KIND) {
+            constexpr int K = decltype(KIND)::value;
 #pragma unroll
-        for (int c = 0; c < CPT; c++) {
-            const uint32_t cell = tid + (uint32_t)c * S::THREADS;
-            const uint32_t x = cell % N, y = S::row(cell), zl = cell / (N * N);
-            const uint32_t z = slab * ZS + zl;
-            const float* q = tile + ((zl + 3) * T + (y + 3)) * T + (x + 3);
-            const uint64_t o = ((uint64_t)slot * N + z) * N * N + (uint64_t)y * N + x;
-            constexpr int st[3] = {1, T, T * T};
-            float d1[3], ko_sum = 0.f;
-#pragma unroll
-            for (int ax = 0; ax < 3; ax++) {
-                const int s = st[ax];
-                d1[ax] = ((q[-2 * s] - q[2 * s]) + 8.f * (q[s] - q[-s])) * i12h;
-                ko_sum += (q[-3 * s] + q[3 * s]) - 6.f * (q[-2 * s] + q[2 * s]) + 15.f * (q[-s] + q[s]) - 20.f * q[0];
-            }
-            // which derivatives this field keeps (evolve.h): first, second (with mixed)
-            int first = -1, second = -1;
-            if (bssn) {
-                if (f == F_CHI) { first = D_CHI1; second = D_CHI2; }
-                else if (f >= F_GXX && f <= F_GZZ) { first = D_G1 + 3 * (f - F_GXX); second = D_GLAP + (f - F_GXX); }
-                else if (f == F_K) first = D_K1;
-                else if (f >= F_AXX && f <= F_AZZ) { if (a.constraints) first = D_AT1 + 3 * (f - F_AXX); }
-                else if (f >= F_GAMX && f <= F_GAMZ) first = D_GAM1 + 3 * (f - F_GAMX);
-                else if (f == F_ALPHA) { first = D_AL1; second = D_AL2; }
-                else if (f >= F_BETAX && f <= F_BETAZ) { first = D_BE1 + 3 * (f - F_BETAX); second = D_BELAP + (f - F_BETAX); }
-            }
-            if (first >= 0)
-#pragma unroll
-                for (int ax = 0; ax < 3; ax++) D[(uint64_t)(first + ax) * ds + o] = d1[ax];
-            if (second >= 0 || !bssn) {
-                float dd[3];
+            for (int c = 0; c < CPT; c++) {
+                const uint32_t cell = tid + (uint32_t)c * S::THREADS;
+                const uint32_t x = cell % N, y = S::row(cell), zl = cell / (N * N);
+                const uint32_t z = slab * ZS + zl;
+                const float* q = tile + ((zl + 3) * T + (y + 3)) * T + (x + 3);
+                const uint64_t o = ((uint64_t)slot * N + z) * N * N + (uint64_t)y * N + x;
+                constexpr int st[3] = {1, T, T * T};
+                float d1[3], ko_sum = 0.f;
 #pragma unroll
                 for (int ax = 0; ax < 3; ax++) {
                     const int s = st[ax];
-                    dd[ax] = (16.f * (q[-s] + q[s]) - (q[-2 * s] + q[2 * s]) - 30.f * q[0]) * i12h2;
+                    d1[ax] = ((q[-2 * s] - q[2 * s]) + 8.f * (q[s] - q[-s])) * i12h;
+                    ko_sum += (q[-3 * s] + q[3 * s]) - 6.f * (q[-2 * s] + q[2 * s]) + 15.f * (q[-s] + q[s]) - 20.f * q[0];
                 }
-                if (!bssn) {
-                    if (f == W_U) D[(uint64_t)WD_LAP * ds + o] = dd[0] + dd[1] + dd[2];
-                } else {
-                    constexpr int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
-                    constexpr float w[4] = {1.f, -8.f, 8.f, -1.f};
-                    constexpr int off[4] = {-2, -1, 1, 2};
-                    float d2[6] = {dd[0], dd[1], dd[2], 0.f, 0.f, 0.f};   // xx yy zz xy xz yz
+                if constexpr (K >= 1 && K <= 4)
 #pragma unroll
-                    for (int m = 0; m < 3; m++) {
-                        const int sa = st[pa[m]], sb = st[pb[m]];
-                        float acc = 0.f;
+                    for (int ax = 0; ax < 3; ax++) D1[(uint64_t)ax * ds + o] = d1[ax];
+                if constexpr (K >= 2) {
+                    float dd[3];
 #pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                            float row = 0.f;
-#pragma unroll
-                            for (int v = 0; v < 4; v++) row = fmaf(w[v], q[off[u] * sa + off[v] * sb], row);
-                            acc = fmaf(w[u], row, acc);
-                        }
-                        d2[3 + m] = acc * i144h2;
+                    for (int ax = 0; ax < 3; ax++) {
+                        const int s = st[ax];
+                        dd[ax] = (16.f * (q[-s] + q[s]) - (q[-2 * s] + q[2 * s]) - 30.f * q[0]) * i12h2;
                     }
-                    if (f == F_CHI || f == F_ALPHA) {   // all six
-#pragma unroll
-                        for (int k = 0; k < 6; k++) D[(uint64_t)(second + k) * ds + o] = d2[k];
+                    if constexpr (K == 5) {
+                        D[(uint64_t)WD_LAP * ds + o] = dd[0] + dd[1] + dd[2];
                     } else {
-                        // gt^lm d_l d_m of the field (the metric's and the shift's components)
-                        const float* G = gi[c];
-                        const float lap = G[0] * d2[0] + G[1] * d2[1] + G[2] * d2[2] +
-                                          2.f * (G[3] * d2[3] + G[4] * d2[4] + G[5] * d2[5]);
-                        D[(uint64_t)second * ds + o] = lap;
-                        if (f >= F_BETAX) {   // d_j d_k beta^k, k = this component
-                            const int k = f - F_BETAX;
-                            ddb[c][0] += k == 0 ? d2[0] : (k == 1 ? d2[3] : d2[4]);
-                            ddb[c][1] += k == 0 ? d2[3] : (k == 1 ? d2[1] : d2[5]);
-                            ddb[c][2] += k == 0 ? d2[4] : (k == 1 ? d2[5] : d2[2]);
-                            if (k == 2)
+                        constexpr int pa[3] = {0, 0, 1}, pb[3] = {1, 2, 2};
+                        constexpr float w[4] = {1.f, -8.f, 8.f, -1.f};
+                        constexpr int off[4] = {-2, -1, 1, 2};
+                        float d2[6] = {dd[0], dd[1], dd[2], 0.f, 0.f, 0.f};   // xx yy zz xy xz yz
 #pragma unroll
-                                for (int j = 0; j < 3; j++) D[(uint64_t)(D_DDIVB + j) * ds + o] = ddb[c][j];
+                        for (int m = 0; m < 3; m++) {
+                            const int sa = st[pa[m]], sb = st[pb[m]];
+                            float acc = 0.f;
+#pragma unroll
+                            for (int u = 0; u < 4; u++) {
+                                float row = 0.f;
+#pragma unroll
+                                for (int v = 0; v < 4; v++) row = fmaf(w[v], q[off[u] * sa + off[v] * sb], row);
+                                acc = fmaf(w[u], row, acc);
+                            }
+                            d2[3 + m] = acc * i144h2;
+                        }
+                        if constexpr (K == 2) {   // all six
+#pragma unroll
+                            for (int k = 0; k < 6; k++) D2[(uint64_t)k * ds + o] = d2[k];
+                        } else {
+                            // gt^lm d_l d_m of the field (the metric's and the shift's components)
+                            const float* G = s_gi + cell;   // G[k * CELLS]: this cell's inverse metric
+                            constexpr int C = S::CELLS;
+                            D2[o] = G[0] * d2[0] + G[C] * d2[1] + G[2 * C] * d2[2] +
+                                    2.f * (G[3 * C] * d2[3] + G[4 * C] * d2[4] + G[5 * C] * d2[5]);
+                            if constexpr (K == 4) {   // d_j d_k beta^k, k = this component
+                                float* B = s_ddb + cell;
+                                B[0] += bk == 0 ? d2[0] : (bk == 1 ? d2[3] : d2[4]);
+                                B[C] += bk == 0 ? d2[3] : (bk == 1 ? d2[1] : d2[5]);
+                                B[2 * C] += bk == 0 ? d2[4] : (bk == 1 ? d2[5] : d2[2]);
+                                if (bk == 2)
+#pragma unroll
+                                    for (int j = 0; j < 3; j++) D[(uint64_t)(D_DDIVB + j) * ds + o] = B[j * C];
+                            }
                         }
                     }
                 }
+                // advection along the shift and dissipation
+                float extra = ko * ko_sum;
+                if (bssn) {
+                    extra = fmaf(beta[c][0], d1[0], fmaf(beta[c][1], d1[1], fmaf(beta[c][2], d1[2], extra)));
+                    if (zero_extra) extra = 0.f;
+                }
+                Dx[o] = extra;
             }
-            // advection along the shift and dissipation (a frozen shift and its driver have neither)
-            float extra = ko * ko_sum;
-            if (bssn) {
-                extra = fmaf(beta[c][0], d1[0], fmaf(beta[c][1], d1[1], fmaf(beta[c][2], d1[2], extra)));
-                if (!shift_on && f >= F_BETAX) extra = 0.f;
-            }
-            D[(uint64_t)((bssn ? D_EXTRA : WD_EXTRA) + f) * ds + o] = extra;
+        };
+        switch (kind) {
+            case 1: cells(std::integral_constant<int, 1>{}); break;
+            case 2: cells(std::integral_constant<int, 2>{}); break;
+            case 3: cells(std::integral_constant<int, 3>{}); break;
+            case 4: cells(std::integral_constant<int, 4>{}); break;
+            case 5: cells(std::integral_constant<int, 5>{}); break;
+            default: cells(std::integral_constant<int, 0>{}); break;
         }
         __syncthreads();   // every thread is done with buffer i % 2
         if (tid == 0 && i + 2 < nf) issue(i + 2);
@@ -579,9 +605,13 @@ __global__ void __launch_bounds__(128) k_evo_constraints(const __grid_constant__
     const uint32_t x = cell % N, y = (cell / N) % N, z = cell / (N * N);
     const uint64_t pi = (uint64_t)slot * T * T * T + ((uint64_t)(z + P) * T + (y + P)) * T + (x + P);
     const uint64_t ii = (uint64_t)slot * N * N * N + cell;
-    float u[BSSN_NF];
+    float u[BSSN_NF], uo[BSSN_NF];
 #pragma unroll
-    for (int f = 0; f < BSSN_NF; f++) u[f] = a.fields[f][pi] + bssn_offset(f);
+    for (int f = 0; f < BSSN_NF; f++) {
+        const float s = a.fields[f][pi];   // the stored form
+        u[f] = s + bssn_offset(f);
+        uo[f] = a.stage == 1 ? s : a.old_f[f][pi];
+    }
     const float* D = a.deriv;
     const uint64_t ds = a.deriv_stride;
     auto dv = [&](int k) { return D[(uint64_t)k * ds + ii]; };
