@@ -9,9 +9,9 @@
 //   conv2  16 -> 16 channels, 3x3x3, padding 1, stride 2, ReLU     -> 16 x 4^3 = 1024
 //   fc1    1024 -> 32, ReLU
 //   fc2    32 -> 1 (the predicted log10 truncation error of the tile)
-// The convolutions and fc1 run as GEMMs on the tensor cores (mma.sync m16n8k16, BF16 operands,
-// FP32 accumulation) over im2col matrices; the backward pass uses the same GEMM for the weight and
-// input gradients.  Master weights, gradients and the Adam moments are FP32; the GEMM operands
+// The convolutions and fc1 run as GEMMs on the fifth-generation tensor cores (tcgen05.mma kind::f16,
+// BF16 operands in shared memory, FP32 accumulation in Tensor Memory) over im2col matrices; the
+// backward pass uses the same GEMM for the weight and input gradients.  Master weights, gradients and the Adam moments are FP32; the GEMM operands
 // (weights, activations, back-propagated gradients) are rounded to BF16.
 //
 // Layouts: activations are position-major, channel-last ([tile][position][channel]); im2col column
@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "capi_internal.h"
+#include "tcgen05.cuh"
 
 namespace amr {
 
@@ -42,8 +43,12 @@ constexpr size_t kOffW1 = 0, kOffB1 = kOffW1 + kK1 * kC1, kOffW2 = kOffB1 + kC1,
 
 // ------------------------------------------------------------------ BF16 GEMM on the tensor cores
 // C[m][n] (+)= sum_k A(m, k) B(k, n); A(m, k) = A[m * sam + k * sak], B(k, n) = B[k * sbk + n * sbn],
-// C[m * scm + n * scn] (FP32).  A block of 4 warps computes a 64 x 32 tile, each warp 16 rows by four
-// 8-column mma tiles; K advances 16 at a time through shared memory (zero-filled past the edges).
+// C[m * scm + n * scn] (FP32).  A CTA of 4 warps computes a 128 x NT tile (NT = 16 or 32) with the
+// fifth-generation tensor cores: per K block of 64 the threads stage A (128 x 64) and B (NT x 64)
+// into shared memory as K-major core matrices (zero past the edges), one thread issues four
+// tcgen05.mma of K = 16 into a TMEM accumulator and commits them to an mbarrier, and after the last
+// block each warp reads its 32 rows of the accumulator back with tcgen05.ld.  Every wait is bounded;
+// a wait that runs out raises *err, waits once more for the MMAs in flight and frees the TMEM.
 struct GemmArgs {
     const bf16* A;
     int64_t sam, sak;
@@ -53,67 +58,103 @@ struct GemmArgs {
     int64_t scm, scn;
     int M, N, K;
     int accumulate;   // 1: C += A B, 0: C = A B
+    int* err;         // device flag raised when a wait gives up
 };
 
-__device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
-    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
+constexpr int kGemmM = 128, kGemmK = 64;
 
+template <int NT>
 __global__ void __launch_bounds__(128) k_gemm_bf16(const GemmArgs g) {
-    __shared__ bf16 As[64][16 + 8];
-    __shared__ bf16 Bs[16][32 + 8];
-    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    const int gid = lane >> 2, tig = lane & 3;
-    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 32;
-    float acc[4][4];
-    for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
-    const bf16 zero = __float2bfloat16_rn(0.f);
-    for (int k0 = 0; k0 < g.K; k0 += 16) {
-        for (int e = tid; e < 64 * 16; e += 128) {
-            const int r = e / 16, c = e % 16, m = m0 + r, k = k0 + c;
-            As[r][c] = (m < g.M && k < g.K) ? g.A[(int64_t)m * g.sam + (int64_t)k * g.sak] : zero;
-        }
-        for (int e = tid; e < 16 * 32; e += 128) {
-            const int r = e / 32, c = e % 32, k = k0 + r, n = n0 + c;
-            Bs[r][c] = (k < g.K && n < g.N) ? g.B[(int64_t)k * g.sbk + (int64_t)n * g.sbn] : zero;
-        }
-        __syncthreads();
-        const int r = warp * 16 + gid;
-        const uint32_t a0 = pack2(As[r][2 * tig], As[r][2 * tig + 1]);
-        const uint32_t a1 = pack2(As[r + 8][2 * tig], As[r + 8][2 * tig + 1]);
-        const uint32_t a2 = pack2(As[r][2 * tig + 8], As[r][2 * tig + 9]);
-        const uint32_t a3 = pack2(As[r + 8][2 * tig + 8], As[r + 8][2 * tig + 9]);
-#pragma unroll
-        for (int nt = 0; nt < 4; nt++) {
-            const int n = nt * 8 + gid;
-            const uint32_t b0 = pack2(Bs[2 * tig][n], Bs[2 * tig + 1][n]);
-            const uint32_t b1 = pack2(Bs[2 * tig + 8][n], Bs[2 * tig + 9][n]);
-            asm volatile(
-                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                "{%0,%1,%2,%3};"
-                : "+f"(acc[nt][0]), "+f"(acc[nt][1]), "+f"(acc[nt][2]), "+f"(acc[nt][3])
-                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-        }
-        __syncthreads();
+    static_assert(NT == 16 || NT == 32, "M = 128 tiles take N in multiples of 16; 32 TMEM columns");
+    constexpr int MT = kGemmM, KT = kGemmK;
+    constexpr uint32_t LBO = 128u, SBO = (KT / 8) * 128u;   // bytes between core matrices along K / M
+    __shared__ __align__(1024) bf16 As[MT * KT];
+    __shared__ __align__(1024) bf16 Bs[NT * KT];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, warp = tid / 32;
+    const int m0 = blockIdx.y * MT, n0 = blockIdx.x * NT;
+    if (warp == 0) tmem_alloc(&s_tmem, 32u);   // the 128 x NT FP32 accumulator
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+        s_fail = 0;
     }
-#pragma unroll
-    for (int nt = 0; nt < 4; nt++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int m = m0 + warp * 16 + gid + (q >= 2 ? 8 : 0);
-            const int n = n0 + nt * 8 + 2 * tig + (q & 1);
-            if (m < g.M && n < g.N) {
-                float* c = g.C + (int64_t)m * g.scm + (int64_t)n * g.scn;
-                *c = g.accumulate ? *c + acc[nt][q] : acc[nt][q];
-            }
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    if (warp == 0) tmem_relinquish();
+    const uint32_t tmem = s_tmem;
+    constexpr uint32_t idesc = umma_idesc_bf16_f32(MT, NT);
+    const bf16 zero = __float2bfloat16_rn(0.f);
+    // element (row r, k) of a K-major operand: core matrix (r / 8, k / 8) of 64 elements, row r % 8
+    auto at = [](int r, int k) { return ((r >> 3) * (KT / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7); };
+    uint32_t phase = 0;
+    const int nkb = (g.K + KT - 1) / KT;
+    for (int kb = 0; kb < nkb; kb++) {
+        const int k0 = kb * KT;
+        for (int e = tid; e < MT * KT; e += 128) {
+            const int r = e / KT, c = e % KT, m = m0 + r, k = k0 + c;
+            As[at(r, c)] = (m < g.M && k < g.K) ? g.A[(int64_t)m * g.sam + (int64_t)k * g.sak] : zero;
         }
+        for (int e = tid; e < NT * KT; e += 128) {
+            const int r = e / KT, c = e % KT, n = n0 + r, k = k0 + c;
+            Bs[at(r, c)] = (n < g.N && k < g.K) ? g.B[(int64_t)k * g.sbk + (int64_t)n * g.sbn] : zero;
+        }
+        fence_proxy_async_smem();   // these writes, visible to the tensor core
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after_sync();
+            const uint32_t a0 = smem_addr(As), b0 = smem_addr(Bs);
+#pragma unroll
+            for (int kk = 0; kk < KT / 16; kk++)   // K = 16 per MMA: two core matrices along K
+                umma_bf16(tmem, umma_desc_kmajor(a0 + kk * 2 * LBO, LBO, SBO), umma_desc_kmajor(b0 + kk * 2 * LBO, LBO, SBO),
+                          idesc, kb > 0 || kk > 0);
+            umma_commit(&bar);
+        }
+        // the block's MMAs have read As and Bs once the barrier's phase completes
+        const bool ok = mbar_wait(&bar, phase);
+        phase ^= 1u;
+        if (!ok) s_fail = 1;
+        __syncthreads();
+        if (s_fail) break;
+    }
+    if (!s_fail) {
+        tc_fence_after_sync();
+        float v[NT];
+        const uint32_t row_addr = tmem + ((uint32_t)(warp * 32) << 16);   // lanes 32 w .. 32 w + 31
+        tmem_ld16(row_addr, v);
+        if constexpr (NT == 32) tmem_ld16(row_addr + 16u, v + 16);
+        const int m = m0 + warp * 32 + (tid & 31);
+        if (m < g.M) {
+#pragma unroll
+            for (int n = 0; n < NT; n++)
+                if (n0 + n < g.N) {
+                    float* c = g.C + (int64_t)m * g.scm + (int64_t)(n0 + n) * g.scn;
+                    *c = g.accumulate ? *c + v[n] : v[n];
+                }
+        }
+    } else if (tid == 0) {
+        atomicExch(g.err, 1);
+        mbar_wait(&bar, phase ^ 1u);   // the MMAs of the block whose wait gave up
+    }
+    tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after_sync();
+        tmem_dealloc(tmem, 32u);
+    }
 }
 
-cudaError_t gemm(const GemmArgs& g, cudaStream_t st) {
+cudaError_t gemm(GemmArgs g, cudaStream_t st) {
     if (g.M <= 0 || g.N <= 0) return cudaSuccess;
-    const dim3 grid((unsigned)((g.N + 31) / 32), (unsigned)((g.M + 63) / 64));
-    k_gemm_bf16<<<grid, 128, 0, st>>>(g);
+    if (!g.err) g.err = device_error_flag();
+    if (!g.err) return cudaErrorMemoryAllocation;
+    const int nt = g.N <= 16 ? 16 : 32;
+    const dim3 grid((unsigned)((g.N + nt - 1) / nt), (unsigned)((g.M + kGemmM - 1) / kGemmM));
+    if (nt == 16) k_gemm_bf16<16><<<grid, 128, 0, st>>>(g);
+    else k_gemm_bf16<32><<<grid, 128, 0, st>>>(g);
     return cudaGetLastError();
 }
 
@@ -471,7 +512,8 @@ AMR_API int amr_estimator_forward(amr_estimator* e, const float* features, uint3
         if (st == cudaSuccess) st = cudaMemcpyAsync(out + b0, e->net.out, (size_t)B * 4, cudaMemcpyDeviceToDevice, e->net.stream);
         if (st != cudaSuccess) return cuda_status(st);
     }
-    return cuda_status(cudaStreamSynchronize(e->net.stream));
+    const int st = cuda_status(cudaStreamSynchronize(e->net.stream));
+    return st ? st : take_device_error(device_error_flag());
 }
 AMR_API int amr_estimator_gradients(amr_estimator* e, const float* features, const float* targets, uint32_t n,
                                     float* grads_host, float* loss) {
@@ -484,7 +526,8 @@ AMR_API int amr_estimator_gradients(amr_estimator* e, const float* features, con
     if (st == cudaSuccess) st = cudaMemcpyAsync(&l, e->net.loss, 4, cudaMemcpyDeviceToHost, e->net.stream);
     if (st == cudaSuccess) st = cudaStreamSynchronize(e->net.stream);
     if (loss) *loss = l / (float)n;
-    return cuda_status(st);
+    const int status = cuda_status(st);
+    return status ? status : take_device_error(device_error_flag());
 }
 AMR_API int amr_estimator_train_step(amr_estimator* e, const float* features, const float* targets, uint32_t n,
                                      float lr, float* loss) {
@@ -496,5 +539,6 @@ AMR_API int amr_estimator_train_step(amr_estimator* e, const float* features, co
     if (st == cudaSuccess && loss) st = cudaMemcpyAsync(&l, e->net.loss, 4, cudaMemcpyDeviceToHost, e->net.stream);
     if (st == cudaSuccess) st = cudaStreamSynchronize(e->net.stream);
     if (loss) *loss = l / (float)n;
-    return cuda_status(st);
+    const int status = cuda_status(st);
+    return status ? status : take_device_error(device_error_flag());
 }

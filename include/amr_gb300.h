@@ -399,7 +399,7 @@ int amr_sim_constraint_norms(amr_sim* s, float excision_radius, double* out5);
  * (SimpleWave.h:91-187, 228-248).  A small network predicts each tile's (domain's) log10 truncation
  * error from 3 x 8^3 features (conformal factor, lapse, |d gt| dx, averaged onto 8^3): conv 3->16
  * (3^3, ReLU), conv 16->16 (3^3, stride 2, ReLU), dense 1024->32 (ReLU), dense 32->1.  Forward and
- * backward run on the tensor cores (BF16 operands, FP32 accumulation); FP32 master weights and
+ * backward run on the tcgen05 tensor cores (BF16 operands, FP32 accumulation in Tensor Memory); FP32 master weights and
  * Adam.  Buffers are device pointers; features are [tile][3][512] floats. */
 typedef struct amr_estimator amr_estimator;
 int amr_estimator_create(uint32_t max_batch, uint64_t seed, amr_estimator** out);
