@@ -124,6 +124,7 @@ struct EvoArgs {
     float dt0;                    // dt at depth 0
     int stage;                    // 1..4
     int constraints;              // derivative pass: also store d_k A_ij
+    uint32_t deriv_zs;            // derivative pass: interior z-planes per slab (0: the default)
     EvoParams prm;
     int* err;
 };

@@ -87,6 +87,8 @@ bool evo_config_supported(uint32_t n, uint32_t p);
 cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st);
 cudaError_t launch_evo_init(const EvoInitArgs& a, cudaStream_t st);
 cudaError_t launch_evo_derivs(const EvoArgs& a, cudaStream_t st);
+// The derivative pass's compiled slab depths for size_domain n (written to out, at most 4); their count.
+uint32_t evo_deriv_zs_candidates(uint32_t n, uint32_t* out);
 cudaError_t launch_evo_rhs(const EvoArgs& a, cudaStream_t st);
 cudaError_t launch_evo_ghost(const EvoGhostArgs& g, cudaStream_t st);
 cudaError_t launch_evo_constraints(const EvoArgs& a, const ConsPtrs& cons, cudaStream_t st);

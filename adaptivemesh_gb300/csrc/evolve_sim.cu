@@ -314,6 +314,48 @@ public:
         tree.set_timer(0u);
         return check(launch_evo_init(a, stream));
     }
+    // Launch-shape tuning of the derivative pass (amr_sim_autotune): its slab depth (interior
+    // z-planes per CTA) timed at every compiled depth over all evolved domains, reps launches each
+    // with CUDA events; the fastest is kept.  The pass writes only its derivative scratch, which
+    // every RK stage rewrites, so the state is unchanged.
+    int autotune(uint32_t reps, uint32_t* n_tuned) override {
+        if (n_tuned) *n_tuned = 0;
+        if (capturing || reps == 0u || reps > 100u) return AMR_ERR_INVALID;
+        int st = wait_side(-1, 0);
+        if (!st) st = prepare();
+        if (st) return st;
+        if (all_evolved_cnt == 0u) return AMR_OK;
+        uint32_t cand[4];
+        const uint32_t nc = evo_deriv_zs_candidates(dims.n, cand);
+        EvoArgs a = args(0, new_f, new_f, 1, 0);
+        a.items = d_lists + all_evolved_off;
+        a.n_items = all_evolved_cnt;
+        cudaEvent_t ev[2] = {nullptr, nullptr};
+        cudaError_t e = cudaEventCreate(&ev[0]);
+        if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+        uint32_t best = 0;
+        float best_ms = 0.f;
+        for (uint32_t i = 0; i < nc && e == cudaSuccess; i++) {
+            a.deriv_zs = cand[i];
+            e = launch_evo_derivs(a, stream);   // warm-up
+            if (e == cudaSuccess) e = cudaEventRecord(ev[0], stream);
+            for (uint32_t r = 0; r < reps && e == cudaSuccess; r++) e = launch_evo_derivs(a, stream);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            if (e == cudaSuccess && (best == 0u || ms < best_ms)) { best = cand[i]; best_ms = ms; }
+        }
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        if (e != cudaSuccess) return cuda_status(e);
+        if ((st = take_device_error(err_flag))) return st;
+        deriv_zs = best;
+        tuned_ctas.assign(1, {all_evolved_cnt, best});
+        graph_valid = false;
+        if (n_tuned) *n_tuned = 1;
+        return AMR_OK;
+    }
     int constraint_norms(float excision, double* out) {
         if (kind != AMR_SIM_BSSN_EVOLVE) return AMR_ERR_INVALID;
         int st = prepare();
@@ -496,6 +538,7 @@ private:
         a.dt0 = prm.cfl * cfg.outer_size / (float)dims.n;
         a.stage = stage;
         a.constraints = constraints;
+        a.deriv_zs = deriv_zs;
         a.prm = prm;
         a.err = err_flag;
         return a;
@@ -549,6 +592,7 @@ private:
     bool lists_valid = false;
     std::vector<uint32_t> act_off, act_cnt, evo_off, evo_cnt, leaves;
     uint32_t all_evolved_off = 0, all_evolved_cnt = 0, leaves_off = 0;
+    uint32_t deriv_zs = 0;   // the derivative pass's slab depth (0: the default; amr_sim_autotune)
     cudaGraphExec_t graph_exec = nullptr;
     uint64_t graph_launches = 0;
 };

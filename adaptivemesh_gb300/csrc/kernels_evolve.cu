@@ -61,13 +61,15 @@ __global__ void k_evo_init(EvoInitArgs a) {
 }
 
 // ------------------------------------------------------------------ derivative pass
-// z-slab planes per unit: the slab's padded planes (ZS + 6) of one field fit twice in shared memory
-template <int N>
+// A CTA per (domain, slab of ZS interior z-planes): the slab's padded planes (ZS + 6) of one field
+// fit twice in shared memory.  ZS is a launch-shape choice (amr_sim_autotune times the compiled
+// ones, DerivZs below); the default takes two cells per thread at 16^3 (one at 8^3 and 32^3): a
+// thread keeps, per cell, the shift through the whole pass.
+constexpr int deriv_default_zs(int n) { return n == 8 ? 4 : (n == 16 ? 2 : 1); }
+template <int N, int ZS_ = deriv_default_zs(N)>
 struct DerivShape {
     static constexpr int P = 3, T = N + 2 * P;
-    // two cells per thread at 16^3 (one at 8^3, four at 32^3): a thread keeps, per cell, the shift
-    // and the inverse metric through the whole pass
-    static constexpr int ZS = N == 8 ? 4 : (N == 16 ? 2 : 1);
+    static constexpr int ZS = ZS_;
     static constexpr int THREADS = 256;
     static constexpr int CELLS = N * N * ZS;
     static constexpr int CPT = CELLS / THREADS;          // cells per thread
@@ -94,9 +96,10 @@ __device__ __forceinline__ int deriv_field_order(int physics, int i) {
     return i < 3 ? F_BETAX + i : (i < 21 ? i - 3 : i);
 }
 
-template <int N>
-__global__ void __launch_bounds__(DerivShape<N>::THREADS, N >= 32 ? 2 : 3) k_evo_derivs(const __grid_constant__ EvoArgs a) {
-    using S = DerivShape<N>;
+template <int N, int ZS_>
+__global__ void __launch_bounds__(DerivShape<N, ZS_>::THREADS, DerivShape<N, ZS_>::CPT <= 2 ? 3 : 2)
+    k_evo_derivs(const __grid_constant__ EvoArgs a) {
+    using S = DerivShape<N, ZS_>;
     constexpr int T = S::T, ZS = S::ZS, CPT = S::CPT;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* buf = reinterpret_cast<float*>(smem_raw);
@@ -547,6 +550,31 @@ __global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ Ev
     if (item >= g.n_items) return;
     const uint32_t slot = g.items[item];
     const uint64_t cells = (uint64_t)t * t * t;
+    bool leaf = true;
+#pragma unroll
+    for (int c = 0; c < 8; c++) leaf &= g.children[slot * 8u + c] == -1;
+    if (leaf) {
+        // a domain without children: plane z of every field is a straight copy, 16 bytes at a time
+        // (planes are t^2 floats, t^2 * 4 a multiple of 16, every plane 16-byte aligned)
+        const uint32_t q4 = t * t / 4u;
+        const uint64_t base4 = (slot * cells + (uint64_t)z * t * t) / 4u;
+        const uint32_t total = (uint32_t)g.nf * q4;
+        constexpr uint32_t U = 4;   // loads in flight per thread before their stores
+        for (uint32_t e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
+            float4 v[U];
+#pragma unroll
+            for (uint32_t u = 0; u < U; u++) {
+                const uint32_t e = e0 + u * blockDim.x;
+                if (e < total) v[u] = reinterpret_cast<const float4*>(g.new_f[e / q4])[base4 + e % q4];
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < U; u++) {
+                const uint32_t e = e0 + u * blockDim.x;
+                if (e < total) reinterpret_cast<float4*>(g.old_f[e / q4])[base4 + e % q4] = v[u];
+            }
+        }
+        return;
+    }
     constexpr float w4[4] = {-1.f / 16.f, 9.f / 16.f, 9.f / 16.f, -1.f / 16.f};
     for (uint32_t k = threadIdx.x; k < t * t; k += blockDim.x) {
         const uint32_t x = k % t, y = k / t;
@@ -818,14 +846,30 @@ cudaError_t launch_evo_init(const EvoInitArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+template <int N, int ZS>
+static cudaError_t derivs_zs(const EvoArgs& a, cudaStream_t st) {
+    using S = DerivShape<N, ZS>;
+    static std::atomic<uint64_t> configured{0};
+    cudaError_t e = ensure_smem_limit(k_evo_derivs<N, ZS>, S::SMEM, configured);
+    if (e != cudaSuccess || a.n_items == 0) return e;
+    k_evo_derivs<N, ZS><<<a.n_items * (N / ZS), S::THREADS, S::SMEM, st>>>(a);
+    return cudaGetLastError();
+}
+// The compiled slab depths (a.deriv_zs; 0 = the default): whole cells per thread of 256.
 template <int N>
 static cudaError_t derivs_t(const EvoArgs& a, cudaStream_t st) {
-    using S = DerivShape<N>;
-    static std::atomic<uint64_t> configured{0};
-    cudaError_t e = ensure_smem_limit(k_evo_derivs<N>, S::SMEM, configured);
-    if (e != cudaSuccess || a.n_items == 0) return e;
-    k_evo_derivs<N><<<a.n_items * (N / S::ZS), S::THREADS, S::SMEM, st>>>(a);
-    return cudaGetLastError();
+    const uint32_t zs = a.deriv_zs ? a.deriv_zs : (uint32_t)deriv_default_zs(N);
+    if constexpr (N == 8) {
+        if (zs == 4) return derivs_zs<8, 4>(a, st);
+        if (zs == 8) return derivs_zs<8, 8>(a, st);
+    } else if constexpr (N == 16) {
+        if (zs == 1) return derivs_zs<16, 1>(a, st);
+        if (zs == 2) return derivs_zs<16, 2>(a, st);
+        if (zs == 4) return derivs_zs<16, 4>(a, st);
+    } else {
+        if (zs == 1) return derivs_zs<32, 1>(a, st);   // deeper slabs would spill registers
+    }
+    return cudaErrorInvalidValue;
 }
 cudaError_t launch_evo_derivs(const EvoArgs& a, cudaStream_t st) {
     switch (a.n) {
@@ -834,6 +878,13 @@ cudaError_t launch_evo_derivs(const EvoArgs& a, cudaStream_t st) {
         case 32: return derivs_t<32>(a, st);
         default: return cudaErrorInvalidValue;
     }
+}
+uint32_t evo_deriv_zs_candidates(uint32_t n, uint32_t* out) {
+    const uint32_t c8[] = {4, 8}, c16[] = {1, 2, 4}, c32[] = {1};
+    const uint32_t* c = n == 8 ? c8 : (n == 16 ? c16 : c32);
+    const uint32_t k = n == 16 ? 3u : (n == 8 ? 2u : 1u);
+    for (uint32_t i = 0; i < k; i++) out[i] = c[i];
+    return n == 8 || n == 16 || n == 32 ? k : 0u;
 }
 
 template <int N>

@@ -381,6 +381,7 @@ def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool, depth: int 
         cases.tree_uniform(sim, depth)
         sim.set_evolution(am.Evolution(slicing=am.SLICING_1PLUSLOG, shift=0, ko_sigma=0.1, cfl=0.25, periodic=1))
         sim.initial_data(am.InitialData(kind=am.ID_GAUGE_WAVE, amplitude=1e-2, wavelength=1.0))
+        tuned = sim.autotune(3) if mode != am.MODE_PLAIN else None   # the derivative pass's slab depth
         sim.timestep()                       # warm-up (graph capture)
         sim.synchronize()
         l0 = sim.kernel_launches
@@ -393,6 +394,8 @@ def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool, depth: int 
         zc = zone_cycles_per_root_step(sim.state(), 16) * steps
         gw[name] = {"value": zc / (ms / 1e3), "ms_per_root_step": ms / steps, "root_steps": steps,
                     "gpu_launches_per_root_step": (sim.kernel_launches - l0) / steps}
+        if tuned:
+            gw[name]["derivative_slab_planes"] = next(iter(tuned.values()))
         if name == "batched":
             gw[name].update({k: v for k, v in sim.constraint_norms().items() if k != "cells"})
             gw[name]["finest_steps"] = (1 << depth) * (steps + 1)
@@ -423,6 +426,8 @@ def binary_run(am, E, punct, params, net, bmode: int, steps: int = 16) -> tuple[
     for step in range(steps):
         if step % 8 == 0:
             regrids.append(sim.regrid(params, net))
+            if bmode != am.MODE_PLAIN:
+                sim.autotune(2)   # the derivative pass's slab depth for the new tree
         zc += zone_cycles_per_root_step(sim.state(), 16)
         sim.timestep()
     sim.synchronize()

@@ -322,18 +322,23 @@ int amr_sim_set_fault_injection(amr_sim* s, uint32_t spin_limit, uint32_t withho
  * contiguous range of the active domains' planes).  The reference sizes its launches from the
  * domain constants instead (AMR.h:1119-1142). */
 int amr_sim_set_stencil_ctas(amr_sim* s, uint32_t ctas);
-/* Autotuner of the fused BSSN derivative pass's grid (no counterpart in the reference, whose
- * launch shapes are fixed by the domain constants, AMR.h:647-668, 1119-1142): for every distinct
- * number of active domains among the current octree's substeps, times candidate grids (the
- * library's rule, 1-4 CTAs per SM, ranges of 2-64 planes per CTA) reps times each with CUDA events
- * and keeps the fastest, which AMR_MODE_BATCHED / AMR_MODE_GRAPH then use for that count (a fixed
- * amr_sim_set_stencil_ctas still wins).  The candidate launches write only scratch memory
- * allocated for the call; the simulation's buffers are unchanged.  Synchronises the simulation's
- * stream; call it between timesteps, after the octree changes.  *n_tuned = domain counts tuned.
- * BSSN plugin only (AMR_ERR_INVALID otherwise). */
+/* Launch-shape autotuner (no counterpart in the reference, whose launch shapes are fixed by the
+ * domain constants, AMR.h:647-668, 1119-1142).  Times candidate shapes reps times each with CUDA
+ * events on the simulation's stream and keeps the fastest; synchronises the stream; call it
+ * between timesteps, after the octree changes.
+ *   AMR_SIM_BSSN: the fused derivative pass's grid, for every distinct number of active domains
+ *   among the octree's substeps (candidates: the library's rule, 1-4 CTAs per SM, ranges of 2-64
+ *   planes per CTA), used by AMR_MODE_BATCHED / AMR_MODE_GRAPH for that count (a fixed
+ *   amr_sim_set_stencil_ctas still wins).  The candidate launches write only scratch memory
+ *   allocated for the call.
+ *   AMR_SIM_BSSN_EVOLVE / AMR_SIM_WAVE_RK4: the derivative pass's slab depth (interior z-planes
+ *   per CTA: 1, 2 or 4 at 16^3; 4 or 8 at 8^3; 1 at 32^3), timed over every evolved domain; the
+ *   pass writes only its derivative scratch, which every RK stage rewrites.
+ * The simulation's state is unchanged.  *n_tuned = shapes tuned.  AMR_SIM_WAVE: AMR_ERR_INVALID. */
 int amr_sim_autotune(amr_sim* s, uint32_t reps, uint32_t* n_tuned);
-/* The tuned (active domains, CTAs) pairs, up to capacity; *count = how many there are
- * (AMR_ERR_CAPACITY if more than capacity). */
+/* The tuned pairs, up to capacity: (active domains, CTAs of the fused pass) for AMR_SIM_BSSN,
+ * (evolved domains, z-planes per derivative slab) for the evolution kinds; *count = how many
+ * there are (AMR_ERR_CAPACITY if more than capacity). */
 int amr_sim_tuned_shapes(const amr_sim* s, uint32_t capacity, uint32_t* domains, uint32_t* ctas, uint32_t* count);
 /* Optional timing of the dominant kernel (the derivative stencil) with CUDA events on the
  * simulation's stream.  amr_sim_kernel_timing returns the summed milliseconds and launch count

@@ -228,8 +228,37 @@ def test_autotune_leaves_state_and_results_unchanged(am, cuda, mode):
     assert results[1]["rng"] == results[0]["rng"]
 
 
-def test_autotune_rejects_other_kinds(am, cuda):
-    sim = am.Sim(am.Config(16, 3, 1.0), am.SIM_BSSN_EVOLVE, slots=9, mode=am.MODE_BATCHED)
+def test_autotune_evolution_slab_depth(am, cuda):
+    """amr_sim_autotune on the BSSN evolution (the gauge wave on uniform depth 2, 73 evolved
+    domains of 16^3): it picks one of the derivative pass's compiled slab depths, leaves every
+    state buffer bit-identical, and the next timestep on the tuned depth equals an untuned
+    simulation's bit for bit (every cell's derivatives are the same arithmetic whatever the slab)."""
+    import torch
+    states = []
+    for tune in (False, True):
+        sim = am.Sim(am.Config(16, 3, 1.0), am.SIM_BSSN_EVOLVE, slots=73, mode=am.MODE_GRAPH)
+        cases.tree_uniform(sim, 2)
+        sim.set_evolution(am.Evolution(slicing=am.SLICING_1PLUSLOG, shift=0, ko_sigma=0.1, cfl=0.25, periodic=1))
+        sim.initial_data(am.InitialData(kind=am.ID_GAUGE_WAVE, amplitude=1e-2, wavelength=1.0))
+        sim.timestep()
+        sim.synchronize()
+        used, t = sim.state()["used_slots"], sim.cfg.total
+        if tune:
+            before = [sim.tensor(w, f)[: used * t ** 3].clone() for w in (sim.OLD_STATE, sim.NEW_STATE) for f in range(24)]
+            shapes = sim.autotune(2)
+            after = [sim.tensor(w, f)[: used * t ** 3].clone() for w in (sim.OLD_STATE, sim.NEW_STATE) for f in range(24)]
+            assert all(torch.equal(x, y) for x, y in zip(before, after)), "autotune changed the state"
+            assert list(shapes) == [73] and shapes[73] in (1, 2, 4), shapes
+        sim.timestep()
+        sim.synchronize()
+        states.append([sim.tensor(sim.NEW_STATE, f)[: used * t ** 3].cpu().numpy() for f in range(24)])
+        sim.close()
+    for f in range(24):
+        same(states[1][f], states[0][f], f"tuned vs default slab depth: field {f}")
+
+
+def test_autotune_rejects_the_wave_plugin(am, cuda):
+    sim = am.Sim(am.Config(28, 2, 100.0), am.SIM_WAVE, slots=9, mode=am.MODE_BATCHED)
     with pytest.raises(RuntimeError):
         sim.autotune(2)
     sim.close()
