@@ -312,51 +312,64 @@ __device__ __forceinline__ void rk_update(const EvoArgs& a, int f, uint64_t pi, 
 }
 
 // BSSN right-hand side and RK stage update: a CTA per kRhsCells consecutive interior cells of one
-// domain.  The cells' BSSN_ND derivative values arrive in shared memory as one bulk copy per
-// derivative plane (kRhsCells * 4 bytes, contiguous in the inner layout), all issued at once by
-// thread 0 and counted on one mbarrier, while every thread loads its cell's fields; the
-// right-hand side then reads its derivatives from shared memory (consecutive threads read
-// consecutive words).
+// domain, every input in shared memory before the arithmetic starts.  Thread 0 issues one bulk
+// copy per derivative plane (and, after the first stage, per RK-accumulator plane): kRhsCells * 4
+// contiguous bytes of the inner layout each, counted on one mbarrier.  Every thread meanwhile
+// issues 4-byte asynchronous copies (cp.async) of its cell's fields and their step-start values
+// from the padded layout, and waits for its own.  Consecutive threads read consecutive words.
 constexpr int kRhsCells = 128;
-constexpr size_t kRhsSmem = (size_t)BSSN_ND * kRhsCells * 4u + 16u;
+constexpr int kRhsPlanes = BSSN_ND + 3 * BSSN_NF;   // derivatives, fields, step-start values, accumulator
+constexpr size_t kRhsSmem = (size_t)kRhsPlanes * kRhsCells * 4u + 16u;
+
+__device__ __forceinline__ void cp_async4(float* dst_smem, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
 
 template <int N>
 __global__ void __launch_bounds__(kRhsCells) k_evo_rhs_bssn(const __grid_constant__ EvoArgs a) {
-    constexpr int P = 3, T = N + 2 * P;
+    constexpr int P = 3, T = N + 2 * P, C = kRhsCells;
     constexpr uint32_t CHUNKS = (uint32_t)(N * N * N / kRhsCells);
     static_assert((N * N * N) % kRhsCells == 0 && (kRhsCells * 4) % 16 == 0, "whole, aligned chunks per domain");
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    float* sd = reinterpret_cast<float*>(smem_raw);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)BSSN_ND * kRhsCells * 4u);
+    float* sd = reinterpret_cast<float*>(smem_raw);   // [BSSN_ND][C] derivatives
+    float* su = sd + (size_t)BSSN_ND * C;              // [BSSN_NF][C] fields (stored form)
+    float* so = su + (size_t)BSSN_NF * C;              // [BSSN_NF][C] step-start values (stages 2-4)
+    float* sa = so + (size_t)BSSN_NF * C;              // [BSSN_NF][C] RK accumulator (stages 2-4)
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sa + (size_t)BSSN_NF * C);
     const uint32_t tid = threadIdx.x;
     const uint32_t item = blockIdx.x / CHUNKS, chunk = blockIdx.x % CHUNKS;
     if (item >= a.n_items) return;   // the whole CTA
     const uint32_t slot = a.items[item];
     const uint32_t cell = chunk * (uint32_t)kRhsCells + tid;
     const uint64_t ii0 = (uint64_t)slot * N * N * N + chunk * (uint32_t)kRhsCells;
+    const bool later = a.stage != 1;   // stages 2-4 read the step-start state and the accumulator
     if (tid == 0) {
         mbar_init(bar, 1);
         mbar_fence_init();
     }
     __syncthreads();
     if (tid == 0) {
-        mbar_arrive_expect_tx(bar, (uint32_t)(BSSN_ND * kRhsCells * 4));
+        mbar_arrive_expect_tx(bar, (uint32_t)((BSSN_ND + (later ? BSSN_NF : 0)) * C * 4));
         for (int k = 0; k < BSSN_ND; k++)
-            bulk_g2s(sd + k * kRhsCells, a.deriv + (uint64_t)k * a.deriv_stride + ii0, kRhsCells * 4u, bar);
+            bulk_g2s(sd + k * C, a.deriv + (uint64_t)k * a.deriv_stride + ii0, C * 4u, bar);
+        if (later)
+            for (int f = 0; f < BSSN_NF; f++) bulk_g2s(sa + f * C, a.acc[f] + ii0, C * 4u, bar);
     }
     const uint32_t x = cell % N, y = (cell / N) % N, z = cell / (N * N);
-    const int depth = pos_depth(a.positions[slot]);
-    const float dt = a.dt0 / (float)(1u << depth);
     const uint64_t pi = (uint64_t)slot * T * T * T + ((uint64_t)(z + P) * T + (y + P)) * T + (x + P);
     const uint64_t ii = ii0 + tid;
-    float u[BSSN_NF], uo[BSSN_NF];
 #pragma unroll
     for (int f = 0; f < BSSN_NF; f++) {
-        const float s = a.fields[f][pi];   // the stored form
-        u[f] = s + bssn_offset(f);
-        uo[f] = a.stage == 1 ? s : a.old_f[f][pi];
+        cp_async4(su + f * C + tid, a.fields[f] + pi);
+        if (later) cp_async4(so + f * C + tid, a.old_f[f] + pi);
     }
-    // every copy lands before any thread reads shared memory or leaves (bounded waits)
+    const int depth = pos_depth(a.positions[slot]);
+    const float dt = a.dt0 / (float)(1u << depth);
+    cp_async_wait_all();   // this thread's own copies (only it reads them)
+    // every bulk copy lands before any thread reads them or leaves (bounded waits)
     const bool ok = __syncthreads_and(mbar_wait(bar, 0));
     if (!ok) {
         if (tid == 0) {
@@ -366,14 +379,30 @@ __global__ void __launch_bounds__(kRhsCells) k_evo_rhs_bssn(const __grid_constan
         __syncthreads();
         return;
     }
-    auto dv = [&](int k) { return sd[k * kRhsCells + tid]; };
+    float u[BSSN_NF];
+#pragma unroll
+    for (int f = 0; f < BSSN_NF; f++) u[f] = su[f * C + tid] + bssn_offset(f);
+    auto dv = [&](int k) { return sd[k * C + tid]; };
     float rhs[BSSN_NF];
     bssn_rhs(u, dv, a.prm, rhs);
+    // RK4 (rk_update): stage 1: acc = old + dt/6 k1, out = old + dt/2 k1; stage 2: acc += dt/3 k2,
+    // out = old + dt/2 k2; stage 3: acc += dt/3 k3, out = old + dt k3; stage 4: out = acc + dt/6 k4
+    const float c_acc = a.stage == 1 ? dt * (1.f / 6.f) : dt * (1.f / 3.f);
+    const float c_out = a.stage == 3 ? dt : (a.stage == 4 ? dt * (1.f / 6.f) : dt * .5f);
 #pragma unroll
     for (int f = 0; f < BSSN_NF; f++) {
         const float r = rhs[f] + dv(D_EXTRA + f);
+        const float uo = later ? so[f * C + tid] : su[f * C + tid];   // the stored form
+        float v;
+        if (a.stage == 4) {
+            v = fmaf(c_out, r, sa[f * C + tid]);
+        } else {
+            a.acc[f][ii] = fmaf(c_acc, r, later ? sa[f * C + tid] : uo);
+            v = fmaf(c_out, r, uo);
+        }
         // chi (stored less 1) is kept at or above its floor, as the geometry divides by it
-        rk_update(a, f, pi, ii, uo[f], r, dt, f == F_CHI ? a.prm.chi_floor - 1.f : -INFINITY);
+        const float lo = f == F_CHI ? a.prm.chi_floor - 1.f : -INFINITY;
+        a.out[f][pi] = v < lo ? lo : v;
     }
 }
 
