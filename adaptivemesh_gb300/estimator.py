@@ -97,8 +97,10 @@ def binary_punctures(seed: int, separation: float = 6.0, mass: float = 0.5, jitt
     return out
 
 
-def refine_around(sim, points, depth: int, outer: float) -> None:
-    """Refine every domain that contains or touches one of the points down to `depth`."""
+def refine_around(sim, points, depth: int, outer: float, margin: float = 1.25) -> None:
+    """Refine every domain that contains or touches one of the points down to `depth`: a domain is
+    refined when a point lies within `margin` half-edges of its centre along every axis (1.25: the
+    domain and a quarter of its neighbours; larger margins refine shells of neighbours too)."""
     for d in range(depth):
         st = sim.state()
         used, pos, ch = st["used_slots"], st["positions"], st["children"]
@@ -116,7 +118,7 @@ def refine_around(sim, points, depth: int, outer: float) -> None:
                 path >>= 3
             c *= outer
             half = outer / 2 / (1 << d)
-            if not any(np.all(np.abs(np.asarray(q) - c) <= half * 1.25) for q in points):
+            if not any(np.all(np.abs(np.asarray(q) - c) <= half * margin) for q in points):
                 continue
             for o in range(8):
                 if ch[s * 8 + o] == -1:

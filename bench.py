@@ -365,6 +365,8 @@ def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: 
     bmode = {"graph": am.MODE_GRAPH, "batched": am.MODE_BATCHED}[batched_mode]
     if case in ("all", "gauge_wave"):
         out["gauge_wave"] = gauge_wave_report(am, cases, bmode, cpu, plain, gw_depth, gw_steps)
+    if case in ("all", "single"):
+        out["single_puncture"] = single_puncture_report(am, E, bmode, plain)
     if case in ("all", "binary"):
         out["binary"] = binary_report(am, E, estimator_path, bmode, plain)
     if case == "pareto":
@@ -413,6 +415,74 @@ def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool, depth: int 
         except Exception as e:   # no fixture or oracle library
             gw["cpu_fp64"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
     return gw
+
+
+def leaf_zone_cycles_of_substep(st, n: int, s: int) -> int:
+    """Leaf zones that advance at substep s (a depth-d leaf advances when s is a multiple of
+    2^(max_depth - d))."""
+    used, pos, ch, md = st["used_slots"], st["positions"], st["children"], st["max_depth"]
+    total = 0
+    for k in range(used):
+        p = int(pos[k])
+        if p != 0xFFFFFFFF and all(c == -1 for c in ch[8 * k:8 * k + 8]) and s % (1 << (md - (p >> 27))) == 0:
+            total += n ** 3
+    return total
+
+
+def single_puncture_report(am, E, bmode: int, plain: bool) -> dict:
+    """A single Brill-Lindquist puncture (m = 1, seeded offset |d| < 0.05) on [-64, 64]^3, refined
+    around it to depth 6 with shells of neighbours (2 121 domains of 16^3, 1 856 leaves), 1+log
+    slicing and the Gamma-driver (eta = 2).  Batched: the derivative pass's slab depth autotuned,
+    one root step (64 finest substeps) replayed from a CUDA graph after a warm-up root step.  Both
+    forms also run the first two substeps phase by phase (every domain active, then the finest
+    level alone), the plain per-domain launches against the batched ones, which compute the same
+    state bit for bit; a whole plain root step would take about a minute."""
+    import numpy as np
+    rng = np.random.default_rng(2024)
+    d = rng.normal(size=3)
+    d = d / np.linalg.norm(d) * rng.uniform(0.0, 0.05)
+    punct = [(1.0, tuple(float(v) for v in d))]
+    rep = {"puncture": punct[0][1]}
+    phases = (am.PHASE_COPY_BACK, am.PHASE_MODIFY_NODES, am.PHASE_PREDICTOR, am.PHASE_COPY_BOUNDS,
+              am.PHASE_CORRECTOR, am.PHASE_INCREMENT_TIMER)
+    arms = [("batched", bmode)] + ([("plain", am.MODE_PLAIN)] if plain else [])
+    for name, mode in arms:
+        progress(f"evolution: single puncture, {name}")
+        sim = am.Sim(am.Config(16, 3, 128.0), am.SIM_BSSN_EVOLVE, slots=2200, mode=mode)
+        E.refine_around(sim, [punct[0][1]], 6, 128.0, margin=3.25)
+        sim.set_evolution(am.Evolution(slicing=am.SLICING_1PLUSLOG, shift=1, eta=2.0, ko_sigma=0.1, cfl=0.25))
+        sim.initial_data(am.InitialData(kind=am.ID_BRILL_LINDQUIST, punctures=punct))
+        st = sim.state()
+        arm = {}
+        if mode != am.MODE_PLAIN:
+            arm["derivative_slab_planes"] = next(iter(sim.autotune(3).values()))
+            sim.timestep()                   # warm-up (graph capture)
+            sim.synchronize()
+            sim.event_record(0)
+            sim.timestep()
+            sim.event_record(1)
+            sim.synchronize()
+            ms = sim.event_elapsed(0, 1)
+            arm.update({"value": zone_cycles_per_root_step(st, 16) / (ms / 1e3), "ms_per_root_step": ms})
+            arm.update({k: v for k, v in sim.constraint_norms(1.0).items() if k != "cells"})
+        sim.synchronize()
+        sim.event_record(0)
+        for _ in range(2):                   # substeps 0 and 1, phase by phase
+            for ph in phases:
+                sim.phase(ph)
+        sim.event_record(1)
+        sim.synchronize()
+        ms2 = sim.event_elapsed(0, 1)
+        zc2 = leaf_zone_cycles_of_substep(st, 16, 0) + leaf_zone_cycles_of_substep(st, 16, 1)
+        arm["first_two_substeps"] = {"value": zc2 / (ms2 / 1e3), "ms": ms2}
+        rep[name] = arm
+        rep["domains"] = st["used_slots"]
+        rep["leaves"] = sum(1 for k in range(st["used_slots"]) if st["positions"][k] != 0xFFFFFFFF and
+                            all(c == -1 for c in st["children"][8 * k:8 * k + 8]))
+        sim.close()
+    if plain:
+        rep["speedup_first_two_substeps"] = rep["batched"]["first_two_substeps"]["value"] / rep["plain"]["first_two_substeps"]["value"]
+    return rep
 
 
 def binary_run(am, E, punct, params, net, bmode: int, steps: int = 16) -> tuple[dict, object]:
@@ -534,7 +604,7 @@ def main() -> None:
     ap.add_argument("--no-evolution", action="store_true", help="leave out the evolution's report")
     ap.add_argument("--no-autotune", action="store_true", help="time the library's launch-shape rule, untuned")
     ap.add_argument("--estimator", default=None, help="trained estimator weights (.npz) for the evolution's report")
-    ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "binary", "pareto"],
+    ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "single", "binary", "pareto"],
                     help="--plugin evolution: the configurations to run")
     ap.add_argument("--no-plain", action="store_true", help="--plugin evolution: leave out the plain launches")
     ap.add_argument("--evo-depth", type=int, default=3, help="--plugin evolution: the gauge wave's uniform octree depth")

@@ -59,6 +59,23 @@ def tree_uniform(o, depth: int):
         level = nxt
 
 
+def tree_random(o, depth: int, p_refine: float = 0.3, seed: int = 0):
+    """Seeded Bernoulli refinement: the root is refined, then every domain at depth 1 .. depth-1 is
+    refined (all eight octants) with probability p_refine, level by level."""
+    rng = np.random.default_rng(seed)
+    level = [0]
+    for d in range(depth):
+        nxt = []
+        for p in level:
+            if d > 0 and rng.random() >= p_refine:
+                continue
+            for c in range(8):
+                idx = o.state()["first_free"]
+                o.add_node(p, c)
+                nxt.append(idx)
+        level = nxt
+
+
 def tree_root(o):
     """The root alone: one domain at depth 0, no ghost fill."""
 
