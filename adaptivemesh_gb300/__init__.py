@@ -160,6 +160,7 @@ EXPORTS = {
     "amr_sim_rng": (ctypes.c_int, [VP, ctypes.POINTER(I32)]),
     "amr_sim_set_rng": (ctypes.c_int, [VP, I32]),
     "amr_sim_stream": (ctypes.c_int, [VP, ctypes.POINTER(VP)]),
+    "amr_sim_set_stream": (ctypes.c_int, [VP, VP]),
     "amr_sim_synchronize": (ctypes.c_int, [VP]),
     "amr_sim_kernel_launches": (U64, [VP]),
     "amr_sim_set_stencil_ctas": (ctypes.c_int, [VP, U32]),

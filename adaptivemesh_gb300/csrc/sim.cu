@@ -994,6 +994,10 @@ AMR_API int amr_sim_stream(amr_sim* s, void** stream) {
     *stream = s->impl->stream;
     return AMR_OK;
 }
+AMR_API int amr_sim_set_stream(amr_sim* s, void* stream) {
+    if (!s) return AMR_ERR_INVALID;
+    return s->impl->set_stream(static_cast<cudaStream_t>(stream));
+}
 AMR_API int amr_sim_synchronize(amr_sim* s) {
     if (!s) return AMR_ERR_INVALID;
     int st = s->impl->sync_transfer_streams();

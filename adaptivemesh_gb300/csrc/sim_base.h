@@ -56,12 +56,13 @@ public:
         cudaFree(ghost_stage);
         for (auto& ev : events) cudaEventDestroy(ev);
         for (auto& ev : user_events) if (ev) cudaEventDestroy(ev);
-        if (stream) cudaStreamDestroy(stream);
+        if (own_stream) cudaStreamDestroy(own_stream);   // a caller's stream stays the caller's
     }
 
     virtual int init() {
         const uint32_t s = tree.max_slots();
         cudaError_t e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+        own_stream = stream;
         if (e == cudaSuccess) e = dev_alloc(&d_positions, s);
         if (e == cudaSuccess) e = dev_alloc(&d_children, (size_t)s * 8u);
         if (e == cudaSuccess) e = dev_alloc(&d_boundaries, (size_t)s * 6u);
@@ -256,7 +257,19 @@ public:
     Geo geo;
     int mode;
     Octree tree;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;       // where the simulation's work goes: its own or a caller's
+    cudaStream_t own_stream = nullptr;   // the stream the simulation created (destroyed with it)
+    // Run the simulation's work on a caller's stream from now on (nullptr: its own again); the
+    // work queued so far, on every stream of the simulation, completes first.
+    int set_stream(cudaStream_t s) {
+        if (capturing) return AMR_ERR_INVALID;
+        int st = sync_transfer_streams();
+        if (!st && side_stream && cudaStreamSynchronize(side_stream) != cudaSuccess) st = AMR_ERR_CUDA;
+        if (!st) st = cuda_status(cudaStreamSynchronize(stream));
+        if (st) return st;
+        stream = s ? s : own_stream;
+        return AMR_OK;
+    }
     uint32_t* d_positions = nullptr;
     int32_t* d_children = nullptr;
     uint64_t* d_boundaries = nullptr;

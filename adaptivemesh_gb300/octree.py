@@ -238,6 +238,10 @@ class Sim:
         check(load().amr_sim_stream(self.h, ctypes.byref(s)), "amr_sim_stream")
         return int(s.value or 0)
 
+    def set_stream(self, stream: int) -> None:
+        """Run the simulation's work on a caller's stream (a cudaStream_t as an int; 0: its own)."""
+        check(load().amr_sim_set_stream(self.h, stream or None), "amr_sim_set_stream")
+
     def synchronize(self) -> None:
         check(load().amr_sim_synchronize(self.h), "amr_sim_synchronize")
 

@@ -307,6 +307,12 @@ int amr_sim_set_octree(amr_sim* s, const uint32_t* positions, const int32_t* par
 int amr_sim_rng(const amr_sim* s, int32_t* seed);
 int amr_sim_set_rng(amr_sim* s, int32_t seed);
 int amr_sim_stream(amr_sim* s, void** stream);
+/* Enqueue the simulation's work on a caller-supplied stream from now on (the reference passes its
+ * cudaStream_t& to every operator, AMR.h:880-1310); nullptr returns to the simulation's own stream.
+ * Everything queued so far completes first.  The stream must not be the legacy default stream
+ * (AMR_MODE_GRAPH captures on it) and must outlive its use by the simulation (amr_sim_destroy
+ * synchronises it but does not destroy it).  Not during a stream capture. */
+int amr_sim_set_stream(amr_sim* s, void* stream);
 /* Wait for the simulation's work; AMR_ERR_TIMEOUT (once) if a kernel gave up a bounded wait. */
 int amr_sim_synchronize(amr_sim* s);
 /* Kernel launches the library issued for this simulation since creation (graph replays count

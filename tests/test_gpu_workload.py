@@ -257,6 +257,37 @@ def test_autotune_evolution_slab_depth(am, cuda):
         same(states[1][f], states[0][f], f"tuned vs default slab depth: field {f}")
 
 
+@pytest.mark.parametrize("mode", ["graph", "batched"])
+def test_caller_stream(am, cuda, mode):
+    """amr_sim_set_stream: the simulation enqueues on a caller's stream (a torch stream here), graph
+    capture included; two timesteps on it equal two timesteps on the simulation's own stream bit
+    for bit, and the caller's stream carries the work (a torch event recorded on it after the
+    timesteps sees the results)."""
+    import torch
+    cfg = am.Config(16, 3, 100.0)
+    m = {"graph": am.MODE_GRAPH, "batched": am.MODE_BATCHED}[mode]
+    results = []
+    for use_caller in (False, True):
+        sim, st, _ = _uniform_sim(am, cfg, 2, m)
+        s = torch.cuda.Stream()
+        if use_caller:
+            sim.set_stream(s.cuda_stream)
+            assert sim.stream == s.cuda_stream
+        sim.timestep()
+        sim.timestep()
+        if use_caller:
+            done = torch.cuda.Event()
+            done.record(s)
+            done.synchronize()
+            sim.set_stream(0)   # back to its own
+        sim.synchronize()
+        results.append(dump(am, sim, st["used_slots"], cfg))
+        sim.close()
+    for k, v in results[0].items():
+        if k != "rng":
+            same(results[1][k], v, f"caller's stream vs own: {k}")
+
+
 def test_autotune_rejects_the_wave_plugin(am, cuda):
     sim = am.Sim(am.Config(28, 2, 100.0), am.SIM_WAVE, slots=9, mode=am.MODE_BATCHED)
     with pytest.raises(RuntimeError):
