@@ -357,7 +357,10 @@ def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: 
                   error estimate on the estimator's training samples); 16 root steps batched,
                   regrids and graph recaptures included in the time; the plain per-domain launches
                   timed over one root step on the plain-criterion tree.  H and M L2 outside r = 1
-                  of each puncture after the run."""
+                  of each puncture after the run.
+      single_puncture  one puncture nested to depth 6 (2 121 domains of 16^3), batched against the
+                  plain per-domain launches (single_puncture_report)
+      sweep       random octrees of 16^3 and 32^3 domains with 1-4 punctures (sweep_report)"""
     import adaptivemesh_gb300 as am
     from adaptivemesh_gb300 import estimator as E
     import cases
@@ -369,6 +372,8 @@ def evolution_report(cpu: bool = True, estimator_path: str | None = None, case: 
         out["single_puncture"] = single_puncture_report(am, E, bmode, plain)
     if case in ("all", "binary"):
         out["binary"] = binary_report(am, E, estimator_path, bmode, plain)
+    if case in ("all", "sweep"):
+        out["sweep"] = sweep_report(am, cases, bmode)
     if case == "pareto":
         out["pareto"] = pareto_report(am, E, estimator_path, bmode)
     return out
@@ -483,6 +488,43 @@ def single_puncture_report(am, E, bmode: int, plain: bool) -> dict:
     if plain:
         rep["speedup_first_two_substeps"] = rep["batched"]["first_two_substeps"]["value"] / rep["plain"]["first_two_substeps"]["value"]
     return rep
+
+
+def sweep_report(am, cases, bmode: int) -> list:
+    """The throughput sweep's octrees: seeded Bernoulli(0.3) refinement per level (cases.tree_random)
+    to depth 6 with 16^3 domains (1 569 domains) and to depth 5 with 32^3 domains (1 265), root edge
+    64, holding 1-4 Brill-Lindquist punctures of seeded masses in [0.2, 1] and positions in
+    [-8, 8]^3, 1+log slicing and the Gamma-driver: slab depth autotuned, one root step of batched
+    launches (each a few seconds long, so launch overhead is negligible and no graph is captured)."""
+    import numpy as np
+    out = []
+    bmode = am.MODE_BATCHED
+    for n, depth, seed, slots in ((16, 6, 3, 1569), (32, 5, 25, 1265)):
+        progress(f"evolution: sweep, {n}^3 domains")
+        rng = np.random.default_rng(100 + seed)
+        punct = [(float(rng.uniform(0.2, 1.0)), tuple(float(v) for v in rng.uniform(-8.0, 8.0, 3)))
+                 for _ in range(1 + seed % 4)]
+        sim = am.Sim(am.Config(n, 3, 64.0), am.SIM_BSSN_EVOLVE, slots=slots, mode=bmode)
+        cases.tree_random(sim, depth, 0.3, seed)
+        sim.set_evolution(am.Evolution(slicing=am.SLICING_1PLUSLOG, shift=1, eta=2.0, ko_sigma=0.1, cfl=0.25))
+        sim.initial_data(am.InitialData(kind=am.ID_BRILL_LINDQUIST, punctures=punct))
+        st = sim.state()
+        zs = next(iter(sim.autotune(2).values()))
+        sim.synchronize()
+        sim.event_record(0)
+        sim.timestep()
+        sim.event_record(1)
+        sim.synchronize()
+        ms = sim.event_elapsed(0, 1)
+        leaves = sum(1 for k in range(st["used_slots"]) if st["positions"][k] != 0xFFFFFFFF and
+                     all(c == -1 for c in st["children"][8 * k:8 * k + 8]))
+        row = {"size_domain": n, "max_depth": st["max_depth"], "domains": st["used_slots"], "leaves": leaves,
+               "punctures": len(punct), "derivative_slab_planes": zs,
+               "value": zone_cycles_per_root_step(st, n) / (ms / 1e3), "ms_per_root_step": ms}
+        row.update({k: v for k, v in sim.constraint_norms(1.0).items() if k != "cells"})
+        out.append(row)
+        sim.close()
+    return out
 
 
 def binary_run(am, E, punct, params, net, bmode: int, steps: int = 16) -> tuple[dict, object]:
@@ -604,7 +646,7 @@ def main() -> None:
     ap.add_argument("--no-evolution", action="store_true", help="leave out the evolution's report")
     ap.add_argument("--no-autotune", action="store_true", help="time the library's launch-shape rule, untuned")
     ap.add_argument("--estimator", default=None, help="trained estimator weights (.npz) for the evolution's report")
-    ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "single", "binary", "pareto"],
+    ap.add_argument("--evo-case", default="all", choices=["all", "gauge_wave", "single", "binary", "sweep", "pareto"],
                     help="--plugin evolution: the configurations to run")
     ap.add_argument("--no-plain", action="store_true", help="--plugin evolution: leave out the plain launches")
     ap.add_argument("--evo-depth", type=int, default=3, help="--plugin evolution: the gauge wave's uniform octree depth")

@@ -80,6 +80,26 @@ def test_gauge_wave_matches_fp64(am, cuda, orc, mode):
     sim.close()
 
 
+def test_gauge_wave_32_matches_fp64(am, cuda, orc):
+    """The same periodic gauge wave on 32^3 domains (uniform depth 1: 64^3 zones), one root step on
+    the GPU (the derivative pass at its 32^3 slab depth) against the FP64 oracle: every field within
+    1e-4 of its scale, as at 8^3."""
+    build = lambda o: cases.tree_uniform(o, 1)   # noqa: E731
+    ev_g = am.Evolution(slicing=am.SLICING_1PLUSLOG, shift=0, ko_sigma=0.1, cfl=0.25, periodic=1)
+    data = am.InitialData(kind=am.ID_GAUGE_WAVE, amplitude=0.05, wavelength=1.0)
+    sim = gpu_sim(am, 32, 1.0, build, am.SIM_BSSN_EVOLVE, ev_g, data, am.MODE_GRAPH, slots=9)
+    sim.timestep()
+    sim.synchronize()
+    st = sim.state()
+    gpu = gpu_state(am, sim, 24)
+    sim.close()
+    e = evo_params(orc, 32, 1.0, slicing=0, shift=0, id_kind=1, amplitude=0.05, wavelength=1.0)
+    ref = OracleEvolution(orc, e, st)
+    ref.timestep(1)
+    worst = compare(gpu, ref.new, st, 32, 1e-4, "gauge wave 32^3")
+    print(f"\ngauge wave on 32^3 domains, GPU FP32 vs FP64 after one root step: worst field error {worst:.2e} of scale")
+
+
 def test_puncture_matches_fp64(am, cuda, orc):
     """A Brill-Lindquist puncture (m = 1, offset) on the reference's nested tree (kernel.cu:69-83,
     depth 6, 8^3 domains) with 1+log slicing and the Gamma-driver shift: one root step (64 substeps
