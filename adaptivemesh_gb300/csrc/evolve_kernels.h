@@ -35,6 +35,8 @@ struct EvoGhostArgs {
     int axis;
     int nf;
     float c_stage;                // time of the state being filled, as a fraction of the target's step
+    uint32_t interp_floats;       // shared memory of the interpolating faces (set by the launcher)
+    int* err;                     // raised when a face needs more than that
 };
 
 // Device addresses of the four constraint buffers (H, M_x, M_y, M_z; inner layout).

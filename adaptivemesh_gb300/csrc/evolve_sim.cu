@@ -558,6 +558,7 @@ private:
         g.max_depth = (uint32_t)tree.read_max_depth();
         g.nf = nf;
         g.c_stage = c_stage;
+        g.err = err_flag;
         for (int axis = 0; axis < 3; axis++) {   // every domain's pass along an axis before the next axis
             g.axis = axis;
             if (mode == AMR_MODE_PLAIN) {   // one launch per domain

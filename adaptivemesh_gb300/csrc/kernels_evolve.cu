@@ -433,6 +433,23 @@ __global__ void __launch_bounds__(256) k_evo_rhs_wave(const __grid_constant__ Ev
 // (one face-normal axis) no cell is both read and written: the fill writes the cells whose index
 // along the axis lies in a ghost layer and reads sources inside the interior along it.
 constexpr int kGhostFields = 4;
+constexpr uint32_t kGhostMaxT = 38;   // the largest padded edge (32 + 2 * 3)
+// Shared memory of the interpolating faces, in floats, for padded edge t, size n, padding p: the
+// per-axis tables, then the largest source box (E_a <= ext_a / 2 + 5 cells along each axis, the
+// source being at least twice as coarse) and the two intermediate stages, over the three passes.
+inline uint32_t ghost_interp_floats(uint32_t n, uint32_t p, uint32_t t) {
+    uint32_t best = 0;
+    for (uint32_t d = 0; d < 3; d++) {
+        uint32_t ext[3], E[3];
+        for (uint32_t a = 0; a < 3; a++) {
+            ext[a] = a == d ? p : (a < d ? t : n);
+            E[a] = ext[a] / 2u + 5u;
+        }
+        const uint32_t need = E[0] * E[1] * E[2] + E[2] * E[1] * ext[0] + E[2] * ext[1] * ext[0];
+        best = need > best ? need : best;
+    }
+    return best;
+}
 
 __global__ void __launch_bounds__(256, 4) k_evo_ghost(const __grid_constant__ EvoGhostArgs g) {
     const uint32_t item = blockIdx.x >> 1, side = blockIdx.x & 1u;   // side 0: + face, 1: - face
@@ -462,7 +479,6 @@ __global__ void __launch_bounds__(256, 4) k_evo_ghost(const __grid_constant__ Ev
         const uint32_t kp = (g.substep >> (g.max_depth - (uint32_t)cd)) & ((1u << dd) - 1u);
         frac = ((float)kp + g.c_stage) / (float)(1u << dd);
     }
-    const bool use0 = mode != 1, use1 = mode != 0;   // which of the two source states are read
     const float3 relp = cf3_decode((uint32_t)(bd >> 32));
     const float rel_scale = 1.f / (float)(1u << dd);
     // extents of the fill: axes before d over the whole padded range (their ghosts are filled),
@@ -485,11 +501,12 @@ __global__ void __launch_bounds__(256, 4) k_evo_ghost(const __grid_constant__ Ev
     // a same-depth source is this domain shifted by rel * n cells (rel = 0 or +-1 per axis, exact)
     const int r0 = __float2int_rn(relp.x * (float)n), r1 = __float2int_rn(relp.y * (float)n),
               r2 = __float2int_rn(relp.z * (float)n);
-    for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) {
-        const uint32_t q = (uint32_t)(((uint64_t)k * m0) >> 21), q2 = (uint32_t)(((uint64_t)q * m1) >> 21);
-        const uint32_t w0 = lo0 + (k - q * ext0), w1 = lo1 + (q - q2 * ext1), w2 = lo2 + q2;
-        const uint64_t dst = (uint64_t)slot * cells + ((uint64_t)w2 * t + w1) * t + w0;
-        if (exact) {   // a copy: every load of the group, then the stores
+    if (exact) {
+        for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) {
+            const uint32_t q = (uint32_t)(((uint64_t)k * m0) >> 21), q2 = (uint32_t)(((uint64_t)q * m1) >> 21);
+            const uint32_t w0 = lo0 + (k - q * ext0), w1 = lo1 + (q - q2 * ext1), w2 = lo2 + q2;
+            const uint64_t dst = (uint64_t)slot * cells + ((uint64_t)w2 * t + w1) * t + w0;
+            // a copy: every load of the group, then the stores
             const int64_t si = (int64_t)src * (int64_t)cells + ((int64_t)((int)w2 + r2) * t + ((int)w1 + r1)) * t +
                                ((int)w0 + r0);
             float v[kGhostFields];
@@ -499,72 +516,96 @@ __global__ void __launch_bounds__(256, 4) k_evo_ghost(const __grid_constant__ Ev
 #pragma unroll
             for (int q4 = 0; q4 < kGhostFields; q4++)
                 if (q4 < nfg) g.X[f0 + q4][dst] = v[q4];
-            continue;
         }
-        // source cell (same depth: the cell itself) or the base cell b of a tricubic stencil b-1 .. b+2
-        // kept inside the cells that are valid: the interior along the normal axis and the later
-        // axes, the whole padded range along the earlier axes (filled by earlier passes) and
-        // everywhere in the root (its frozen ghost layer is the outer boundary)
-        int idx[3];
-        float wgt[3][4];
-        auto axis_taps = [&](uint32_t a2, uint32_t wa, float rela) {
-            float rp = ((float)wa - (float)p + .5f) / (float)n - .5f;
-            rp = rp * rel_scale + rela;
-            const float ri = (rp + .5f) * (float)n + (float)p - .5f;
-            if (exact) {
-                idx[a2] = __float2int_rn(ri);
-            } else {
-                const int lo_c = root_src || a2 < d ? 1 : (int)p + 1;
-                const int hi_c = root_src || a2 < d ? (int)t - 3 : (int)(t - p) - 3;
-                int b = __float2int_rd(ri);
-                b = b < lo_c ? lo_c : (b > hi_c ? hi_c : b);
-                const float x = ri - (float)b;
-                idx[a2] = b;
-                wgt[a2][0] = -x * (x - 1.f) * (x - 2.f) * (1.f / 6.f);
-                wgt[a2][1] = (x + 1.f) * (x - 1.f) * (x - 2.f) * .5f;
-                wgt[a2][2] = -(x + 1.f) * x * (x - 2.f) * .5f;
-                wgt[a2][3] = (x + 1.f) * x * (x - 1.f) * (1.f / 6.f);
-            }
-        };
-        axis_taps(0, w0, relp.x);
-        axis_taps(1, w1, relp.y);
-        axis_taps(2, w2, relp.z);
-        const int64_t si = (int64_t)src * (int64_t)cells + ((int64_t)idx[2] * t + idx[1]) * t + idx[0];
-        float va[kGhostFields], vb[kGhostFields];
-#pragma unroll
-        for (int q = 0; q < kGhostFields; q++) { va[q] = 0.f; vb[q] = 0.f; }
-        if (exact) {
-#pragma unroll
-            for (int q = 0; q < kGhostFields; q++) {
-                if (use0) va[q] = A0(q)[si];
-                if (use1) vb[q] = A1(q)[si];
-            }
-        } else {
-#pragma unroll
-            for (int k2 = 0; k2 < 4; k2++)
-#pragma unroll
-                for (int k1 = 0; k1 < 4; k1++) {
-                    const float w12 = wgt[1][k1] * wgt[2][k2];
-                    const int64_t row = si + ((int64_t)(k2 - 1) * t + (k1 - 1)) * t - 1;
-#pragma unroll
-                    for (int k0 = 0; k0 < 4; k0++) {
-                        const float wk = wgt[0][k0] * w12;
-#pragma unroll
-                        for (int q = 0; q < kGhostFields; q++) {
-                            if (use0) va[q] = fmaf(wk, A0(q)[row + k0], va[q]);
-                            if (use1) vb[q] = fmaf(wk, A1(q)[row + k0], vb[q]);
-                        }
-                    }
-                }
+        return;
+    }
+    // A coarser source: separable tricubic interpolation through shared memory.  Along each axis a
+    // the ghost cell's coordinate w_a alone gives the base cell b_a of its four-point stencil
+    // b_a - 1 .. b_a + 2 and the four Lagrange weights; b_a is kept inside the cells that are
+    // valid (the interior along the normal axis and the later axes, the whole padded range along
+    // the earlier axes, which earlier passes filled, and everywhere in the root, whose frozen
+    // ghost layer is the outer boundary).  b_a grows with w_a, so the source cells read form a
+    // box.  Per field: the box, with the time interpolation applied to each source cell
+    // (frac X + (1 - frac) old, or old alone), then the interpolation along x, along y and along z,
+    // each stage through shared memory.
+    extern __shared__ __align__(16) float gsm[];
+    float* W = gsm;                                                  // [3][kGhostMaxT][4] weights
+    int* B = reinterpret_cast<int*>(W + 3 * kGhostMaxT * 4);         // [3][kGhostMaxT] base cells
+    float* S = reinterpret_cast<float*>(B + 3 * kGhostMaxT);         // source box (time-interpolated)
+    for (uint32_t e = threadIdx.x; e < ext0 + ext1 + ext2; e += blockDim.x) {
+        const uint32_t a2 = e < ext0 ? 0u : (e < ext0 + ext1 ? 1u : 2u);
+        const uint32_t j = e - (a2 == 0u ? 0u : (a2 == 1u ? ext0 : ext0 + ext1));
+        const uint32_t wa = (a2 == 0u ? lo0 : (a2 == 1u ? lo1 : lo2)) + j;
+        float rp = ((float)wa - (float)p + .5f) / (float)n - .5f;
+        rp = rp * rel_scale + (a2 == 0u ? relp.x : (a2 == 1u ? relp.y : relp.z));
+        const float ri = (rp + .5f) * (float)n + (float)p - .5f;
+        const int lo_c = root_src || a2 < d ? 1 : (int)p + 1;
+        const int hi_c = root_src || a2 < d ? (int)t - 3 : (int)(t - p) - 3;
+        int b = __float2int_rd(ri);
+        b = b < lo_c ? lo_c : (b > hi_c ? hi_c : b);
+        const float x = ri - (float)b;
+        B[a2 * kGhostMaxT + j] = b;
+        float* w = W + (a2 * kGhostMaxT + j) * 4;
+        w[0] = -x * (x - 1.f) * (x - 2.f) * (1.f / 6.f);
+        w[1] = (x + 1.f) * (x - 1.f) * (x - 2.f) * .5f;
+        w[2] = -(x + 1.f) * x * (x - 2.f) * .5f;
+        w[3] = (x + 1.f) * x * (x - 1.f) * (1.f / 6.f);
+    }
+    __syncthreads();
+    // the box: from b_min - 1 to b_max + 2 along each axis (the first and the last w_a)
+    const int bmin[3] = {B[0], B[kGhostMaxT], B[2 * kGhostMaxT]};
+    const int E[3] = {B[ext0 - 1] - bmin[0] + 4, B[kGhostMaxT + ext1 - 1] - bmin[1] + 4,
+                      B[2 * kGhostMaxT + ext2 - 1] - bmin[2] + 4};
+    const uint32_t nS = (uint32_t)(E[0] * E[1] * E[2]), nT1 = (uint32_t)(E[2] * E[1]) * ext0,
+                   nT2 = (uint32_t)E[2] * ext1 * ext0;
+    if (nS + nT1 + nT2 > g.interp_floats) {   // larger than the launch provided: report, skip the face
+        if (threadIdx.x == 0) atomicExch(g.err, 1);
+        return;
+    }
+    float* T1 = S + nS;    // [E2][E1][ext0]
+    float* T2 = T1 + nT1;  // [E2][ext1][ext0]
+    const int64_t sbase = (int64_t)src * (int64_t)cells;
+    for (int q4 = 0; q4 < nfg; q4++) {
+        const float* a0 = A0(q4);
+        const float* a1 = A1(q4);
+        for (uint32_t e = threadIdx.x; e < nS; e += blockDim.x) {
+            const uint32_t i0 = e % (uint32_t)E[0], r = e / (uint32_t)E[0];
+            const uint32_t i1 = r % (uint32_t)E[1], i2 = r / (uint32_t)E[1];
+            const int64_t si = sbase + ((int64_t)(bmin[2] - 1 + (int)i2) * t + (bmin[1] - 1 + (int)i1)) * t +
+                               (bmin[0] - 1 + (int)i0);
+            S[e] = mode == 0 ? a0[si] : fmaf(frac, a1[si], (1.f - frac) * a0[si]);
         }
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < nT1; e += blockDim.x) {   // along x
+            const uint32_t j0 = e % ext0, r = e / ext0;              // r = i2 * E1 + i1
+            const float* w = W + j0 * 4;
+            const float* src_row = S + r * (uint32_t)E[0] + (B[j0] - bmin[0]);
+            float v = 0.f;
 #pragma unroll
-        for (int q = 0; q < kGhostFields; q++) {
-            float v;
-            if (mode == 0) v = va[q];
-            else if (mode == 1) v = vb[q];
-            else v = fmaf(frac, vb[q], (1.f - frac) * va[q]);
-            if (q < nfg) g.X[f0 + q][dst] = v;
+            for (int k = 0; k < 4; k++) v = fmaf(w[k], src_row[k], v);
+            T1[e] = v;
         }
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < nT2; e += blockDim.x) {   // along y
+            const uint32_t j0 = e % ext0, r = e / ext0, j1 = r % ext1, i2 = r / ext1;
+            const float* w = W + (kGhostMaxT + j1) * 4;
+            const float* col = T1 + ((size_t)i2 * E[1] + (B[kGhostMaxT + j1] - bmin[1])) * ext0 + j0;
+            float v = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; k++) v = fmaf(w[k], col[(size_t)k * ext0], v);
+            T2[e] = v;
+        }
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < count; e += blockDim.x) {   // along z, into the ghost cells
+            const uint32_t j0 = e % ext0, r = e / ext0, j1 = r % ext1, j2 = r / ext1;
+            const float* w = W + (2 * kGhostMaxT + j2) * 4;
+            const float* col = T2 + ((size_t)(B[2 * kGhostMaxT + j2] - bmin[2]) * ext1 + j1) * ext0 + j0;
+            float v = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; k++) v = fmaf(w[k], col[(size_t)k * ext1 * ext0], v);
+            g.X[f0 + q4][(uint64_t)slot * cells + ((uint64_t)(lo2 + j2) * t + lo1 + j1) * t + lo0 + j0] = v;
+        }
+        __syncthreads();   // S, T1, T2 are reused by the next field
     }
 }
 
@@ -947,9 +988,16 @@ cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st) {
 
 cudaError_t launch_evo_ghost(const EvoGhostArgs& g, cudaStream_t st) {
     if (g.n_items == 0) return cudaSuccess;
-    if (g.t > 38u) return cudaErrorInvalidValue;   // the kernel's index arithmetic covers padded edges up to 38
+    if (g.t > kGhostMaxT) return cudaErrorInvalidValue;   // the kernel's index arithmetic and tables cover edges up to 38
+    EvoGhostArgs a = g;
+    a.interp_floats = ghost_interp_floats(g.n, g.p, g.t);
+    const size_t smem = (size_t)(3u * kGhostMaxT * 5u + a.interp_floats) * 4u;
+    static std::atomic<uint64_t> configured{0};   // the limit for the largest edge, once per device
+    const cudaError_t e = ensure_smem_limit(k_evo_ghost, (size_t)(3u * kGhostMaxT * 5u + ghost_interp_floats(32u, 3u, 38u)) * 4u,
+                                            configured);
+    if (e != cudaSuccess) return e;
     const dim3 grid(g.n_items * 2u, (unsigned)((g.nf + kGhostFields - 1) / kGhostFields));
-    k_evo_ghost<<<grid, 256, 0, st>>>(g);
+    k_evo_ghost<<<grid, 256, smem, st>>>(a);
     return cudaGetLastError();
 }
 
