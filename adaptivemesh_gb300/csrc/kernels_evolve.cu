@@ -317,7 +317,7 @@ __device__ __forceinline__ void rk_update(const EvoArgs& a, int f, uint64_t pi, 
 // contiguous bytes of the inner layout each, counted on one mbarrier.  Every thread meanwhile
 // issues 4-byte asynchronous copies (cp.async) of its cell's fields and their step-start values
 // from the padded layout, and waits for its own.  Consecutive threads read consecutive words.
-constexpr int kRhsCells = 128;
+constexpr int kRhsCells = 64;   // 42 KB of inputs per CTA: 5 CTAs per SM (128 cells: 2; 539 against 480 us)
 constexpr int kRhsPlanes = BSSN_ND + 3 * BSSN_NF;   // derivatives, fields, step-start values, accumulator
 constexpr size_t kRhsSmem = (size_t)kRhsPlanes * kRhsCells * 4u + 16u;
 
