@@ -8,8 +8,12 @@
 //   k_evo_derivs    derivative pass: a CTA per (domain, z-slab); each field's padded slab moves into
 //                   shared memory with one 1-D bulk copy (two buffers, the next field in flight),
 //                   then first / second / mixed derivatives, advection and Kreiss-Oliger terms
-//   k_evo_rhs_*     pointwise right-hand side and RK4 stage update
-//   k_evo_ghost     ghost fill of a stage's state, one face-normal axis per launch
+//   k_evo_rhs_*     pointwise right-hand side and RK4 stage update (BSSN: every input staged in
+//                   shared memory by bulk copies and cp.async first)
+//   k_evo_ghost     ghost fill of a stage's state, one face-normal axis per launch (copies from
+//                   same-depth neighbours, separable tricubic interpolation from coarser ones)
+//   k_evo_restrict  restriction of children into parents (leaves: 16-byte copies)
+//   k_evo_prolong   tricubic prolongation of new domains
 //   k_evo_constraints, k_evo_norms_*   Hamiltonian and momentum constraints, FP64 norms
 #include <cmath>
 #include <type_traits>
@@ -428,10 +432,12 @@ __global__ void __launch_bounds__(256) k_evo_rhs_wave(const __grid_constant__ Ev
 }
 
 // ------------------------------------------------------------------ ghost fill
-// A CTA per (slot, side, group of kGhostFields fields): the geometry of a ghost cell is computed
-// once per group, and every load of a cell's group is issued before its stores.  Within one launch
-// (one face-normal axis) no cell is both read and written: the fill writes the cells whose index
-// along the axis lies in a ghost layer and reads sources inside the interior along it.
+// A CTA per (slot, side, group of kGhostFields fields).  A same-depth face is a copy: the geometry of
+// a ghost cell is computed once per group and every load of a cell's group is issued before its
+// stores.  A face with a coarser source is interpolated separably through shared memory (below).
+// Within one launch (one face-normal axis) no cell is both read and written: the fill writes the
+// cells whose index along the axis lies in a ghost layer and reads sources inside the interior
+// along it.
 constexpr int kGhostFields = 4;
 constexpr uint32_t kGhostMaxT = 38;   // the largest padded edge (32 + 2 * 3)
 // Shared memory of the interpolating faces, in floats, for padded edge t, size n, padding p: the
