@@ -140,7 +140,7 @@ def fused_restriction_bytes_per_leaf() -> int:
 def golden_tree(depth: int) -> dict:
     """The uniform octree's arrays as the reference's own host code (AMR<T>, AMR.h:118-294) builds
     them, from the committed fixture (tests/golden/gen_host_golden.py), so that the CPU legs need
-    neither this library nor the checker library to lay out their work."""
+    neither this library nor the reference-build library to lay out their work."""
     import numpy as np
     hg = np.load(os.path.join(ROOT, "tests", "golden", "host_golden.npz"))
     key = f"tree/uniform{depth}"
@@ -238,13 +238,13 @@ def reference_arm(args) -> None:
     if steps < args.steps:
         line["steps_requested"] = args.steps
     # For comparison only (not this arm's value): the reference's own CUDA plugin on this GPU, its
-    # headers compiled for sm_103a into the checker library, on the same workload
+    # headers compiled for sm_103a into the reference-build library, on the same workload
     try:
         import torch
         if torch.cuda.is_available():
             from oracle import time_reference_gpu
             line["reference_gpu"] = time_reference_gpu.measure(N, P, args.depth, steps=10, warmup=2)
-    except Exception as e:  # no checker library for this size, or no reference headers staged
+    except Exception as e:  # no reference-build library for this size, or no reference headers staged
         line["reference_gpu"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
     print(json.dumps(line))
 
@@ -254,7 +254,7 @@ def wave_line(args) -> None:
     children and a smooth seeded blob: each timestep timed alone between device synchronisations
     (the plugin reads its criterion back to the host every substep), its leaf zones counted after
     it.  The reference plugin's figure on the same run comes from its own headers built for this
-    GPU (the timing script beside the checker library)."""
+    GPU (the timing script beside the reference-build library)."""
     import numpy as np
     import torch
     import adaptivemesh_gb300 as am

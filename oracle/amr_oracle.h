@@ -1,6 +1,6 @@
 /* amr_oracle.h -- CPU restatement of AdaptiveMesh's per-timestep hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA kernels are compared with:
+ * TEST INFRASTRUCTURE ONLY.  The CUDA kernels are compared with this restatement:
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs
  * load it (through oracle/oracle.py).  The product never links or calls it.
  *

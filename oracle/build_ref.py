@@ -1,4 +1,4 @@
-"""Build recipe for the reference checker libraries under oracle/_ref/.
+"""Build recipe for the reference-build libraries under oracle/_ref/.
 
 TEST INFRASTRUCTURE ONLY.  The libraries built here wrap the reference's own code
 (oracle/ref_harness.cu) and are loaded only by tests, the smoke check and the

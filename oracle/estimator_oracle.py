@@ -3,7 +3,7 @@ forward pass, mean-squared-error loss and its gradients, in float64 with the GPU
 applied at the same points (the GEMM operands: im2col matrices, weights, activations and the
 back-propagated gradients).
 
-TEST INFRASTRUCTURE ONLY: the checker of the GPU network's forward pass and gradients.  The
+TEST INFRASTRUCTURE ONLY: what the GPU network's forward pass and gradients are compared with.  The
 reference has no learned estimator; the network, its layouts and its parameter vector are this
 library's (documented in include/amr_gb300.h, amr_estimator_get_params).
 """

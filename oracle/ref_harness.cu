@@ -94,7 +94,7 @@ REF_API void refh_boundary_decode(uint64_t raw, int32_t* target, uint32_t* depth
     float3 r = d.rel_pos_t(); rel_pos3[0] = r.x; rel_pos3[1] = r.y; rel_pos3[2] = r.z;
 }
 
-// AMR<T> never initialises timer_helper (AMR.h:178, constructor AMR.h:189-191); the checker
+// AMR<T> never initialises timer_helper (AMR.h:178, constructor AMR.h:189-191); this harness
 // starts it at 0, the value a fresh timestep loop assumes.
 struct RefOctree { AMR<blank_AMR_data> amr; explicit RefOctree(uint32_t s) : amr(s) { amr.timer_helper = 0u; } };
 REF_API void* refh_octree_create(uint32_t slots) { return new RefOctree(slots); }

@@ -2,7 +2,7 @@
 // tensors.h, AMR.h, BSSN.h, SimpleWave.h) compile unmodified with gcc/nvcc on Linux.
 //
 // TEST INFRASTRUCTURE ONLY.  Part of the oracle: this file is used to build the
-// reference checker library under oracle/_ref and is never linked into the product.
+// reference-build library under oracle/_ref and is never linked into the product.
 //
 // The reference's CUDA_memory.h (smart buffers) and image_process.h (PNG output)
 // contain MSVC-only constructs (std::exception("msg"), members of a dependent

@@ -88,7 +88,7 @@ def available(cfg: str = "n28p2") -> bool:
 
 
 def load(cfg: str = "n28p2") -> ctypes.CDLL:
-    """Load (building first if needed and possible) the checker library for a configuration."""
+    """Load (building first if needed and possible) the reference-build library for a configuration."""
     if cfg in _LIBS:
         return _LIBS[cfg]
     path = build_ref.lib_path(cfg)

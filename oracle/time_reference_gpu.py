@@ -1,6 +1,6 @@
 """Time the reference's own CUDA plugin (BSSN_AMR_data::timestep, BSSN.h:104-171) on this GPU.
 
-Test infrastructure beside the checker library: it drives the reference's unmodified headers,
+Test infrastructure beside the reference-build library: it drives the reference's unmodified headers,
 compiled for sm_103a into oracle/_ref/libamr_ref_<cfg>.so by oracle/build_ref.py, through the
 harness entry points refd_bssn_*.  The workload is the benchmark's: a uniform octree of the given
 depth (3: 512 leaf + 73 parent domains), domains of 16^3 cells with padding 3 (or the reference's

@@ -35,8 +35,8 @@ def _ref(cfg: str):
     from oracle import reflib
     try:
         return reflib.load(cfg)
-    except Exception as e:  # the checker library needs the staged reference headers
-        pytest.skip(f"reference checker {cfg} unavailable: {e}")
+    except Exception as e:  # the reference-build library needs the staged reference headers
+        pytest.skip(f"reference-build library {cfg} unavailable: {e}")
 
 
 @pytest.fixture(scope="session")

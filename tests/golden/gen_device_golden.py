@@ -1,6 +1,6 @@
 """Generate the device-side golden fixtures from the reference's own CUDA kernels.
 
-Runs on a GPU machine where the reference checker libraries build (oracle/build_ref.py).  For
+Runs on a GPU machine where the reference-build libraries build (oracle/build_ref.py).  For
 every case it runs the reference's kernels (through oracle/ref_harness.cu) on the seeded inputs
 of tests/golden/cases.py, and the CPU oracle on the same inputs, and writes
 

@@ -1,6 +1,6 @@
 """The benchmark script's command line and its CPU arm (no GPU needed).
 
-The GPU arm runs only on a GPU machine; here the script must at least compile, and `--impl reference`
+The GPU arm runs only where a GPU is visible; here the script must at least compile, and `--impl reference`
 (the oracle's restatement of the timestep on the host cores) must print one JSON line with the
 benchmark contract's keys.
 """

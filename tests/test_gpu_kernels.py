@@ -1,7 +1,7 @@
 """GPU parity of every operator kernel.
 
 Each kernel of libamr_gb300.so runs on seeded inputs (tests/golden/cases.py) and is compared
-  * with the reference's own kernel on the same inputs, run through the reference checker
+  * with the reference's own kernel on the same inputs, run through the reference-build library
     library (oracle/_ref, the reference's headers compiled with its Release flags), and
   * with the CPU oracle (oracle/amr_oracle.c).
 Integer/codec outputs must be bit-identical.  Two documented exceptions:
@@ -128,7 +128,7 @@ def test_codec_noise_rounding(am, cuda, orc):
     am.ops.cf3_encode(torch.from_numpy(xyz).cuda(), out, torch.from_numpy(seeds).cuda())
     ref = ref_lib("n28p2")
     if ref is None:
-        pytest.skip("reference checker unavailable")
+        pytest.skip("reference-build library unavailable")
     r = torch.zeros(len(seeds), dtype=torch.int32, device="cuda")
     xd, sd = torch.from_numpy(xyz).cuda(), torch.from_numpy(seeds).cuda()   # alive while the kernel runs
     assert ref.refd_cf3_encode_seeded(xd.data_ptr(), sd.data_ptr(), len(seeds), r.data_ptr()) == 0
