@@ -65,15 +65,15 @@ def tree_random(o, depth: int, p_refine: float = 0.3, seed: int = 0):
     rng = np.random.default_rng(seed)
     level = [0]
     for d in range(depth):
-        nxt = []
-        for p in level:
-            if d > 0 and rng.random() >= p_refine:
-                continue
-            for c in range(8):
-                idx = o.state()["first_free"]
-                o.add_node(p, c)
-                nxt.append(idx)
-        level = nxt
+        chosen = [p for p in level if d == 0 or rng.random() < p_refine]
+        if hasattr(o, "add_nodes"):   # one batch per level: the same slots as the calls one by one
+            o.add_nodes([p for p in chosen for _ in range(8)], [c for _ in chosen for c in range(8)])
+        else:
+            for p in chosen:
+                for c in range(8):
+                    o.add_node(p, c)
+        ch = o.state()["children"]
+        level = [int(ch[p * 8 + c]) for p in chosen for c in range(8)]
 
 
 def tree_root(o):
