@@ -406,6 +406,11 @@ def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool, depth: int 
         if name == "batched":
             gw[name].update({k: v for k, v in sim.constraint_norms().items() if k != "cells"})
             gw[name]["finest_steps"] = (1 << depth) * (steps + 1)
+            gbs = evolution_bytes_per_root_step(sim.state(), 16) / (ms / steps / 1e3) / 1e9
+            pk = peaks()
+            gw[name]["roofline"] = {"bound": "hbm", "achieved": gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                    "frac": gbs / pk["hbm_gbs"], "peak_source": pk["source"],
+                                    "bytes": "algorithmic bytes of the whole root step (bench.evolution_bytes_per_root_step)"}
         sim.close()
     if plain:
         gw["speedup"] = gw["batched"]["value"] / gw["plain"]["value"]
@@ -420,6 +425,25 @@ def gauge_wave_report(am, cases, bmode: int, cpu: bool, plain: bool, depth: int 
         except Exception as e:   # no fixture or oracle library
             gw["cpu_fp64"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
     return gw
+
+
+def evolution_bytes_per_root_step(st, n: int, p: int = 3) -> float:
+    """Algorithmic HBM bytes of one root step of the BSSN evolution: every evolved domain active at a
+    substep (covered parents included) does, per RK stage, a derivative pass (24 fields read once,
+    93 derivative planes written: 117 planes of n^3 floats) and an update (93 derivative planes and
+    the 24 fields read, plus after the first stage the step-start values and the accumulator; the
+    24 fields written, plus the accumulator in stages 1-3: 165 + 213 + 213 + 189 planes over the
+    four stages), four ghost fills (every ghost cell of the 24 fields read once and written once)
+    and one restriction (the padded state of the 24 fields copied)."""
+    t = n + 2 * p
+    used, pos, md = st["used_slots"], st["positions"], st["max_depth"]
+    per_domain = (4 * 117 + 165 + 213 + 213 + 189) * n ** 3 * 4 + 4 * (t ** 3 - n ** 3) * 24 * 8 + t ** 3 * 24 * 8
+    active = 0
+    for k in range(used):
+        q = int(pos[k])
+        if q != 0xFFFFFFFF:
+            active += 1 << (q >> 27)   # a depth-d domain is active at 2^d of the 2^max_depth substeps
+    return float(active * per_domain)
 
 
 def leaf_zone_cycles_of_substep(st, n: int, s: int) -> int:
