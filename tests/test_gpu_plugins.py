@@ -139,7 +139,7 @@ def test_bssn_timestep_matches_reference_plugin(am, cuda, ref16, steps):
     sim.close()
 
 
-@pytest.mark.parametrize("n,p,tree", [(16, 3, "uneven"), (32, 3, "uneven"), (16, 3, "root")])
+@pytest.mark.parametrize("n,p,tree", [(16, 3, "uneven"), (32, 3, "uneven"), (28, 2, "uneven"), (16, 3, "root")])
 def test_bssn_timestep_matches_oracle(am, cuda, orc, n, p, tree):
     """One batched timestep (the fused pass; half-plane tiles at 32^3) against the oracle."""
     cfg = am.Config(n, p, 100.0)
