@@ -1,7 +1,7 @@
 // kernels_stencil.cu -- finite-difference stencils on padded domains (sm_103a).
 //
-// A persistent grid works through units of domains (whole domains, or z-ranges of them to fill a
-// last round).  A unit's padded z-planes are streamed through a shared-memory ring with 1-D TMA
+// A persistent grid works through units of domains (whole domains, or z-ranges of them to fill the
+// last wave of CTAs).  A unit's padded z-planes are streamed through a shared-memory ring with 1-D TMA
 // bulk copies (cp.async.bulk, one copy per plane and component, completion on an mbarrier per ring
 // slot); thread (x, y) computes the interior cell (x, y, z) of every plane, so each plane is read
 // from HBM once per unit and every stencil tap comes from shared memory.  k_stencil (one operator)

@@ -1,6 +1,6 @@
 // ref_harness.cu -- extern "C" access to the reference's own code for parity checks.
 //
-// TEST INFRASTRUCTURE ONLY: this builds the checker library oracle/_ref/libamr_ref_<cfg>.so
+// TEST INFRASTRUCTURE ONLY: this builds the reference-build library oracle/_ref/libamr_ref_<cfg>.so
 // from the reference's unmodified headers (staged by oracle/build_ref.py).  Only the
 // tests, the smoke check and the benchmark's reference leg load it; the product never does.
 //

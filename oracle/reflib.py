@@ -1,4 +1,4 @@
-"""ctypes access to the reference checker library (oracle/_ref/libamr_ref_<cfg>.so).
+"""ctypes access to the reference-build library (oracle/_ref/libamr_ref_<cfg>.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
 reference leg.  The library wraps the reference's own code; see oracle/ref_harness.cu.

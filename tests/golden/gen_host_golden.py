@@ -1,6 +1,6 @@
 """Generate the host-side golden fixture from the reference's own host code.
 
-Runs on a machine with the reference sources (the checker library oracle/_ref/libamr_ref_n28p2.so
+Runs on a machine with the reference sources (the reference-build library oracle/_ref/libamr_ref_n28p2.so
 is built from them by oracle/build_ref.py; no GPU is needed: only its refh_* entry points, which
 run the reference's __host__ code, are called).  Writes <out>/host_golden.npz with
 
