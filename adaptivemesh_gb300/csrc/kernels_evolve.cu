@@ -321,9 +321,15 @@ __device__ __forceinline__ void rk_update(const EvoArgs& a, int f, uint64_t pi, 
 // contiguous bytes of the inner layout each, counted on one mbarrier.  Every thread meanwhile
 // issues 4-byte asynchronous copies (cp.async) of its cell's fields and their step-start values
 // from the padded layout, and waits for its own.  Consecutive threads read consecutive words.
-constexpr int kRhsCells = 64;   // 42 KB of inputs per CTA: 5 CTAs per SM (128 cells: 2; 539 against 480 us)
-constexpr int kRhsPlanes = BSSN_ND + 3 * BSSN_NF;   // derivatives, fields, step-start values, accumulator
-constexpr size_t kRhsSmem = (size_t)kRhsPlanes * kRhsCells * 4u + 16u;
+// Stage 1 stages the derivatives and fields, stages 2 and 3 also the step-start values and the
+// accumulator, stage 4 the accumulator only (it updates from it): 30, 42 and 36 KB per CTA, so
+// 6, 5 and 6 CTAs per SM (128 cells at stages 2-3: 2 CTAs per SM, 539 against 480 us).
+constexpr int kRhsCells = 64;
+__host__ __device__ constexpr int rhs_planes(int stage) {   // derivatives, fields, [step-start values], [accumulator]
+    return BSSN_ND + BSSN_NF + (stage == 2 || stage == 3 ? 2 * BSSN_NF : (stage == 4 ? BSSN_NF : 0));
+}
+constexpr size_t rhs_smem(int stage) { return (size_t)rhs_planes(stage) * kRhsCells * 4u + 16u; }
+constexpr size_t kRhsSmem = rhs_smem(2);   // the largest
 
 __device__ __forceinline__ void cp_async4(float* dst_smem, const float* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
@@ -338,18 +344,19 @@ __global__ void __launch_bounds__(kRhsCells) k_evo_rhs_bssn(const __grid_constan
     constexpr uint32_t CHUNKS = (uint32_t)(N * N * N / kRhsCells);
     static_assert((N * N * N) % kRhsCells == 0 && (kRhsCells * 4) % 16 == 0, "whole, aligned chunks per domain");
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    const bool later = a.stage != 1;                        // stages 2-4 read the accumulator
+    const bool start = a.stage == 2 || a.stage == 3;        // stages 2-3 the step-start state
     float* sd = reinterpret_cast<float*>(smem_raw);   // [BSSN_ND][C] derivatives
     float* su = sd + (size_t)BSSN_ND * C;              // [BSSN_NF][C] fields (stored form)
-    float* so = su + (size_t)BSSN_NF * C;              // [BSSN_NF][C] step-start values (stages 2-4)
-    float* sa = so + (size_t)BSSN_NF * C;              // [BSSN_NF][C] RK accumulator (stages 2-4)
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sa + (size_t)BSSN_NF * C);
+    float* so = su + (size_t)BSSN_NF * C;              // [BSSN_NF][C] step-start values (stages 2-3)
+    float* sa = so + (start ? (size_t)BSSN_NF * C : 0u);   // [BSSN_NF][C] RK accumulator (stages 2-4)
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sa + (later ? (size_t)BSSN_NF * C : 0u));
     const uint32_t tid = threadIdx.x;
     const uint32_t item = blockIdx.x / CHUNKS, chunk = blockIdx.x % CHUNKS;
     if (item >= a.n_items) return;   // the whole CTA
     const uint32_t slot = a.items[item];
     const uint32_t cell = chunk * (uint32_t)kRhsCells + tid;
     const uint64_t ii0 = (uint64_t)slot * N * N * N + chunk * (uint32_t)kRhsCells;
-    const bool later = a.stage != 1;   // stages 2-4 read the step-start state and the accumulator
     if (tid == 0) {
         mbar_init(bar, 1);
         mbar_fence_init();
@@ -368,7 +375,7 @@ __global__ void __launch_bounds__(kRhsCells) k_evo_rhs_bssn(const __grid_constan
 #pragma unroll
     for (int f = 0; f < BSSN_NF; f++) {
         cp_async4(su + f * C + tid, a.fields[f] + pi);
-        if (later) cp_async4(so + f * C + tid, a.old_f[f] + pi);
+        if (start) cp_async4(so + f * C + tid, a.old_f[f] + pi);
     }
     const int depth = pos_depth(a.positions[slot]);
     const float dt = a.dt0 / (float)(1u << depth);
@@ -396,11 +403,11 @@ __global__ void __launch_bounds__(kRhsCells) k_evo_rhs_bssn(const __grid_constan
 #pragma unroll
     for (int f = 0; f < BSSN_NF; f++) {
         const float r = rhs[f] + dv(D_EXTRA + f);
-        const float uo = later ? so[f * C + tid] : su[f * C + tid];   // the stored form
         float v;
         if (a.stage == 4) {
             v = fmaf(c_out, r, sa[f * C + tid]);
         } else {
+            const float uo = start ? so[f * C + tid] : su[f * C + tid];   // the stored form
             a.acc[f][ii] = fmaf(c_acc, r, later ? sa[f * C + tid] : uo);
             v = fmaf(c_out, r, uo);
         }
@@ -971,7 +978,8 @@ static cudaError_t rhs_t(const EvoArgs& a, cudaStream_t st) {
         static std::atomic<uint64_t> configured{0};
         const cudaError_t e = ensure_smem_limit(k_evo_rhs_bssn<N>, kRhsSmem, configured);
         if (e != cudaSuccess) return e;
-        k_evo_rhs_bssn<N><<<(unsigned)(total / kRhsCells), kRhsCells, kRhsSmem, st>>>(a);
+        if (a.stage < 1 || a.stage > 4) return cudaErrorInvalidValue;
+        k_evo_rhs_bssn<N><<<(unsigned)(total / kRhsCells), kRhsCells, rhs_smem(a.stage), st>>>(a);
     } else {
         k_evo_rhs_wave<N><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(a);
     }

@@ -431,13 +431,13 @@ def evolution_bytes_per_root_step(st, n: int, p: int = 3) -> float:
     """Algorithmic HBM bytes of one root step of the BSSN evolution: every evolved domain active at a
     substep (covered parents included) does, per RK stage, a derivative pass (24 fields read once,
     93 derivative planes written: 117 planes of n^3 floats) and an update (93 derivative planes and
-    the 24 fields read, plus after the first stage the step-start values and the accumulator; the
-    24 fields written, plus the accumulator in stages 1-3: 165 + 213 + 213 + 189 planes over the
-    four stages), four ghost fills (every ghost cell of the 24 fields read once and written once)
-    and one restriction (the padded state of the 24 fields copied)."""
+    the 24 fields read, plus the step-start values in stages 2-3 and the accumulator in stages 2-4;
+    the 24 fields written, plus the accumulator in stages 1-3: 165 + 213 + 213 + 165 planes over
+    the four stages), four ghost fills (every ghost cell of the 24 fields read once and written
+    once) and one restriction (the padded state of the 24 fields copied)."""
     t = n + 2 * p
     used, pos, md = st["used_slots"], st["positions"], st["max_depth"]
-    per_domain = (4 * 117 + 165 + 213 + 213 + 189) * n ** 3 * 4 + 4 * (t ** 3 - n ** 3) * 24 * 8 + t ** 3 * 24 * 8
+    per_domain = (4 * 117 + 165 + 213 + 213 + 165) * n ** 3 * 4 + 4 * (t ** 3 - n ** 3) * 24 * 8 + t ** 3 * 24 * 8
     active = 0
     for k in range(used):
         q = int(pos[k])
