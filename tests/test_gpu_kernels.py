@@ -588,3 +588,49 @@ def test_ghost_fill_special_values(am, cuda, orc, kind):
         assert_same_nan(host(sim.tensor(am.Sim.OLD, k)[: used * t ** 3]), old6[k], f"{kind} timestep old{k}")
         assert_same_nan(host(sim.tensor(am.Sim.NEW, k)[: used * t ** 3]), new6[k], f"{kind} timestep new{k}")
     sim.close()
+
+
+# ----------------------------------------------------------------------------- empty inputs
+@pytest.mark.parametrize("cfgname", ["n16p3", "n28p2"])
+def test_empty_inputs_are_no_ops(am, cuda, cfgname):
+    """Zero domains (used = 0) and zero elements are accepted and touch nothing.  The reference's
+    wrappers size their grids from `used` (AMR.h:880-900, 998-1018, 1280-1302), so with no domains
+    they launch nothing that writes; this library returns AMR_OK without a launch, the device
+    status stays clean, and every buffer keeps its contents.  An extremum of nothing has no value
+    and is rejected (find_maximum_val would read data[0], parallel.h:239-251)."""
+    import torch
+    n, p = CFGS[cfgname]
+    cfg = am.Config(n, p, OUTER)
+    ops = am.ops
+    f = torch.full((256,), 7.0, device="cuda")
+    f2 = torch.full((256,), 9.0, device="cuda")
+    u = torch.full((256,), 5, dtype=torch.int32, device="cuda")
+    u2 = torch.full((256,), 6, dtype=torch.int32, device="cuda")
+    fo = torch.full((256,), 3.0, device="cuda")
+    pos = torch.zeros(8, dtype=torch.int32, device="cuda")
+    ch = torch.full((64,), -1, dtype=torch.int32, device="cuda")
+    bd = torch.zeros(48, dtype=torch.int64, device="cuda")
+    empty_f, empty_u = fo[:0], u2[:0]   # torch gives zero-element tensors a null address
+    before = [x.clone() for x in (f, f2, u, u2, fo)]
+    ops.cf3_encode(empty_f, empty_u)
+    ops.cf3_decode(empty_u, empty_f)
+    ops.differentiate(cfg, f, u, u2, pos, 0, 0, 0, 5)
+    ops.mixed_partials(cfg, f, u, pos, 0, 0, 0, 5)
+    ops.deriv_trace(cfg, u, u2, [f] * 6, fo, pos, 0, 0, 0)
+    ops.christoffel(cfg, [f] * 6, [u] * 6, 5, [u2] * 6, pos, 0, 0, 0)
+    ops.copy_boundaries(cfg, f, f2, bd, 0, 0, 0, copy_only_new=False)
+    assert am.load().amr_copy_boundaries_noalloc(ctypes.byref(cfg), f.data_ptr(), f2.data_ptr(), bd.data_ptr(),
+                                                 0, 0, 0, 0, None) == 0
+    ops.copy_new_to_old(cfg, f, f2, pos, ch, 0, 0, 0)
+    ops.wave_step(cfg, False, f, u, u2, f2, pos, 0, 0, 0)
+    ops.wave_step(cfg, True, f, u, u2, f2, pos, 0, 0, 0)
+    ops.criterion(cfg, u, u2, fo, pos, 0, 0, 0)
+    assert ops.field_norms(cfg, f, pos, ch, 0) == {"sum": 0.0, "sum_sq": 0.0, "max_abs": 0.0, "cells": 0}
+    lib = am.load()
+    assert lib.amr_inclusive_scan(am.DTYPE_FLOAT32, 1, fo.data_ptr(), 0, None) == 0
+    res = np.zeros(1, np.float32)
+    assert lib.amr_reduce_max(am.DTYPE_FLOAT32, 1, fo.data_ptr(), 0, res.ctypes.data, None) == am.ERR_INVALID
+    torch.cuda.synchronize()
+    assert am.load().amr_device_status(None) == 0
+    for a, b in zip(before, (f, f2, u, u2, fo)):
+        assert torch.equal(a, b)
