@@ -53,7 +53,11 @@ struct EvoRestrictArgs {
     uint32_t n_items;
     uint32_t n, p, t;
     int nf;
+    int fgroup;   // fields per CTA: the grid's y extent is ceil(nf / fgroup)
 };
+// Fields per CTA when restricting domains with children: each covered cell costs 64 loads per field,
+// so those CTAs take few fields and many run side by side (the leaves' straight copies take all).
+constexpr int kEvoRestrictGroup = 4;
 
 // Tile features of the learned estimator and the plain criterion's indicator, per listed slot
 // (kernels_evolve.cu, k_evo_features): features [slot][3][8^3], indicator [slot].

@@ -140,18 +140,25 @@ public:
             evolved[i] = 1;
             if (nchild == 0) leaves.push_back(i);
         }
-        std::vector<uint32_t> all;
-        act_off.assign(nsub, 0); act_cnt.assign(nsub, 0); evo_off.assign(nsub, 0); evo_cnt.assign(nsub, 0);
+        std::vector<uint8_t> is_leaf(tree.max_slots(), 0);
+        for (uint32_t i : leaves) is_leaf[i] = 1;
+        std::vector<uint32_t> all, sub;
+        act_off.assign(nsub, 0); act_cnt.assign(nsub, 0); act_leaves.assign(nsub, 0);
+        evo_off.assign(nsub, 0); evo_cnt.assign(nsub, 0);
         for (uint32_t s = 0; s < nsub; s++) {
-            act_off[s] = (uint32_t)all.size();
+            sub.clear();   // the substep's active domains in slot order
             for (uint32_t i = 0; i < used; i++) {
                 const int d = pos_depth_host(tree.positions()[i]);
-                if (d != -1 && (s & ((1u << (md - (uint32_t)d)) - 1u)) == 0u) all.push_back(i);
+                if (d != -1 && (s & ((1u << (md - (uint32_t)d)) - 1u)) == 0u) sub.push_back(i);
             }
+            // the restriction's list: the leaves (straight copies) first, then the domains with children
+            act_off[s] = (uint32_t)all.size();
+            for (uint32_t i : sub) if (is_leaf[i]) all.push_back(i);
+            act_leaves[s] = (uint32_t)all.size() - act_off[s];
+            for (uint32_t i : sub) if (!is_leaf[i]) all.push_back(i);
             act_cnt[s] = (uint32_t)all.size() - act_off[s];
             evo_off[s] = (uint32_t)all.size();
-            for (uint32_t k = act_off[s]; k < act_off[s] + act_cnt[s]; k++)
-                if (evolved[all[k]]) all.push_back(all[k]);
+            for (uint32_t i : sub) if (evolved[i]) all.push_back(i);
             evo_cnt[s] = (uint32_t)all.size() - evo_off[s];
         }
         all_evolved_off = (uint32_t)all.size();
@@ -190,6 +197,7 @@ public:
         g.n_items = act_cnt[s];
         g.n = dims.n; g.p = dims.p; g.t = dims.t;
         g.nf = nf;
+        g.fgroup = nf;
         (void)md;
         if (mode == AMR_MODE_PLAIN) {   // one launch per domain
             const uint32_t* base = g.items;
@@ -200,7 +208,15 @@ public:
             }
             return AMR_OK;
         }
-        return check(launch_evo_restrict(g, stream));
+        // the leaves with every field of a plane per CTA, then the domains with children with
+        // kEvoRestrictGroup fields per CTA
+        g.n_items = act_leaves[s];
+        if (g.n_items && (st = check(launch_evo_restrict(g, stream)))) return st;
+        g.items = d_lists + act_off[s] + act_leaves[s];
+        g.n_items = act_cnt[s] - act_leaves[s];
+        g.fgroup = kEvoRestrictGroup;
+        if (g.n_items && (st = check(launch_evo_restrict(g, stream)))) return st;
+        return AMR_OK;
     }
     int modify_nodes() override { return AMR_OK; }
     int predictor() override {
@@ -591,7 +607,7 @@ private:
     double* d_part = nullptr;
     double* d_norms = nullptr;
     bool lists_valid = false;
-    std::vector<uint32_t> act_off, act_cnt, evo_off, evo_cnt, leaves;
+    std::vector<uint32_t> act_off, act_cnt, act_leaves, evo_off, evo_cnt, leaves;
     uint32_t all_evolved_off = 0, all_evolved_cnt = 0, leaves_off = 0;
     uint32_t deriv_zs = 0;   // the derivative pass's slab depth (0: the default; amr_sim_autotune)
     cudaGraphExec_t graph_exec = nullptr;

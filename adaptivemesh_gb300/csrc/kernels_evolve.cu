@@ -627,10 +627,12 @@ __global__ void __launch_bounds__(256, 4) k_evo_ghost(const __grid_constant__ Ev
 // centre (the corner shared by 2x2x2 child cells), by the 4-point midpoint rule (-1, 9, 9, -1)/16 along
 // each axis (child cells 2c-1 .. 2c+2, the child's ghost layer at its faces included).  The reference
 // averages the 2x2x2 block (AMR.h:961-996), a second-order rule.
+// A CTA per (slot, plane z, group of g.fgroup fields).
 __global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ EvoRestrictArgs g) {
     const uint32_t t = g.t, p = g.p, n = g.n, hn = n / 2;
     const uint32_t item = blockIdx.x / t, z = blockIdx.x % t;
-    if (item >= g.n_items) return;
+    const int fb = (int)blockIdx.y * g.fgroup, fe = min(g.nf, fb + g.fgroup);   // this CTA's fields
+    if (item >= g.n_items || fb >= fe) return;
     const uint32_t slot = g.items[item];
     const uint64_t cells = (uint64_t)t * t * t;
     bool leaf = true;
@@ -641,19 +643,19 @@ __global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ Ev
         // (planes are t^2 floats, t^2 * 4 a multiple of 16, every plane 16-byte aligned)
         const uint32_t q4 = t * t / 4u;
         const uint64_t base4 = (slot * cells + (uint64_t)z * t * t) / 4u;
-        const uint32_t total = (uint32_t)g.nf * q4;
+        const uint32_t total = (uint32_t)(fe - fb) * q4;
         constexpr uint32_t U = 4;   // loads in flight per thread before their stores
         for (uint32_t e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
             float4 v[U];
 #pragma unroll
             for (uint32_t u = 0; u < U; u++) {
                 const uint32_t e = e0 + u * blockDim.x;
-                if (e < total) v[u] = reinterpret_cast<const float4*>(g.new_f[e / q4])[base4 + e % q4];
+                if (e < total) v[u] = reinterpret_cast<const float4*>(g.new_f[fb + (int)(e / q4)])[base4 + e % q4];
             }
 #pragma unroll
             for (uint32_t u = 0; u < U; u++) {
                 const uint32_t e = e0 + u * blockDim.x;
-                if (e < total) reinterpret_cast<float4*>(g.old_f[e / q4])[base4 + e % q4] = v[u];
+                if (e < total) reinterpret_cast<float4*>(g.old_f[fb + (int)(e / q4)])[base4 + e % q4] = v[u];
             }
         }
         return;
@@ -667,21 +669,21 @@ __global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ Ev
         // fields in groups, every load of a group before its stores (old and new are distinct buffers)
         constexpr int G = 8;
         if (ch == -1) {
-            for (int f0 = 0; f0 < g.nf; f0 += G) {
+            for (int f0 = fb; f0 < fe; f0 += G) {
                 float v[G];
 #pragma unroll
                 for (int q = 0; q < G; q++)
-                    if (f0 + q < g.nf) v[q] = g.new_f[f0 + q][o];
+                    if (f0 + q < fe) v[q] = g.new_f[f0 + q][o];
 #pragma unroll
                 for (int q = 0; q < G; q++)
-                    if (f0 + q < g.nf) g.old_f[f0 + q][o] = v[q];
+                    if (f0 + q < fe) g.old_f[f0 + q][o] = v[q];
             }
             continue;
         }
         const uint32_t cx = ((x - p) * 2u) % n + p, cy = ((y - p) * 2u) % n + p, cz = ((z - p) * 2u) % n + p;
         const uint64_t base = (uint64_t)ch * cells + ((uint64_t)(cz - 1) * t + (cy - 1)) * t + (cx - 1);
         constexpr int GI = 2;
-        for (int f0 = 0; f0 < g.nf; f0 += GI) {
+        for (int f0 = fb; f0 < fe; f0 += GI) {
             float acc[GI];
 #pragma unroll
             for (int q = 0; q < GI; q++) acc[q] = 0.f;
@@ -691,7 +693,7 @@ __global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ Ev
                 for (int k1 = 0; k1 < 4; k1++) {
 #pragma unroll
                     for (int q = 0; q < GI; q++) {
-                        const float* v = g.new_f[min(f0 + q, g.nf - 1)];
+                        const float* v = g.new_f[min(f0 + q, fe - 1)];
                         float row = 0.f;
 #pragma unroll
                         for (int k0 = 0; k0 < 4; k0++) row = fmaf(w4[k0], v[base + ((uint64_t)k2 * t + k1) * t + k0], row);
@@ -700,7 +702,7 @@ __global__ void __launch_bounds__(256) k_evo_restrict(const __grid_constant__ Ev
                 }
 #pragma unroll
             for (int q = 0; q < GI; q++)
-                if (f0 + q < g.nf) g.old_f[f0 + q][o] = acc[q];
+                if (f0 + q < fe) g.old_f[f0 + q][o] = acc[q];
         }
     }
 }
@@ -996,7 +998,8 @@ cudaError_t launch_evo_rhs(const EvoArgs& a, cudaStream_t st) {
 
 cudaError_t launch_evo_restrict(const EvoRestrictArgs& g, cudaStream_t st) {
     if (g.n_items == 0) return cudaSuccess;
-    k_evo_restrict<<<g.n_items * g.t, 256, 0, st>>>(g);
+    if (g.nf <= 0 || g.nf > kMaxFields || g.fgroup <= 0) return cudaErrorInvalidValue;
+    k_evo_restrict<<<dim3(g.n_items * g.t, (unsigned)((g.nf + g.fgroup - 1) / g.fgroup)), 256, 0, st>>>(g);
     return cudaGetLastError();
 }
 
